@@ -1,0 +1,239 @@
+"""Python mirror of the fmm-blis FMM GEMM interface over the GB300 C ABI.
+
+The compute path is the CUDA library ``libfmm_gb300.so`` (include/fmm_gb300.h);
+this module only loads it with ctypes and converts arguments. There is no
+CPU fallback: if the library is missing, ``lib()`` raises.
+
+Names follow the reference's interface (frame/include/bli_fmm.h:61-89):
+``new_fmm``/``free_fmm`` read and release a coefficient algorithm,
+``STRASSEN_FMM`` is the built-in Strassen <2,2,2>, ``bli_strassen_ab_ex``
+computes C += A*B through one FMM level (host arrays, like the reference's
+obj_t call), ``bl_clock`` is the monotonic timer. The device-resident forms are
+``dgemm`` (plain FP64) and ``split_dgemm`` (BF16 digit slices on the tensor
+cores), both taking column-major CUDA tensors.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from pathlib import Path
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "libfmm_gb300.so"
+
+FMM_OK = 0
+_STATUS = {
+    0: "ok", 1: "invalid argument", 2: "coefficient file cannot be opened",
+    3: "coefficient file malformed", 4: "allocation failed", 5: "CUDA call failed",
+    6: "unsupported size or option", 7: "coefficients violate the Brent equations",
+    8: "kernel reported an error (bounded wait expired)", 9: "workspace too small",
+}
+
+
+class FmmError(RuntimeError):
+    def __init__(self, status: int, what: str = ""):
+        self.status = status
+        super().__init__(f"{what}: {_STATUS.get(status, 'unknown status')} (status {status})")
+
+
+class FmmT(ctypes.Structure):
+    """Same layout as the reference's fmm_t (plugin/bli_plugin_fmm_blis.h:58-68)."""
+
+    _fields_ = [
+        ("m_tilde", ctypes.c_int),
+        ("n_tilde", ctypes.c_int),
+        ("k_tilde", ctypes.c_int),
+        ("R", ctypes.c_int),
+        ("U", ctypes.POINTER(ctypes.c_int)),
+        ("V", ctypes.POINTER(ctypes.c_int)),
+        ("W", ctypes.POINTER(ctypes.c_int)),
+    ]
+
+    def coeffs(self):
+        """(U, V, W) as lists of rows (row q, column r)."""
+        R = self.R
+        a = self.m_tilde * self.k_tilde
+        b = self.k_tilde * self.n_tilde
+        c = self.m_tilde * self.n_tilde
+        U = [[self.U[q * R + r] for r in range(R)] for q in range(a)]
+        V = [[self.V[q * R + r] for r in range(R)] for q in range(b)]
+        W = [[self.W[q * R + r] for r in range(R)] for q in range(c)]
+        return U, V, W
+
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    """The loaded CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise RuntimeError(f"{LIB_PATH} is missing: build it with fmm_blis_gb300.build.build()")
+    L = ctypes.CDLL(str(LIB_PATH))
+    i64, dbl, vp, ci = ctypes.c_int64, ctypes.c_double, ctypes.c_void_p, ctypes.c_int
+    pf = ctypes.POINTER(FmmT)
+    L.new_fmm.restype = FmmT
+    L.new_fmm.argtypes = [ctypes.c_char_p]
+    L.free_fmm.restype = None
+    L.free_fmm.argtypes = [FmmT]
+    L.fmm_load.restype = ci
+    L.fmm_load.argtypes = [ctypes.c_char_p, pf]
+    L.fmm_check_brent.restype = ci
+    L.fmm_check_brent.argtypes = [pf, ctypes.POINTER(ctypes.c_long)]
+    L.fmm_kron.restype = ci
+    L.fmm_kron.argtypes = [pf, pf, pf]
+    L.fmm_copy.restype = ci
+    L.fmm_copy.argtypes = [pf, pf]
+    L.fmm_status_string.restype = ctypes.c_char_p
+    L.fmm_status_string.argtypes = [ci]
+    L.bl_clock.restype = dbl
+    L.bl_clock.argtypes = []
+    L.fmm_gpu_dgemm.restype = ci
+    L.fmm_gpu_dgemm.argtypes = [pf, ci, i64, i64, i64, dbl, vp, i64, vp, i64, dbl, vp, i64, vp]
+    L.fmm_gpu_strassen_ab_ex.restype = ci
+    L.fmm_gpu_strassen_ab_ex.argtypes = [dbl, vp, i64, vp, i64, dbl, vp, i64, i64, i64, i64, FmmT]
+    L.fmm_gpu_strassen_ab.restype = ci
+    L.fmm_gpu_strassen_ab.argtypes = [dbl, vp, i64, vp, i64, dbl, vp, i64, i64, i64, i64]
+    L.fmm_gpu_split_workspace_size.restype = ctypes.c_size_t
+    L.fmm_gpu_split_workspace_size.argtypes = [pf, ci, i64, i64, i64, ci]
+    L.fmm_gpu_split_dgemm.restype = ci
+    L.fmm_gpu_split_dgemm.argtypes = [pf, ci, i64, i64, i64, dbl, vp, i64, vp, i64, dbl, vp, i64, ci, vp,
+                                      ctypes.c_size_t, vp]
+    L.fmm_gpu_launch_count.restype = ctypes.c_uint64
+    L.fmm_gpu_launch_count.argtypes = []
+    L.fmm_gpu_take_device_error.restype = ci
+    L.fmm_gpu_take_device_error.argtypes = []
+    _lib = L
+    return L
+
+
+def _check(status: int, what: str) -> None:
+    if status != FMM_OK:
+        raise FmmError(status, what)
+
+
+# ------------------------------------------------------------ algorithms --
+
+def new_fmm(path: str | os.PathLike) -> FmmT:
+    """Reads a coefficient file (frame/base/bli_read_fmm.c:24-80); raises on error."""
+    f = FmmT()
+    _check(lib().fmm_load(str(path).encode(), ctypes.byref(f)), f"new_fmm({path})")
+    return f
+
+
+def free_fmm(f: FmmT) -> None:
+    """Releases an algorithm from new_fmm/kron (frame/base/bli_read_fmm.c:82-86)."""
+    lib().free_fmm(f)
+
+
+def strassen_fmm() -> FmmT:
+    """The built-in Strassen <2,2,2> algorithm (frame/base/bli_strassen_ab.c:12-24)."""
+    return FmmT.in_dll(lib(), "STRASSEN_FMM")
+
+
+def check_brent(f: FmmT) -> int:
+    """Number of violated Brent equations (0 for a correct algorithm)."""
+    bad = ctypes.c_long(0)
+    lib().fmm_check_brent(ctypes.byref(f), ctypes.byref(bad))
+    return bad.value
+
+
+def kron(outer: FmmT, inner: FmmT) -> FmmT:
+    """Two levels as one flat algorithm (free with free_fmm)."""
+    out = FmmT()
+    _check(lib().fmm_kron(ctypes.byref(outer), ctypes.byref(inner), ctypes.byref(out)), "fmm_kron")
+    return out
+
+
+def bl_clock() -> float:
+    return lib().bl_clock()
+
+
+def launch_count() -> int:
+    """Kernels this library has launched since it was loaded."""
+    return int(lib().fmm_gpu_launch_count())
+
+
+def take_device_error() -> int:
+    return int(lib().fmm_gpu_take_device_error())
+
+
+# ------------------------------------------------------------ GPU calls --
+
+def _colmajor_ld(t, rows: int, name: str) -> int:
+    if t.dtype.__str__() != "torch.float64":
+        raise TypeError(f"{name} must be float64")
+    if not t.is_cuda:
+        raise TypeError(f"{name} must be a CUDA tensor")
+    if t.dim() != 2 or (t.shape[0] > 1 and t.stride(0) != 1):
+        raise ValueError(f"{name} must be a column-major 2-D tensor (stride(0) == 1)")
+    return max(int(t.stride(1)), max(rows, 1))
+
+
+def colmajor(t):
+    """A column-major (Fortran-order) copy/view of a 2-D torch tensor."""
+    return t.t().contiguous().t()
+
+
+def _stream_ptr(stream) -> int | None:
+    if stream is None:
+        import torch
+        return torch.cuda.current_stream().cuda_stream
+    return int(getattr(stream, "cuda_stream", stream))
+
+
+def dgemm(A, B, C, fmm: FmmT | None = None, levels: int = 1, alpha: float = 1.0, beta: float = 1.0,
+          stream=None) -> None:
+    """C := beta*C + alpha*A*B on the GPU in FP64 with `levels` levels of `fmm`
+    (fmm None or levels 0: the classical FP64 kernel). Column-major tensors."""
+    m, k = A.shape
+    k2, n = B.shape
+    if k2 != k or tuple(C.shape) != (m, n):
+        raise ValueError("shape mismatch")
+    lda, ldb, ldc = _colmajor_ld(A, m, "A"), _colmajor_ld(B, k, "B"), _colmajor_ld(C, m, "C")
+    pf = ctypes.byref(fmm) if fmm is not None else None
+    st = lib().fmm_gpu_dgemm(pf, levels if fmm is not None else 0, m, n, k, alpha, A.data_ptr(), lda,
+                             B.data_ptr(), ldb, beta, C.data_ptr(), ldc, _stream_ptr(stream))
+    _check(st, "fmm_gpu_dgemm")
+
+
+def split_workspace_size(m: int, n: int, k: int, fmm: FmmT | None, levels: int, slices: int) -> int:
+    pf = ctypes.byref(fmm) if fmm is not None else None
+    return int(lib().fmm_gpu_split_workspace_size(pf, levels if fmm is not None else 0, m, n, k, slices))
+
+
+def split_dgemm(A, B, C, fmm: FmmT | None = None, levels: int = 1, slices: int = 6, alpha: float = 1.0,
+                beta: float = 1.0, workspace=None, stream=None) -> None:
+    """C := beta*C + alpha*A*B from BF16 digit slices on the tensor cores.
+    `workspace` is a CUDA uint8 tensor of at least split_workspace_size bytes
+    (allocated here when None)."""
+    import torch
+    m, k = A.shape
+    k2, n = B.shape
+    if k2 != k or tuple(C.shape) != (m, n):
+        raise ValueError("shape mismatch")
+    lda, ldb, ldc = _colmajor_ld(A, m, "A"), _colmajor_ld(B, k, "B"), _colmajor_ld(C, m, "C")
+    need = split_workspace_size(m, n, k, fmm, levels, slices)
+    if workspace is None:
+        workspace = torch.empty(max(need, 256), dtype=torch.uint8, device=C.device)
+    pf = ctypes.byref(fmm) if fmm is not None else None
+    st = lib().fmm_gpu_split_dgemm(pf, levels if fmm is not None else 0, m, n, k, alpha, A.data_ptr(), lda,
+                                   B.data_ptr(), ldb, beta, C.data_ptr(), ldc, slices,
+                                   workspace.data_ptr(), workspace.numel(), _stream_ptr(stream))
+    _check(st, "fmm_gpu_split_dgemm")
+
+
+def bli_strassen_ab_ex(alpha: float, A, B, beta: float, C, fmm: FmmT) -> None:
+    """Host-array drop-in for bli_strassen_ab_ex (frame/base/bli_strassen_ab.c:123):
+    numpy float64 Fortran-order arrays, C updated in place."""
+    import numpy as np
+    for name, x in (("A", A), ("B", B), ("C", C)):
+        if x.dtype != np.float64 or not x.flags.f_contiguous:
+            raise ValueError(f"{name} must be a Fortran-ordered float64 array")
+    m, k = A.shape
+    n = B.shape[1]
+    st = lib().fmm_gpu_strassen_ab_ex(alpha, A.ctypes.data, max(m, 1), B.ctypes.data, max(k, 1), beta,
+                                      C.ctypes.data, max(m, 1), m, n, k, fmm)
+    _check(st, "fmm_gpu_strassen_ab_ex")

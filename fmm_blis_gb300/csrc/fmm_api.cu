@@ -1,0 +1,281 @@
+/*
+ * C ABI entry points (include/fmm_gb300.h): argument checks, flattening of
+ * multi-level algorithms, the per-device cache of algorithm tables, and the
+ * host-buffer drop-in for bli_strassen_ab_ex (frame/base/bli_strassen_ab.c:123).
+ */
+#include "fmm_internal.h"
+
+#include <atomic>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+namespace {
+
+std::atomic<uint64_t> g_launches{0};
+
+__device__ int g_device_error;
+
+struct CachedAlg {
+    int device;
+    std::vector<int> table;
+    int* dtab;
+    AlgView view;
+};
+
+std::mutex g_mu;
+std::vector<CachedAlg*> g_cache;
+
+int* g_err_ptr[64];
+bool g_err_init[64];
+
+bool ld_ok(int64_t ld, int64_t rows) { return ld >= (rows > 1 ? rows : 1); }
+
+std::vector<int> build_table(const fmm_t* f)
+{
+    const int R = f->R;
+    const int a = f->m_tilde * f->k_tilde, b = f->k_tilde * f->n_tilde, c = f->m_tilde * f->n_tilde;
+    std::vector<int> off_u(R + 1), off_v(R + 1), off_w(R + 1);
+    std::vector<int> eu, ev, ew;
+    for (int r = 0; r < R; ++r) {
+        off_u[r] = (int)eu.size() / 2;
+        for (int q = 0; q < a; ++q)
+            if (int x = f->U[(size_t)q * R + r]) { eu.push_back(q); eu.push_back(x); }
+        off_v[r] = (int)ev.size() / 2;
+        for (int q = 0; q < b; ++q)
+            if (int x = f->V[(size_t)q * R + r]) { ev.push_back(q); ev.push_back(x); }
+        off_w[r] = (int)ew.size() / 2;
+        for (int q = 0; q < c; ++q)
+            if (int x = f->W[(size_t)q * R + r]) { ew.push_back(q); ew.push_back(x); }
+    }
+    off_u[R] = (int)eu.size() / 2;
+    off_v[R] = (int)ev.size() / 2;
+    off_w[R] = (int)ew.size() / 2;
+    std::vector<int> t;
+    t.push_back(f->m_tilde); t.push_back(f->k_tilde); t.push_back(f->n_tilde); t.push_back(R);
+    t.insert(t.end(), off_u.begin(), off_u.end());
+    t.insert(t.end(), off_v.begin(), off_v.end());
+    t.insert(t.end(), off_w.begin(), off_w.end());
+    t.insert(t.end(), eu.begin(), eu.end());
+    t.insert(t.end(), ev.begin(), ev.end());
+    t.insert(t.end(), ew.begin(), ew.end());
+    return t;
+}
+
+void fill_view(CachedAlg* c)
+{
+    const int* t = c->table.data();
+    AlgView v;
+    v.tab = c->dtab;
+    v.htab = t;
+    v.mt = t[0]; v.kt = t[1]; v.nt = t[2]; v.R = t[3];
+    const int* ou = t + FMM_ALG_HDR;
+    const int* ov = ou + v.R + 1;
+    const int* ow = ov + v.R + 1;
+    v.max_nnz_u = v.max_nnz_v = v.max_nnz_w = 0;
+    for (int r = 0; r < v.R; ++r) {
+        v.max_nnz_u = std::max(v.max_nnz_u, ou[r + 1] - ou[r]);
+        v.max_nnz_v = std::max(v.max_nnz_v, ov[r + 1] - ov[r]);
+        v.max_nnz_w = std::max(v.max_nnz_w, ow[r + 1] - ow[r]);
+    }
+    v.avg_nnz_u = (double)ou[v.R] / v.R;
+    v.avg_nnz_v = (double)ov[v.R] / v.R;
+    v.avg_nnz_w = (double)ow[v.R] / v.R;
+    v.tab_len = (int)c->table.size();
+    c->view = v;
+}
+
+bool valid_fmm(const fmm_t* f)
+{
+    return f && f->R > 0 && f->m_tilde > 0 && f->k_tilde > 0 && f->n_tilde > 0 && f->U && f->V && f->W;
+}
+
+}  // namespace
+
+void fmm_count_launch(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+extern "C" uint64_t fmm_gpu_launch_count(void) { return g_launches.load(); }
+
+int* fmm_device_error_word(void)
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (!g_err_init[dev]) {
+        void* p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_device_error) != cudaSuccess) return nullptr;
+        g_err_ptr[dev] = (int*)p;
+        g_err_init[dev] = true;
+    }
+    return g_err_ptr[dev];
+}
+
+extern "C" int fmm_gpu_take_device_error(void)
+{
+    int v = 0, zero = 0;
+    if (cudaDeviceSynchronize() != cudaSuccess) return -1;
+    if (cudaMemcpyFromSymbol(&v, g_device_error, sizeof(int)) != cudaSuccess) return -1;
+    if (v != 0) cudaMemcpyToSymbol(g_device_error, &zero, sizeof(int));
+    return v;
+}
+
+/* flat <- levels-fold Kronecker power of fmm (levels 0: the classical
+ * 1x1x1 algorithm). *owned says whether flat's arrays must be freed. */
+int fmm_flatten(const fmm_t* fmm, int levels, fmm_t* flat, int* owned)
+{
+    static int one[1] = {1};
+    *owned = 0;
+    if (levels < 0 || levels > 4) return FMM_ERR_ARG;
+    if (levels == 0 || fmm == nullptr) {
+        *flat = fmm_t{1, 1, 1, 1, one, one, one};
+        return FMM_OK;
+    }
+    if (!valid_fmm(fmm)) return FMM_ERR_ARG;
+    if (fmm_check_brent(fmm, nullptr) != FMM_OK) return FMM_ERR_BRENT;
+    if (levels == 1) {
+        *flat = *fmm;
+        return FMM_OK;
+    }
+    fmm_t cur;
+    int rc = fmm_copy(fmm, &cur);
+    if (rc != FMM_OK) return rc;
+    for (int l = 1; l < levels; ++l) {
+        fmm_t nxt;
+        if ((long)cur.R * fmm->R > 1000000) { free_fmm(cur); return FMM_ERR_UNSUPPORTED; }
+        rc = fmm_kron(&cur, fmm, &nxt);
+        free_fmm(cur);
+        if (rc != FMM_OK) return rc;
+        cur = nxt;
+    }
+    *flat = cur;
+    *owned = 1;
+    return FMM_OK;
+}
+
+int fmm_alg_get(const fmm_t* flat, AlgView* out)
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return FMM_ERR_CUDA;
+    std::vector<int> t = build_table(flat);
+    std::lock_guard<std::mutex> lk(g_mu);
+    for (CachedAlg* c : g_cache)
+        if (c->device == dev && c->table == t) { *out = c->view; return FMM_OK; }
+    CachedAlg* c = new CachedAlg;
+    c->device = dev;
+    c->table = std::move(t);
+    c->dtab = nullptr;
+    if (cudaMalloc(&c->dtab, sizeof(int) * c->table.size()) != cudaSuccess) { delete c; return FMM_ERR_ALLOC; }
+    if (cudaMemcpy(c->dtab, c->table.data(), sizeof(int) * c->table.size(), cudaMemcpyHostToDevice) !=
+        cudaSuccess) {
+        cudaFree(c->dtab);
+        delete c;
+        return FMM_ERR_CUDA;
+    }
+    fill_view(c);
+    g_cache.push_back(c);
+    *out = c->view;
+    return FMM_OK;
+}
+
+static int check_gemm_args(int64_t m, int64_t n, int64_t k, const void* A, int64_t lda, const void* B,
+                           int64_t ldb, const void* C, int64_t ldc)
+{
+    if (m < 0 || n < 0 || k < 0) return FMM_ERR_ARG;
+    if (!ld_ok(lda, m) || !ld_ok(ldb, k) || !ld_ok(ldc, m)) return FMM_ERR_ARG;
+    if (m > 0 && n > 0 && C == nullptr) return FMM_ERR_ARG;
+    if (m > 0 && n > 0 && k > 0 && (A == nullptr || B == nullptr)) return FMM_ERR_ARG;
+    return FMM_OK;
+}
+
+extern "C" int fmm_gpu_dgemm(const fmm_t* fmm, int levels, int64_t m, int64_t n, int64_t k, double alpha,
+                             const double* A, int64_t lda, const double* B, int64_t ldb, double beta,
+                             double* C, int64_t ldc, void* stream)
+{
+    int rc = check_gemm_args(m, n, k, A, lda, B, ldb, C, ldc);
+    if (rc != FMM_OK) return rc;
+    fmm_t flat;
+    int owned = 0;
+    rc = fmm_flatten(fmm, levels, &flat, &owned);
+    if (rc != FMM_OK) return rc;
+    AlgView alg;
+    rc = fmm_alg_get(&flat, &alg);
+    if (owned) free_fmm(flat);
+    if (rc != FMM_OK) return rc;
+    return fmm_f64_launch(alg, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, (cudaStream_t)stream);
+}
+
+extern "C" int fmm_gpu_strassen_ab_ex(double alpha, const double* A, int64_t lda, const double* B,
+                                      int64_t ldb, double beta, double* C, int64_t ldc, int64_t m,
+                                      int64_t n, int64_t k, fmm_t fmm)
+{
+    int rc = check_gemm_args(m, n, k, A, lda, B, ldb, C, ldc);
+    if (rc != FMM_OK) return rc;
+    if (m == 0 || n == 0) return FMM_OK;
+    double *dA = nullptr, *dB = nullptr, *dC = nullptr;
+    const int64_t ka = k > 0 ? k : 1;
+    rc = FMM_OK;
+    if (cudaMalloc(&dA, sizeof(double) * (size_t)(m * ka)) != cudaSuccess ||
+        cudaMalloc(&dB, sizeof(double) * (size_t)(ka * n)) != cudaSuccess ||
+        cudaMalloc(&dC, sizeof(double) * (size_t)(m * n)) != cudaSuccess)
+        rc = FMM_ERR_ALLOC;
+    if (rc == FMM_OK && k > 0 &&
+        (cudaMemcpy2D(dA, sizeof(double) * m, A, sizeof(double) * lda, sizeof(double) * m, k,
+                      cudaMemcpyHostToDevice) != cudaSuccess ||
+         cudaMemcpy2D(dB, sizeof(double) * k, B, sizeof(double) * ldb, sizeof(double) * k, n,
+                      cudaMemcpyHostToDevice) != cudaSuccess))
+        rc = FMM_ERR_CUDA;
+    if (rc == FMM_OK && cudaMemcpy2D(dC, sizeof(double) * m, C, sizeof(double) * ldc, sizeof(double) * m, n,
+                                     cudaMemcpyHostToDevice) != cudaSuccess)
+        rc = FMM_ERR_CUDA;
+    if (rc == FMM_OK)
+        rc = fmm_gpu_dgemm(&fmm, 1, m, n, k, alpha, dA, m, dB, ka, beta, dC, m, nullptr);
+    if (rc == FMM_OK && cudaMemcpy2D(C, sizeof(double) * ldc, dC, sizeof(double) * m, sizeof(double) * m, n,
+                                     cudaMemcpyDeviceToHost) != cudaSuccess)
+        rc = FMM_ERR_CUDA;
+    cudaFree(dA);
+    cudaFree(dB);
+    cudaFree(dC);
+    return rc;
+}
+
+extern "C" int fmm_gpu_strassen_ab(double alpha, const double* A, int64_t lda, const double* B, int64_t ldb,
+                                   double beta, double* C, int64_t ldc, int64_t m, int64_t n, int64_t k)
+{
+    return fmm_gpu_strassen_ab_ex(alpha, A, lda, B, ldb, beta, C, ldc, m, n, k, STRASSEN_FMM);
+}
+
+extern "C" size_t fmm_gpu_split_workspace_size(const fmm_t* fmm, int levels, int64_t m, int64_t n, int64_t k,
+                                               int slices)
+{
+    if (m < 0 || n < 0 || k < 0 || slices < 2 || slices > 8) return 0;
+    fmm_t flat;
+    int owned = 0;
+    if (fmm_flatten(fmm, levels, &flat, &owned) != FMM_OK) return 0;
+    AlgView v;
+    v.mt = flat.m_tilde; v.kt = flat.k_tilde; v.nt = flat.n_tilde; v.R = flat.R;
+    size_t b = fmm_split_ws_bytes(v, m, n, k, slices);
+    if (owned) free_fmm(flat);
+    return b;
+}
+
+extern "C" int fmm_gpu_split_dgemm(const fmm_t* fmm, int levels, int64_t m, int64_t n, int64_t k,
+                                   double alpha, const double* A, int64_t lda, const double* B, int64_t ldb,
+                                   double beta, double* C, int64_t ldc, int slices, void* workspace,
+                                   size_t workspace_bytes, void* stream)
+{
+    int rc = check_gemm_args(m, n, k, A, lda, B, ldb, C, ldc);
+    if (rc != FMM_OK) return rc;
+    if (slices < 2 || slices > 8) return FMM_ERR_ARG;
+    fmm_t flat;
+    int owned = 0;
+    rc = fmm_flatten(fmm, levels, &flat, &owned);
+    if (rc != FMM_OK) return rc;
+    AlgView alg;
+    rc = fmm_alg_get(&flat, &alg);
+    if (owned) free_fmm(flat);
+    if (rc != FMM_OK) return rc;
+    if (fmm_device_error_word() == nullptr) return FMM_ERR_CUDA;
+    return fmm_split_launch(alg, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, slices, workspace,
+                            workspace_bytes, (cudaStream_t)stream);
+}

@@ -1,0 +1,804 @@
+/*
+ * Split-precision (Ozaki-style) form of the FMM GEMM on the sm_103a tensor
+ * cores.
+ *
+ * Per product r of the (flattened) FMM algorithm:
+ *
+ *   1. exps:   row exponents E_i of S_r = sum_q U[q,r] A_q and column
+ *              exponents F_j of T_r = sum_q V[q,r] B_q, from the bound
+ *              |S_r[i,:]| <= sum_q |U[q,r]| * max|A_q[i,:]|, evaluated in FP64
+ *              in the same order as the sums themselves (so the bound holds
+ *              for the rounded sums too). The per-sub-block row/column maxima
+ *              are computed once per call (amax/bmax kernels).
+ *   2. pack:   the fused multi-operand pack (plugin/ref_kernels/
+ *              bli_packm_fmm_ref.c:89-147): S_r (T_r) is formed in FP64 in
+ *              sub-block order with zero fill, then split there into `s`
+ *              balanced base-256 digits d_1..d_s in [-128, 128]:
+ *                  S[i,p] ~= 2^(E_i + 1 - 8s) * sum_t d_t[i,p] 256^(s-t)
+ *              using integer arithmetic on the FP64 bit pattern. Each digit is
+ *              an integer of at most 8 significant bits, so it is exact in
+ *              BF16. Digits are written K-major ("slices" [t][row][k]).
+ *   3. gemm:   tcgen05.mma (kind::f16, BF16 x BF16 -> FP32 in TMEM) over the
+ *              slice pairs (t,u) with t+u = g for the levels g = 2..s+1. Every
+ *              product of two digits is an integer of magnitude <= 2^14, so a
+ *              256-term chunk sums to an integer of magnitude <= 2^22 that
+ *              FP32 holds exactly; the epilogue warps drain each chunk from
+ *              TMEM (double-buffered, so the tensor core keeps running),
+ *              convert it exactly to int32 and add it to the level sum L_g.
+ *              At the end of a level, L_g is folded into a 64-bit fixed-point
+ *              accumulator Z (held in TMEM) in units of level G (G = 6, or 7
+ *              when k_pad <= 128: the finest unit for which k_pad * 2^14 *
+ *              2^(8(G-2)) stays below 2^62):
+ *                  Z = sum_{g<=G} L_g * 2^(8(G-g)) + sum_{g>G} round(L_g / 2^(8(g-G)))
+ *              and at the end of the tile M_r[i,j] ~= 2^(E_i + F_j + 2 - 8G) * Z
+ *              is formed in FP64 and added with alpha*W[p,r] into every C
+ *              sub-block p (the multi-C epilogue,
+ *              plugin/ref_kernels/bli_gemm_fmm_ref.c:99-120), coalesced.
+ *
+ * FP64 is only used for the packing sums, the bounds, the int64 -> FP64
+ * conversion and the C updates; the digit split, the level sums and Z are
+ * exact integer arithmetic, so the result is deterministic and reproducible
+ * bit for bit by a CPU restatement.
+ *
+ * Limits: k_e = ceil(k/k~) <= 16384 per call (level sums stay inside int32
+ * and Z inside int64); slices 2..8; finite inputs.
+ */
+#include "fmm_internal.h"
+#include "sm103_ptx.cuh"
+
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <mutex>
+
+namespace {
+
+constexpr int kTileM = 128;
+constexpr int kTileN = 128;
+constexpr int kBK = 64;                 /* k elements per stage (128 bytes of BF16) */
+constexpr int kStages = 6;
+constexpr int kChunkKB = 4;             /* k-blocks per exact FP32 chunk: 256 terms */
+constexpr int kEpiWarps = 8;       /* two per TMEM lane quarter, 64 columns each */
+constexpr int kGemmThreads = 64 + 32 * kEpiWarps;
+constexpr uint32_t kTileBytes = kTileM * kBK * 2;  /* 16 KB, same for A and B */
+constexpr uint32_t kStageBytes = 2 * kTileBytes;
+constexpr int kTmemCols = 512;          /* 2 x 128 accumulator columns + 256 for Z */
+constexpr int kZLoCol = 256, kZHiCol = 384;
+constexpr int kMaxKe = 16384;
+constexpr size_t kGemmSmem = (size_t)kStages * kStageBytes + 1024 + 256;
+
+__host__ __device__ __forceinline__ int64_t round_up(int64_t x, int64_t m) { return (x + m - 1) / m * m; }
+
+/* ------------------------------------------------------------ digits ---- */
+
+/* E with 2^(E-1) <= b < 2^E for finite b > 0; 0 for b == 0. */
+__device__ __forceinline__ int exp_above(double b)
+{
+    const uint64_t bits = (uint64_t)__double_as_longlong(b) & 0x7fffffffffffffffull;
+    if (bits == 0) return 0;
+    const int bexp = (int)(bits >> 52);
+    if (bexp > 0) return bexp - 1022;
+    return -1010 - __clzll((long long)bits);
+}
+
+/* Balanced base-256 digits of x relative to 2^E (|x| < 2^E): X =
+ * round(x * 2^(8s-E-1)) (ties away from zero), |X| <= 2^(8s-1), then
+ * d[s-1], ..., d[1] in [-128, 127] from the bottom and d[0] in [-128, 128]. */
+template <int S>
+__device__ __forceinline__ void split_digits(double x, int E, int* d)
+{
+    constexpr int s = S;
+    const uint64_t bits = (uint64_t)__double_as_longlong(x);
+    const bool neg = (bits >> 63) != 0;
+    const int bexp = (int)((bits >> 52) & 0x7ff);
+    uint64_t mant = bits & 0x000fffffffffffffull;
+    int ex;
+    if (bexp == 0) ex = -1074; else { mant |= 0x0010000000000000ull; ex = bexp - 1075; }
+    const int sh = ex + 8 * s - E - 1;
+    int64_t X;
+    if (mant == 0 || sh < -62) X = 0;
+    else if (sh >= 0) X = (int64_t)(mant << sh);
+    else X = (int64_t)((mant + (1ull << (-sh - 1))) >> (-sh));
+    if (neg) X = -X;
+#pragma unroll
+    for (int t = s - 1; t >= 1; --t) {
+        const int dd = (int)((X + 128) & 255) - 128;
+        d[t] = dd;
+        X = (X - dd) >> 8;
+    }
+    d[0] = (int)X;
+}
+
+/* v * 2^e, in at most two exact power-of-two multiplications. */
+__device__ __forceinline__ double scale2(double v, int e)
+{
+    if (e > 1000) {
+        v *= __longlong_as_double((long long)(1000 + 1023) << 52);
+        e -= 1000;
+    } else if (e < -1000) {
+        v *= __longlong_as_double((long long)(-1000 + 1023) << 52);
+        e += 1000;
+    }
+    return v * __longlong_as_double((long long)(e + 1023) << 52);
+}
+
+__device__ __forceinline__ uint16_t bf16_of_int(int d)
+{
+    /* exact: |d| <= 128 has at most 8 significant bits */
+    const uint32_t f = __float_as_uint((float)d);
+    return (uint16_t)(f >> 16);
+}
+
+/* ------------------------------------------------- table access -------- */
+
+struct Tab {
+    int mt, kt, nt, R;
+    const int* u_off; const int* v_off; const int* w_off;
+    const int* u_ent; const int* v_ent; const int* w_ent;
+};
+
+__host__ __device__ __forceinline__ Tab tab_view(const int* tab)
+{
+    Tab t;
+    t.mt = tab[0]; t.kt = tab[1]; t.nt = tab[2]; t.R = tab[3];
+    t.u_off = tab + FMM_ALG_HDR;
+    t.v_off = t.u_off + (t.R + 1);
+    t.w_off = t.v_off + (t.R + 1);
+    t.u_ent = t.w_off + (t.R + 1);
+    t.v_ent = t.u_ent + 2 * t.u_off[t.R];
+    t.w_ent = t.v_ent + 2 * t.v_off[t.R];
+    return t;
+}
+
+/* ----------------------------------------------------- max kernels ----- */
+
+/* amax[b*m + i] = max over the columns of k-block b of |A[i, :]| (as the bit
+ * pattern of a non-negative double, which orders like the value). */
+__global__ void amax_kernel(const double* __restrict__ A, int64_t lda, int64_t m, int64_t k,
+                            int kt, unsigned long long* __restrict__ amax, int cols_per_block)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int b = blockIdx.y;
+    if (i >= m) return;
+    int64_t co, cl;
+    fmm_part_geom(k, kt, b, &co, &cl);
+    const int64_t c0 = (int64_t)blockIdx.z * cols_per_block;
+    if (c0 >= cl) return;
+    const int64_t c1 = cl < c0 + cols_per_block ? cl : c0 + cols_per_block;
+    unsigned long long mx = 0;
+    for (int64_t c = c0; c < c1; ++c) {
+        const unsigned long long v =
+            (unsigned long long)__double_as_longlong(A[i + (co + c) * lda]) & 0x7fffffffffffffffull;
+        mx = v > mx ? v : mx;
+    }
+    atomicMax(&amax[(int64_t)b * m + i], mx);
+}
+
+/* bmax[b*n + j] = max over the rows of k-block b of |B[:, j]|; one warp per
+ * (j, b). */
+__global__ void bmax_kernel(const double* __restrict__ B, int64_t ldb, int64_t k, int64_t n,
+                            int kt, unsigned long long* __restrict__ bmax)
+{
+    const int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / 32;
+    const int lane = threadIdx.x % 32;
+    if (w >= n * kt) return;
+    const int64_t j = w % n;
+    const int b = (int)(w / n);
+    int64_t ro, rl;
+    fmm_part_geom(k, kt, b, &ro, &rl);
+    unsigned long long mx = 0;
+    for (int64_t p = lane; p < rl; p += 32) {
+        const unsigned long long v =
+            (unsigned long long)__double_as_longlong(B[ro + p + j * ldb]) & 0x7fffffffffffffffull;
+        mx = v > mx ? v : mx;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o /= 2) {
+        const unsigned long long y = __shfl_xor_sync(0xffffffffu, mx, o);
+        mx = y > mx ? y : mx;
+    }
+    if (lane == 0) bmax[(int64_t)b * n + j] = mx;
+}
+
+/* Row exponents of S_r (rows < m_pad) and column exponents of T_r. */
+__global__ void exps_kernel(const int* __restrict__ tab, int r, int64_t m, int64_t n, int64_t k,
+                            int64_t m_pad, int64_t n_pad,
+                            const unsigned long long* __restrict__ amax,
+                            const unsigned long long* __restrict__ bmax,
+                            int* __restrict__ e_row, int* __restrict__ f_col)
+{
+    const Tab t = tab_view(tab);
+    const int64_t me = (m + t.mt - 1) / t.mt, ne = (n + t.nt - 1) / t.nt;
+    const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (idx < m_pad) {
+        const int64_t i = idx;
+        double bnd = 0.0;
+        bool first = true;
+        if (i < me) {
+            for (int e = t.u_off[r]; e < t.u_off[r + 1]; ++e) {
+                const int part = t.u_ent[2 * e];
+                const double c = fabs((double)t.u_ent[2 * e + 1]);
+                int64_t ro, rl;
+                fmm_part_geom(m, t.mt, part / t.kt, &ro, &rl);
+                if (i >= rl) continue;
+                const double mx = __longlong_as_double((long long)amax[(int64_t)(part % t.kt) * m + ro + i]);
+                bnd = first ? c * mx : fma(c, mx, bnd);
+                first = false;
+            }
+        }
+        e_row[i] = exp_above(bnd);
+    } else if (idx < m_pad + n_pad) {
+        const int64_t j = idx - m_pad;
+        double bnd = 0.0;
+        bool first = true;
+        if (j < ne) {
+            for (int e = t.v_off[r]; e < t.v_off[r + 1]; ++e) {
+                const int part = t.v_ent[2 * e];
+                const double c = fabs((double)t.v_ent[2 * e + 1]);
+                int64_t co, cl;
+                fmm_part_geom(n, t.nt, part % t.nt, &co, &cl);
+                if (j >= cl) continue;
+                const double mx = __longlong_as_double((long long)bmax[(int64_t)(part / t.nt) * n + co + j]);
+                bnd = first ? c * mx : fma(c, mx, bnd);
+                first = false;
+            }
+        }
+        f_col[j] = exp_above(bnd);
+    }
+    (void)k;
+}
+
+/* ----------------------------------------------------- pack kernels ---- */
+
+constexpr int kPackMaxEnt = 256;
+
+struct PEnt {
+    const double* base;
+    int rows, cols;
+    float coef;
+    int pad;
+};
+
+/* A side: tile of 64 rows x 64 k of S_r; digits written row-major (K-major)
+ * into slices sa[t][m_pad][k_pad]. */
+template <int S>
+__global__ void __launch_bounds__(256)
+pack_a_kernel(const int* __restrict__ tab, int r, const double* __restrict__ A, int64_t lda,
+              int64_t m, int64_t k, int64_t m_pad, int64_t k_pad,
+              const int* __restrict__ e_row, uint16_t* __restrict__ sa)
+{
+    __shared__ double Sf[64][65];
+    __shared__ PEnt ent[kPackMaxEnt];
+    const Tab t = tab_view(tab);
+    const int64_t me = (m + t.mt - 1) / t.mt, ke = (k + t.kt - 1) / t.kt;
+    const int64_t i0 = (int64_t)blockIdx.x * 64, p0 = (int64_t)blockIdx.y * 64;
+    const int eb = t.u_off[r], ne_ = t.u_off[r + 1] - eb;
+    for (int e = threadIdx.x; e < ne_; e += blockDim.x) {
+        const int part = t.u_ent[2 * (eb + e)];
+        int64_t ro, rl, co, cl;
+        fmm_part_geom(m, t.mt, part / t.kt, &ro, &rl);
+        fmm_part_geom(k, t.kt, part % t.kt, &co, &cl);
+        PEnt x;
+        x.base = A + ro + co * lda;
+        x.rows = (int)rl; x.cols = (int)cl;
+        x.coef = (float)t.u_ent[2 * (eb + e) + 1];
+        x.pad = 0;
+        ent[e] = x;
+    }
+    __syncthreads();
+    const int li = threadIdx.x % 64;
+#pragma unroll 4
+    for (int q = 0; q < 16; ++q) {
+        const int lp = threadIdx.x / 64 + 4 * q;
+        const int64_t gi = i0 + li, gp = p0 + lp;
+        double sum = 0.0;
+        if (gi < me && gp < ke) {
+            for (int e = 0; e < ne_; ++e) {
+                const PEnt x = ent[e];
+                const double v = (gi < x.rows && gp < x.cols) ? x.base[gi + gp * lda] : 0.0;
+                sum = e == 0 ? (double)x.coef * v : fma((double)x.coef, v, sum);
+            }
+        }
+        Sf[lp][li] = sum;
+    }
+    __syncthreads();
+    /* thread -> (row, 8 consecutive k): 4 rows x 128 bytes per warp store */
+    const int kg = threadIdx.x % 8;
+    for (int rr = threadIdx.x / 8; rr < 64; rr += 32) {
+        const int64_t gi = i0 + rr;
+        const int E = e_row[gi];
+        int dig[8][S];
+#pragma unroll
+        for (int x = 0; x < 8; ++x) split_digits<S>(Sf[kg * 8 + x][rr], E, dig[x]);
+#pragma unroll
+        for (int tt = 0; tt < S; ++tt) {
+            uint32_t w[4];
+#pragma unroll
+            for (int h = 0; h < 4; ++h)
+                w[h] = (uint32_t)bf16_of_int(dig[2 * h][tt]) | ((uint32_t)bf16_of_int(dig[2 * h + 1][tt]) << 16);
+            uint4* dst = (uint4*)(sa + ((int64_t)tt * m_pad + gi) * k_pad + p0 + kg * 8);
+            *dst = make_uint4(w[0], w[1], w[2], w[3]);
+        }
+    }
+}
+
+/* B side: tile of 32 columns x 64 k of T_r (column j of T_r is contiguous in
+ * k already); digits written into slices sb[t][n_pad][k_pad]. */
+template <int S>
+__global__ void __launch_bounds__(256)
+pack_b_kernel(const int* __restrict__ tab, int r, const double* __restrict__ B, int64_t ldb,
+              int64_t k, int64_t n, int64_t n_pad, int64_t k_pad,
+              const int* __restrict__ f_col, uint16_t* __restrict__ sb)
+{
+    __shared__ PEnt ent[kPackMaxEnt];
+    const Tab t = tab_view(tab);
+    const int64_t ne = (n + t.nt - 1) / t.nt, ke = (k + t.kt - 1) / t.kt;
+    const int eb = t.v_off[r], ne_ = t.v_off[r + 1] - eb;
+    for (int e = threadIdx.x; e < ne_; e += blockDim.x) {
+        const int part = t.v_ent[2 * (eb + e)];
+        int64_t ro, rl, co, cl;
+        fmm_part_geom(k, t.kt, part / t.nt, &ro, &rl);
+        fmm_part_geom(n, t.nt, part % t.nt, &co, &cl);
+        PEnt x;
+        x.base = B + ro + co * ldb;
+        x.rows = (int)rl; x.cols = (int)cl;
+        x.coef = (float)t.v_ent[2 * (eb + e) + 1];
+        x.pad = 0;
+        ent[e] = x;
+    }
+    __syncthreads();
+    const int kg = threadIdx.x % 8;
+    const int64_t gj = (int64_t)blockIdx.x * 32 + threadIdx.x / 8;
+    const int64_t p0 = (int64_t)blockIdx.y * 64 + kg * 8;
+    double v8[8];
+#pragma unroll
+    for (int x = 0; x < 8; ++x) v8[x] = 0.0;
+    if (gj < ne) {
+        for (int e = 0; e < ne_; ++e) {
+            const PEnt x = ent[e];
+            const double c = (double)x.coef;
+#pragma unroll
+            for (int y = 0; y < 8; ++y) {
+                const int64_t gp = p0 + y;
+                const double v = (gp < ke && gp < x.rows && gj < x.cols) ? x.base[gp + gj * ldb] : 0.0;
+                v8[y] = e == 0 ? c * v : fma(c, v, v8[y]);
+            }
+        }
+    }
+    const int F = f_col[gj];
+    int dig[8][S];
+#pragma unroll
+    for (int x = 0; x < 8; ++x) split_digits<S>(v8[x], F, dig[x]);
+#pragma unroll
+    for (int tt = 0; tt < S; ++tt) {
+        uint32_t w[4];
+#pragma unroll
+        for (int h = 0; h < 4; ++h)
+            w[h] = (uint32_t)bf16_of_int(dig[2 * h][tt]) | ((uint32_t)bf16_of_int(dig[2 * h + 1][tt]) << 16);
+        uint4* dst = (uint4*)(sb + ((int64_t)tt * n_pad + gj) * k_pad + p0);
+        *dst = make_uint4(w[0], w[1], w[2], w[3]);
+    }
+}
+
+template <int S>
+void launch_packs_t(const int* tab, int r, const double* A, int64_t lda, const double* B, int64_t ldb,
+                    int64_t m, int64_t n, int64_t k, int64_t m_pad, int64_t n_pad, int64_t k_pad,
+                    const int* e_row, const int* f_col, uint16_t* sa, uint16_t* sb, cudaStream_t st)
+{
+    pack_a_kernel<S><<<dim3((unsigned)(m_pad / 64), (unsigned)(k_pad / 64)), 256, 0, st>>>(
+        tab, r, A, lda, m, k, m_pad, k_pad, e_row, sa);
+    pack_b_kernel<S><<<dim3((unsigned)(n_pad / 32), (unsigned)(k_pad / 64)), 256, 0, st>>>(
+        tab, r, B, ldb, k, n, n_pad, k_pad, f_col, sb);
+}
+
+void launch_packs(int s, const int* tab, int r, const double* A, int64_t lda, const double* B,
+                  int64_t ldb, int64_t m, int64_t n, int64_t k, int64_t m_pad, int64_t n_pad,
+                  int64_t k_pad, const int* e_row, const int* f_col, uint16_t* sa, uint16_t* sb,
+                  cudaStream_t st)
+{
+    switch (s) {
+    case 2: launch_packs_t<2>(tab, r, A, lda, B, ldb, m, n, k, m_pad, n_pad, k_pad, e_row, f_col, sa, sb, st); break;
+    case 3: launch_packs_t<3>(tab, r, A, lda, B, ldb, m, n, k, m_pad, n_pad, k_pad, e_row, f_col, sa, sb, st); break;
+    case 4: launch_packs_t<4>(tab, r, A, lda, B, ldb, m, n, k, m_pad, n_pad, k_pad, e_row, f_col, sa, sb, st); break;
+    case 5: launch_packs_t<5>(tab, r, A, lda, B, ldb, m, n, k, m_pad, n_pad, k_pad, e_row, f_col, sa, sb, st); break;
+    case 6: launch_packs_t<6>(tab, r, A, lda, B, ldb, m, n, k, m_pad, n_pad, k_pad, e_row, f_col, sa, sb, st); break;
+    case 7: launch_packs_t<7>(tab, r, A, lda, B, ldb, m, n, k, m_pad, n_pad, k_pad, e_row, f_col, sa, sb, st); break;
+    default: launch_packs_t<8>(tab, r, A, lda, B, ldb, m, n, k, m_pad, n_pad, k_pad, e_row, f_col, sa, sb, st); break;
+    }
+}
+
+/* ------------------------------------------------------ GEMM kernel ---- */
+
+struct GemmArgs {
+    int s;                /* slices */
+    int zlevel;           /* G: the level whose unit Z counts in */
+    int nkb;              /* k_pad / 64 */
+    int tiles_m;
+    int m_pad, n_pad;
+    int64_t m, n;         /* full C sizes (sub-block geometry) */
+    int mt, nt;
+    const int* e_row;
+    const int* f_col;
+    const int* w_ent;     /* this product's W entries (part, coef) */
+    int nw;
+    double alpha;
+    double* C;
+    int64_t ldc;
+    int* err;
+};
+
+__device__ __forceinline__ int level_pairs(int g, int s) { return min(s, g - 1) - max(1, g - s) + 1; }
+
+/* Z (TMEM, 64-bit as lo/hi columns, in units of level G) += the level-g sum
+ * L of this thread's row and 64 columns, with D = G - g: exact left shift by
+ * 8D for D >= 0, rounded right shift by -8D (ties up) for D < 0. */
+template <int D>
+__device__ __forceinline__ void fold_level(const int* L, uint32_t tz, bool first)
+{
+#pragma unroll
+    for (int h = 0; h < 4; ++h) {
+        uint32_t lo[16], hi[16];
+        const uint32_t zc = h * 16;
+        if (first) {
+#pragma unroll
+            for (int x = 0; x < 16; ++x) { lo[x] = 0; hi[x] = 0; }
+        } else {
+            SM103_TMEM_LD_X16(tz + kZLoCol + zc, lo);
+            SM103_TMEM_LD_X16(tz + kZHiCol + zc, hi);
+            sm103::tmem_wait_ld();
+        }
+#pragma unroll
+        for (int x = 0; x < 16; ++x) {
+            int64_t z = (int64_t)(((uint64_t)hi[x] << 32) | lo[x]);
+            const int64_t lv = L[h * 16 + x];
+            if (D >= 0) z += lv * ((int64_t)1 << (8 * D));
+            else z += (lv + ((int64_t)1 << (-8 * D - 1))) >> (-8 * D);
+            lo[x] = (uint32_t)(uint64_t)z;
+            hi[x] = (uint32_t)((uint64_t)z >> 32);
+        }
+        SM103_TMEM_ST_X16(tz + kZLoCol + zc, lo);
+        SM103_TMEM_ST_X16(tz + kZHiCol + zc, hi);
+    }
+    sm103::tmem_wait_st();
+}
+
+__global__ void __launch_bounds__(kGemmThreads, 1)
+split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                  const GemmArgs a)
+{
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint8_t* sA = smem;
+    uint8_t* sB = smem + kStages * kTileBytes;
+    uint64_t* full = (uint64_t*)(smem + kStages * kStageBytes);
+    uint64_t* empty = full + kStages;
+    uint64_t* accf = empty + kStages;
+    uint64_t* acce = accf + 2;
+    uint64_t* drain = acce + 2;
+    uint32_t* tmem_slot = (uint32_t*)(drain + 1);
+    volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
+
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    const int tile_m = blockIdx.x % a.tiles_m, tile_n = blockIdx.x / a.tiles_m;
+
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < kStages; ++i) { sm103::mbar_init(&full[i], 1); sm103::mbar_init(&empty[i], 1); }
+        for (int i = 0; i < 2; ++i) { sm103::mbar_init(&accf[i], 1); sm103::mbar_init(&acce[i], kEpiWarps); }
+        sm103::mbar_init(drain, 1);
+        *abort_flag = 0;
+        sm103::fence_mbar_init();
+    }
+    if (warp == 1) { sm103::tmem_alloc(tmem_slot, kTmemCols); sm103::tmem_relinquish(); }
+    if (warp == 0 && lane == 0) { sm103::prefetch_tmap(&tmA); sm103::prefetch_tmap(&tmB); }
+    sm103::tc_fence_before();
+    __syncthreads();
+    sm103::tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    const int s = a.s, nkb = a.nkb;
+
+    if (warp == 0) {
+        /* ---------------- TMA producer ---------------- */
+        if (lane == 0) {
+            int st = 0;
+            uint32_t ph = 0;
+            uint32_t armed = 0;  /* stages armed in the current pass (bit mask) */
+            bool ok = true;
+            for (int g = 2; g <= s + 1 && ok; ++g)
+                for (int t = max(1, g - s); t <= min(s, g - 1) && ok; ++t) {
+                    const int u = g - t;
+                    for (int kb = 0; kb < nkb; ++kb) {
+                        if (!sm103::mbar_wait(&empty[st], ph ^ 1, abort_flag, a.err, 1)) { ok = false; break; }
+                        sm103::mbar_arrive_expect_tx(&full[st], kStageBytes);
+                        sm103::tma_load_2d(sA + st * kTileBytes, &tmA, &full[st], kb * kBK,
+                                           (t - 1) * a.m_pad + tile_m * kTileM);
+                        sm103::tma_load_2d(sB + st * kTileBytes, &tmB, &full[st], kb * kBK,
+                                           (u - 1) * a.n_pad + tile_n * kTileN);
+                        armed |= 1u << st;
+                        if (++st == kStages) { st = 0; ph ^= 1; armed = 0; }
+                    }
+                }
+            if (!ok) {
+                /* let every load already issued land before the CTA exits */
+                for (int i = 0; i < kStages; ++i) {
+                    const uint32_t par = (armed >> i) & 1u ? ph : ph ^ 1;
+                    uint64_t t0 = sm103::globaltimer();
+                    while (!sm103::mbar_try_wait(&full[i], par) &&
+                           sm103::globaltimer() - t0 < sm103::kWaitLimitNs) {}
+                }
+            }
+        }
+    } else if (warp == 1) {
+        /* ---------------- MMA issuer ---------------- */
+        if (lane == 0) {
+            constexpr uint32_t idesc = sm103::idesc_bf16_f32(kTileM, kTileN);
+            int st = 0, buf = 0;
+            uint32_t ph = 0, aph = 0;
+            bool ok = true;
+            for (int g = 2; g <= s + 1 && ok; ++g) {
+                const int level_kb = level_pairs(g, s) * nkb;
+                int jl = 0;
+                for (int t = max(1, g - s); t <= min(s, g - 1) && ok; ++t)
+                    for (int kb = 0; kb < nkb; ++kb) {
+                        if (jl % kChunkKB == 0) {
+                            if (!sm103::mbar_wait(&acce[buf], aph ^ 1, abort_flag, a.err, 2)) { ok = false; break; }
+                            sm103::tc_fence_after();
+                        }
+                        if (!sm103::mbar_wait(&full[st], ph, abort_flag, a.err, 3)) { ok = false; break; }
+                        sm103::tc_fence_after();
+                        const uint32_t a0 = sm103::smem_u32(sA + st * kTileBytes);
+                        const uint32_t b0 = sm103::smem_u32(sB + st * kTileBytes);
+#pragma unroll
+                        for (int kk = 0; kk < kBK / 16; ++kk)
+                            sm103::mma_bf16(tmem + buf * kTileN, sm103::smem_desc_sw128(a0 + kk * 32),
+                                            sm103::smem_desc_sw128(b0 + kk * 32), idesc,
+                                            (jl % kChunkKB != 0 || kk != 0) ? 1u : 0u);
+                        sm103::mma_commit(&empty[st]);
+                        if (++st == kStages) { st = 0; ph ^= 1; }
+                        ++jl;
+                        if (jl % kChunkKB == 0 || jl == level_kb) {
+                            sm103::mma_commit(&accf[buf]);
+                            buf ^= 1;
+                            if (buf == 0) aph ^= 1;
+                        }
+                    }
+            }
+            /* all issued MMAs complete before TMEM is released */
+            sm103::mma_commit(drain);
+            uint64_t t0 = sm103::globaltimer();
+            while (!sm103::mbar_try_wait(drain, 0) && sm103::globaltimer() - t0 < sm103::kWaitLimitNs) {}
+        }
+    } else {
+        /* ---------------- epilogue warps ---------------- */
+        const int quarter = warp % 4;          /* TMEM lane quarter this warp may access */
+        const int colbase = ((warp - 2) / 4) * 64;
+        const int row = quarter * 32 + lane;
+        const uint32_t tl = tmem + ((uint32_t)(quarter * 32) << 16);
+        int buf = 0;
+        uint32_t aph = 0;
+        bool ok = true;
+        for (int g = 2; g <= s + 1 && ok; ++g) {
+            int L[64];
+#pragma unroll
+            for (int x = 0; x < 64; ++x) L[x] = 0;
+            const int nchunks = (level_pairs(g, s) * nkb + kChunkKB - 1) / kChunkKB;
+            for (int c = 0; c < nchunks; ++c) {
+                if (!sm103::mbar_wait(&accf[buf], aph, abort_flag, a.err, 4)) { ok = false; break; }
+                sm103::tc_fence_after();
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    uint32_t v[32];
+                    SM103_TMEM_LD_X32(tl + buf * kTileN + colbase + h * 32, v);
+                    sm103::tmem_wait_ld();
+#pragma unroll
+                    for (int x = 0; x < 32; ++x)
+                        L[h * 32 + x] += (int)__float_as_uint(__uint_as_float(v[x]) + 12582912.0f) - 0x4B400000;
+                }
+                sm103::tc_fence_before();
+                __syncwarp();
+                if (lane == 0) sm103::mbar_arrive(&acce[buf]);
+                buf ^= 1;
+                if (buf == 0) aph ^= 1;
+            }
+            if (!ok) break;
+            /* fold L_g into Z (units of level G) */
+            const bool first = g == 2;
+            switch (a.zlevel - g) {
+            case 5: fold_level<5>(L, tl + colbase, first); break;
+            case 4: fold_level<4>(L, tl + colbase, first); break;
+            case 3: fold_level<3>(L, tl + colbase, first); break;
+            case 2: fold_level<2>(L, tl + colbase, first); break;
+            case 1: fold_level<1>(L, tl + colbase, first); break;
+            case 0: fold_level<0>(L, tl + colbase, first); break;
+            case -1: fold_level<-1>(L, tl + colbase, first); break;
+            case -2: fold_level<-2>(L, tl + colbase, first); break;
+            default: fold_level<-3>(L, tl + colbase, first); break;
+            }
+        }
+        if (ok) {
+            /* M_r tile = 2^(E_i + F_j - 46) * Z, added into the C sub-blocks */
+            const int64_t gi = (int64_t)tile_m * kTileM + row;
+            const int Ei = gi < a.m_pad ? a.e_row[gi] : 0;
+#pragma unroll 1
+            for (int h = 0; h < 4; ++h) {
+                uint32_t lo[16], hi[16];
+                const uint32_t zc = colbase + h * 16;
+                SM103_TMEM_LD_X16(tl + kZLoCol + zc, lo);
+                SM103_TMEM_LD_X16(tl + kZHiCol + zc, hi);
+                sm103::tmem_wait_ld();
+                const int64_t gj0 = (int64_t)tile_n * kTileN + zc;
+                double val[16];
+#pragma unroll
+                for (int x = 0; x < 16; ++x) {
+                    const int64_t z = (int64_t)(((uint64_t)hi[x] << 32) | lo[x]);
+                    val[x] = scale2((double)z, Ei + a.f_col[gj0 + x] + 2 - 8 * a.zlevel);
+                }
+                for (int e = 0; e < a.nw; ++e) {
+                    const int part = a.w_ent[2 * e];
+                    const double lam = a.alpha * (double)a.w_ent[2 * e + 1];
+                    int ro, rl, co, cl;
+                    fmm_part_geom32((int)a.m, a.mt, part / a.nt, &ro, &rl);
+                    fmm_part_geom32((int)a.n, a.nt, part % a.nt, &co, &cl);
+                    if (gi >= rl) continue;
+                    double* cb = a.C + ro + gi + (int64_t)co * a.ldc;
+#pragma unroll
+                    for (int x = 0; x < 16; ++x) {
+                        const int64_t gj = gj0 + x;
+                        if (gj < cl) {
+                            double* p = cb + gj * a.ldc;
+                            *p = fma(lam, val[x], *p);
+                        }
+                    }
+                }
+            }
+        }
+    }
+    sm103::tc_fence_before();
+    __syncthreads();
+    sm103::tc_fence_after();
+    if (warp == 1) sm103::tmem_dealloc(tmem, kTmemCols);
+}
+
+/* --------------------------------------------------------- host -------- */
+
+PFN_cuTensorMapEncodeTiled_v12000 get_encode_fn()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, []() {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess && q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    });
+    return fn;
+}
+
+/* 2-D map over slices[rows_total][k_pad] BF16, box 64 (k) x 128 (rows),
+ * 128-byte swizzle. */
+int make_slice_map(CUtensorMap* map, const void* base, int64_t k_pad, int64_t rows_total)
+{
+    PFN_cuTensorMapEncodeTiled_v12000 enc = get_encode_fn();
+    if (!enc) return FMM_ERR_CUDA;
+    cuuint64_t dims[2] = {(cuuint64_t)k_pad, (cuuint64_t)rows_total};
+    cuuint64_t strides[1] = {(cuuint64_t)(k_pad * 2)};
+    cuuint32_t box[2] = {(cuuint32_t)kBK, (cuuint32_t)kTileM};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box,
+                     estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? FMM_OK : FMM_ERR_CUDA;
+}
+
+struct WsLayout {
+    size_t amax, bmax, erow, fcol, sa, sb, total;
+};
+
+WsLayout ws_layout(const AlgView& alg, int64_t m, int64_t n, int64_t k, int s)
+{
+    const int64_t me = (m + alg.mt - 1) / alg.mt, ne = (n + alg.nt - 1) / alg.nt,
+                  ke = (k + alg.kt - 1) / alg.kt;
+    const int64_t m_pad = round_up(std::max<int64_t>(me, 1), kTileM);
+    const int64_t n_pad = round_up(std::max<int64_t>(ne, 1), kTileN);
+    const int64_t k_pad = round_up(std::max<int64_t>(ke, 1), kBK);
+    WsLayout L;
+    size_t off = 0;
+    auto take = [&](size_t bytes) { size_t o = off; off += (bytes + 255) / 256 * 256; return o; };
+    L.amax = take(sizeof(unsigned long long) * (size_t)alg.kt * (size_t)m);
+    L.bmax = take(sizeof(unsigned long long) * (size_t)alg.kt * (size_t)n);
+    L.erow = take(sizeof(int) * (size_t)m_pad);
+    L.fcol = take(sizeof(int) * (size_t)n_pad);
+    L.sa = take(2 * (size_t)s * (size_t)m_pad * (size_t)k_pad);
+    L.sb = take(2 * (size_t)s * (size_t)n_pad * (size_t)k_pad);
+    L.total = off;
+    return L;
+}
+
+}  // namespace
+
+size_t fmm_split_ws_bytes(const AlgView& alg, int64_t m, int64_t n, int64_t k, int slices)
+{
+    return ws_layout(alg, m, n, k, slices).total;
+}
+
+int fmm_split_launch(const AlgView& alg, int64_t m, int64_t n, int64_t k, double alpha,
+                     const double* A, int64_t lda, const double* B, int64_t ldb, double beta,
+                     double* C, int64_t ldc, int s, void* ws, size_t ws_bytes, cudaStream_t st)
+{
+    if (s < 2 || s > 8) return FMM_ERR_ARG;
+    int rc = fmm_scale_c(m, n, beta, C, ldc, st);
+    if (rc != FMM_OK) return rc;
+    if (m == 0 || n == 0 || k == 0 || alpha == 0.0) return FMM_OK;
+    if (alg.max_nnz_u > kPackMaxEnt || alg.max_nnz_v > kPackMaxEnt) return FMM_ERR_UNSUPPORTED;
+    const int64_t me = (m + alg.mt - 1) / alg.mt, ne = (n + alg.nt - 1) / alg.nt,
+                  ke = (k + alg.kt - 1) / alg.kt;
+    if (ke > kMaxKe) return FMM_ERR_UNSUPPORTED;
+    const int64_t m_pad = round_up(me, kTileM), n_pad = round_up(ne, kTileN), k_pad = round_up(ke, kBK);
+    if ((m_pad / kTileM) * (n_pad / kTileN) > 0x7fffffffLL || m_pad * s > 0x7fffffffLL ||
+        n_pad * s > 0x7fffffffLL)
+        return FMM_ERR_UNSUPPORTED;
+    const WsLayout L = ws_layout(alg, m, n, k, s);
+    if (ws == nullptr || ws_bytes < L.total) return FMM_ERR_WORKSPACE;
+    if (((uintptr_t)ws & 255) != 0) return FMM_ERR_ARG;
+
+    uint8_t* w = (uint8_t*)ws;
+    unsigned long long* amax = (unsigned long long*)(w + L.amax);
+    unsigned long long* bmax = (unsigned long long*)(w + L.bmax);
+    int* e_row = (int*)(w + L.erow);
+    int* f_col = (int*)(w + L.fcol);
+    uint16_t* sa = (uint16_t*)(w + L.sa);
+    uint16_t* sb = (uint16_t*)(w + L.sb);
+
+    static bool attr_set = false;
+    if (!attr_set) {
+        if (cudaFuncSetAttribute(split_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)kGemmSmem) != cudaSuccess)
+            return FMM_ERR_CUDA;
+        attr_set = true;
+    }
+    CUtensorMap tmA, tmB;
+    if (make_slice_map(&tmA, sa, k_pad, m_pad * s) != FMM_OK) return FMM_ERR_CUDA;
+    if (make_slice_map(&tmB, sb, k_pad, n_pad * s) != FMM_OK) return FMM_ERR_CUDA;
+
+    /* per-sub-block row/column maxima, once per call */
+    if (cudaMemsetAsync(amax, 0, sizeof(unsigned long long) * (size_t)alg.kt * (size_t)m, st) != cudaSuccess)
+        return FMM_ERR_CUDA;
+    {
+        const int cpb = 256;
+        const int64_t kb_max = (k + alg.kt - 1) / alg.kt;
+        dim3 grid((unsigned)((m + 255) / 256), (unsigned)alg.kt, (unsigned)((kb_max + cpb - 1) / cpb));
+        amax_kernel<<<grid, 256, 0, st>>>(A, lda, m, k, alg.kt, amax, cpb);
+        const int64_t warps = n * alg.kt;
+        bmax_kernel<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, st>>>(B, ldb, k, n, alg.kt, bmax);
+        fmm_count_launch(2);
+    }
+    const int* htab = alg.htab;
+    const Tab ht = tab_view(htab);
+    GemmArgs ga;
+    ga.s = s;
+    ga.zlevel = k_pad <= 128 ? 7 : 6;
+    ga.nkb = (int)(k_pad / kBK);
+    ga.tiles_m = (int)(m_pad / kTileM);
+    ga.m_pad = (int)m_pad;
+    ga.n_pad = (int)n_pad;
+    ga.m = m; ga.n = n;
+    ga.mt = alg.mt; ga.nt = alg.nt;
+    ga.e_row = e_row; ga.f_col = f_col;
+    ga.alpha = alpha;
+    ga.C = C; ga.ldc = ldc;
+    ga.err = fmm_device_error_word();
+    const unsigned gemm_blocks = (unsigned)((m_pad / kTileM) * (n_pad / kTileN));
+    for (int r = 0; r < alg.R; ++r) {
+        const int nw = ht.w_off[r + 1] - ht.w_off[r];
+        if (nw == 0) continue;
+        exps_kernel<<<(unsigned)((m_pad + n_pad + 255) / 256), 256, 0, st>>>(
+            alg.tab, r, m, n, k, m_pad, n_pad, amax, bmax, e_row, f_col);
+        launch_packs(s, alg.tab, r, A, lda, B, ldb, m, n, k, m_pad, n_pad, k_pad, e_row, f_col, sa, sb, st);
+        ga.w_ent = alg.tab + (ht.w_ent - htab) + 2 * ht.w_off[r];
+        ga.nw = nw;
+        split_gemm_kernel<<<gemm_blocks, kGemmThreads, kGemmSmem, st>>>(tmA, tmB, ga);
+        fmm_count_launch(4);
+    }
+    return cudaGetLastError() == cudaSuccess ? FMM_OK : FMM_ERR_CUDA;
+}

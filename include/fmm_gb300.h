@@ -1,0 +1,189 @@
+/*
+ * fmm_gb300.h -- C ABI of the GB300 (sm_103a) fast-matrix-multiplication GEMM.
+ *
+ * The library computes C := beta*C + alpha*A*B for column-major FP64 matrices
+ * with a one- or two-level <m~,k~,n~> fast matrix multiplication algorithm of
+ * rank R, read from the reference's U/V/W coefficient files, in the "ABC"
+ * form: the U- and V-weighted sums of A and B sub-blocks are formed while the
+ * operand tiles are loaded, and each of the R products is added with its W
+ * coefficients into every C sub-block it feeds.
+ *
+ * Reference interface each entry point replaces (paths inside fmm-blis):
+ *   fmm_t, STRASSEN_FMM        plugin/bli_plugin_fmm_blis.h:58-68,
+ *                              frame/base/bli_strassen_ab.c:12-24
+ *   new_fmm / free_fmm         frame/include/bli_fmm.h:69-70,
+ *                              frame/base/bli_read_fmm.c:24-86
+ *   bl_clock                   frame/util/bli_fmm_util.c:106-109
+ *   fmm_gpu_strassen_ab_ex     bli_strassen_ab_ex, frame/include/bli_fmm.h:74-81,
+ *                              frame/base/bli_strassen_ab.c:123-295 (host buffers)
+ *   fmm_gpu_strassen_ab        bli_strassen_ab, frame/include/bli_fmm.h:83-89,
+ *                              frame/base/bli_strassen_ab.c:297-300
+ *   fmm_gpu_dgemm              the device-resident form of bli_strassen_ab_ex
+ *                              (the per-product loop at bli_strassen_ab.c:248-294
+ *                              with the packm plugin kernel
+ *                              plugin/ref_kernels/bli_packm_fmm_ref.c:51-148 and
+ *                              the micro-kernel epilogue
+ *                              plugin/ref_kernels/bli_gemm_fmm_ref.c:40-121)
+ *   fmm_gpu_split_dgemm        the same GEMM computed from BF16 slices of the
+ *                              packed FP64 combinations (split-precision form);
+ *                              no counterpart function in the reference, whose
+ *                              pack/epilogue plugin kernels it reuses in spirit
+ *
+ * Error behaviour: every fmm_gpu_* call returns an int status (FMM_OK = 0).
+ * new_fmm keeps the reference's by-value signature; on a missing or malformed
+ * file it returns an fmm_t with R == 0 and NULL arrays (the reference
+ * dereferences NULL instead), and fmm_load returns the status.
+ *
+ * Layout: all matrices are column-major, element (i,j) at ptr[i + j*ld],
+ * ld >= rows. Devices pointers are CUDA global memory of the current device.
+ * `stream` is a cudaStream_t passed as void* (NULL = legacy default stream).
+ */
+#ifndef FMM_GB300_H
+#define FMM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- types -- */
+
+/* Same field order and meaning as the reference's fmm_t
+ * (plugin/bli_plugin_fmm_blis.h:58-68). U is (m_tilde*k_tilde) x R, V is
+ * (k_tilde*n_tilde) x R, W is (m_tilde*n_tilde) x R, all row-major
+ * (U[q*R + r]); row q of U is the A sub-block (q / k_tilde, q % k_tilde), row
+ * q of V the B sub-block (q / n_tilde, q % n_tilde), row q of W the C
+ * sub-block (q / n_tilde, q % n_tilde). */
+typedef struct fmm_s {
+    int m_tilde;
+    int n_tilde;
+    int k_tilde;
+    int R;
+    int* U;
+    int* V;
+    int* W;
+} fmm_t;
+
+enum fmm_status {
+    FMM_OK = 0,
+    FMM_ERR_ARG = 1,         /* bad dimension, stride, pointer or parameter */
+    FMM_ERR_FILE = 2,        /* coefficient file cannot be opened */
+    FMM_ERR_FORMAT = 3,      /* coefficient file malformed */
+    FMM_ERR_ALLOC = 4,       /* host or device allocation failed */
+    FMM_ERR_CUDA = 5,        /* a CUDA runtime/driver call failed */
+    FMM_ERR_UNSUPPORTED = 6, /* size or option outside what the kernels handle */
+    FMM_ERR_BRENT = 7,       /* coefficients do not satisfy the Brent equations */
+    FMM_ERR_DEVICE = 8,      /* a kernel reported an error status (bounded wait expired) */
+    FMM_ERR_WORKSPACE = 9    /* caller workspace too small */
+};
+
+/* ------------------------------------------------ coefficient algorithms -- */
+
+/* Built-in Strassen <2,2,2>, R = 7, same coefficients as 222.txt
+ * (frame/base/bli_strassen_ab.c:12-24). */
+extern fmm_t STRASSEN_FMM;
+
+/* Read a coefficient file (frame/base/bli_read_fmm.c:24-80). Header line
+ * "m~ k~ n~ R" (the order the files are written in; the reference parses it
+ * as m n k, which is only the same when k~ == n~), then m~k~ rows of U,
+ * k~n~ rows of V and m~n~ rows of W; lines starting with '#' are skipped;
+ * lines may be of any length. On failure returns R == 0, NULL arrays. */
+fmm_t new_fmm(const char* file_name);
+
+/* Free the arrays of an fmm_t from new_fmm/fmm_load/fmm_kron
+ * (frame/base/bli_read_fmm.c:82-86). Never call it on STRASSEN_FMM. */
+void free_fmm(fmm_t fmm);
+
+/* Monotonic wall clock in seconds (frame/util/bli_fmm_util.c:106-109). */
+double bl_clock(void);
+
+/* new_fmm with a status code. */
+int fmm_load(const char* file_name, fmm_t* out);
+
+/* Check the Brent equations: for every A block (a,b), B block (b',c), C block
+ * (a',c'), sum_r U*V*W == [a==a'][b==b'][c==c']. Returns FMM_OK or
+ * FMM_ERR_BRENT; *n_bad (may be NULL) receives the number of violated
+ * equations. */
+int fmm_check_brent(const fmm_t* fmm, long* n_bad);
+
+/* Two recursion levels as one flat algorithm: out = outer (x) inner with
+ * m~ = m~o*m~i, k~ = k~o*k~i, n~ = n~o*n~i, R = Ro*Ri; sub-block (a,b) of the
+ * flat grid is block (a % m~i, b % k~i) inside outer block (a / m~i, b / k~i).
+ * out owns new arrays (free_fmm). */
+int fmm_kron(const fmm_t* outer, const fmm_t* inner, fmm_t* out);
+
+/* Deep copy (free_fmm the result). */
+int fmm_copy(const fmm_t* src, fmm_t* dst);
+
+/* Human-readable name of a status code. */
+const char* fmm_status_string(int status);
+
+/* ------------------------------------------------- GPU, plain FP64 form -- */
+
+/* C := beta*C + alpha*A*B on the device, A m x k, B k x n, C m x n, FP64,
+ * computed with `levels` recursion levels of `fmm` (levels == 0 or fmm ==
+ * NULL: the classical FP64 GEMM kernel of this library). Sub-block sizes
+ * follow the reference's split rule: along a dimension d split t ways the
+ * first d % t blocks have ceil(d/t) elements and the rest floor(d/t); each
+ * product is computed at the ceil size with zero fill. Asynchronous on
+ * `stream`. */
+int fmm_gpu_dgemm(const fmm_t* fmm, int levels,
+                  int64_t m, int64_t n, int64_t k,
+                  double alpha, const double* A, int64_t lda,
+                  const double* B, int64_t ldb,
+                  double beta, double* C, int64_t ldc,
+                  void* stream);
+
+/* Drop-in for bli_strassen_ab_ex with the obj_t operands unpacked into plain
+ * HOST pointers, sizes and column strides (frame/base/bli_strassen_ab.c:123).
+ * Copies A, B, C to the device, runs fmm_gpu_dgemm with one level of `fmm`,
+ * copies C back, synchronously. */
+int fmm_gpu_strassen_ab_ex(double alpha, const double* A, int64_t lda,
+                           const double* B, int64_t ldb,
+                           double beta, double* C, int64_t ldc,
+                           int64_t m, int64_t n, int64_t k,
+                           fmm_t fmm);
+
+/* Drop-in for bli_strassen_ab (frame/base/bli_strassen_ab.c:297-300):
+ * fmm_gpu_strassen_ab_ex with STRASSEN_FMM. */
+int fmm_gpu_strassen_ab(double alpha, const double* A, int64_t lda,
+                        const double* B, int64_t ldb,
+                        double beta, double* C, int64_t ldc,
+                        int64_t m, int64_t n, int64_t k);
+
+/* ------------------------------------ GPU, split-precision (Ozaki) form -- */
+
+/* Bytes of device workspace fmm_gpu_split_dgemm needs for this problem. */
+size_t fmm_gpu_split_workspace_size(const fmm_t* fmm, int levels,
+                                    int64_t m, int64_t n, int64_t k,
+                                    int slices);
+
+/* C := beta*C + alpha*A*B computed as the FMM above, but each product's FP64
+ * operand combinations are split (after a power-of-two row/column scaling)
+ * into `slices` BF16 digit slices of 8 bits; all slice pairs (s,t) with
+ * s + t <= slices + 1 are multiplied on the tcgen05 tensor cores with exact
+ * integer-valued FP32 accumulation, and recombined in FP64. slices in 2..8.
+ * `workspace` must hold fmm_gpu_split_workspace_size bytes (256-byte
+ * aligned). Asynchronous on `stream`. */
+int fmm_gpu_split_dgemm(const fmm_t* fmm, int levels,
+                        int64_t m, int64_t n, int64_t k,
+                        double alpha, const double* A, int64_t lda,
+                        const double* B, int64_t ldb,
+                        double beta, double* C, int64_t ldc,
+                        int slices, void* workspace, size_t workspace_bytes,
+                        void* stream);
+
+/* Number of kernels the library launched since load (all entry points). */
+uint64_t fmm_gpu_launch_count(void);
+
+/* Last device-side error word (0 = none) recorded by a kernel whose bounded
+ * wait expired; reading it synchronizes the device. Clears it. */
+int fmm_gpu_take_device_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FMM_GB300_H */

@@ -1,0 +1,27 @@
+"""The C-ABI library loads without a GPU and exports every function the
+public header declares."""
+import re
+
+from conftest import ROOT
+
+
+def header_functions():
+    text = (ROOT / "include" / "fmm_gb300.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = set(re.findall(r"\b([a-z_][a-z0-9_]*)\s*\(", text))
+    return sorted(n for n in names if n not in {"if", "sizeof", "defined"})
+
+
+def test_exports_every_declared_symbol(fmm):
+    L = fmm.lib()
+    names = header_functions()
+    assert "fmm_gpu_dgemm" in names and "new_fmm" in names and "fmm_gpu_split_dgemm" in names
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, missing
+    assert hasattr(L, "STRASSEN_FMM")
+
+
+def test_library_is_sm103a_build(fmm):
+    from fmm_blis_gb300 import build
+    assert "arch=compute_103a,code=sm_103a" in " ".join(build.ARCH)
+    assert fmm.LIB_PATH.exists()
