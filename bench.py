@@ -1,0 +1,366 @@
+#!/usr/bin/env python
+"""Benchmark of the FMM GEMM path on GB300.
+
+Workload (one step): C := C + A*B, m = n = k = 16384, column-major FP64
+operands uniform in [-1, 1) (seeded), computed by the split-precision FMM:
+Strassen <2,2,2> at two recursion levels (49 products of 4096^3) with the FP64
+operand sums split into 6 BF16 digit slices (21 slice pairs per product) on
+the tcgen05 tensor cores. Operands are 2 GiB each, far larger than L2, so no
+flush is needed between steps.
+
+Metric: effective TFLOP/s = 2mnk / t (whole job over all ranks). Reported
+beside it, once per run and outside the timed loop: the plain FP64 FMM and
+the classical FP64 GEMM of this library at the same shape (time and max-norm
+error against the classical result), the split form's error, the dominant
+kernel's roofline, the end-to-end number through host buffers, and the
+reference algorithm on the host cores (the oracle's C restatement, a bounded
+sample of products).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun each rank runs an independent replica of the workload (the
+path needs no exchange); rank 0 prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "eff. TFLOP/s (2mnk/t): split-BF16 FMM vs FP64 FMM at stated err; p99 latency"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--n", type=int, default=16384)
+    p.add_argument("--alg", default="222")
+    p.add_argument("--levels", type=int, default=2)
+    p.add_argument("--slices", type=int, default=6)
+    p.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison runs")
+    p.add_argument("--no-cpu", action="store_true", help="skip the host-core baseline")
+    p.add_argument("--e2e-steps", type=int, default=2)
+    return p.parse_args()
+
+
+def peaks():
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        d = json.loads(f.read_text())
+        return d.get("bf16_tflops_sustained", 1737.1), d.get("bf16_tflops", 1926.8), d.get("hbm_gbs"), "measured"
+    return 1700.0, 1900.0, 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def host_operands(n, seed=7):
+    """Column-major float64 host operands (torch's CPU generator, seeded)."""
+    import torch
+    g = torch.Generator().manual_seed(seed)
+    return [np.asfortranarray((torch.rand((n, n), generator=g, dtype=torch.float64) * 2 - 1).numpy().T)
+            for _ in range(3)]
+
+
+def cpu_reference(alg, levels, n, target_s, arrays=None):
+    """The reference FMM algorithm (oracle, FP64) on the host cores: a bounded
+    sample of the products of the flattened algorithm at the full shape.
+    Returns (eff TFLOP/s extrapolated to all products, dict)."""
+    import oracle
+    from oracle import coeffs as oc
+
+    flat = oc.power(oc.read(ROOT / "tests" / "golden" / "coeffs" / f"{alg}.txt"), levels)
+    R = flat[3]
+    oracle.set_threads(os.cpu_count() or 1)
+    A, B, C = arrays if arrays is not None else host_operands(n)
+    t0 = time.perf_counter()
+    oracle.fmm_dgemm(flat, A, B, C, r_begin=0, r_end=1)
+    t1 = time.perf_counter() - t0
+    P = max(1, min(R, int(target_s / max(t1, 1e-3))))
+    t0 = time.perf_counter()
+    oracle.fmm_dgemm(flat, A, B, C, r_begin=0, r_end=P)
+    tp = time.perf_counter() - t0
+    eff = 2.0 * n ** 3 * (P / R) / tp / 1e12
+    info = {"cores": oracle.num_threads(), "products": P, "of": R, "seconds": tp}
+    return eff, info
+
+
+def run_reference(args):
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return
+    steps, warm = args.steps, args.warmup
+    per_step = max(2.0, 60.0 / max(steps + warm, 1))
+    vals = []
+    info = None
+    arrays = host_operands(args.n)
+    for i in range(warm + steps):
+        v, info = cpu_reference(args.alg, args.levels, args.n, per_step, arrays)
+        if i >= warm:
+            vals.append(v)
+    value = statistics.median(vals)
+    sample = (f"FP64 FMM {args.alg} x{args.levels} levels at m=n=k={args.n}: products 0..{info['products']} "
+              f"of {info['of']} per step ({info['seconds']:.1f} s), extrapolated to all products")
+    out = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": args.gpus,
+        "steps": steps, "warmup": warm, "ms_per_step": 2.0 * args.n ** 3 / (value * 1e12) * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"FMM {args.alg} x{args.levels} levels, m=n=k={args.n} (reference algorithm, FP64, host cores)",
+                   "m": args.n, "n": args.n, "k": args.n, "alg": args.alg, "levels": args.levels},
+        "cpu_baseline": {"value": value, "unit": "TFLOP/s", "cores": info["cores"], "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+
+    import fmm_blis_gb300 as fmm
+    from fmm_blis_gb300 import build as fbuild
+
+    world, rank, local = dist_setup()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    fbuild.build()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    n, levels, s = args.n, args.levels, args.slices
+    f = fmm.new_fmm(ROOT / "tests" / "golden" / "coeffs" / f"{args.alg}.txt")
+    flops = 2.0 * n ** 3
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    def max_over_ranks(x: float) -> float:
+        if world == 1:
+            return x
+        import torch.distributed as dist
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    g = torch.Generator(device=dev).manual_seed(1234 + rank)
+    A = (torch.rand((n, n), generator=g, device=dev, dtype=torch.float64) * 2 - 1).t()
+    B = (torch.rand((n, n), generator=g, device=dev, dtype=torch.float64) * 2 - 1).t()
+    C0 = (torch.rand((n, n), generator=g, device=dev, dtype=torch.float64) * 2 - 1).t()
+    C = C0.clone()
+    ws = torch.empty(fmm.split_workspace_size(n, n, n, f, levels, s), dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def step(Cx):
+        fmm.split_dgemm(A, B, Cx, f, levels, s, workspace=ws, stream=stream)
+
+    for _ in range(args.warmup):
+        step(C)
+    torch.cuda.synchronize()
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    n_launch0 = fmm.launch_count()
+    fmm.read_kernel_timing()
+    fmm.set_kernel_timing(True)
+    with Clocks(torch.cuda.current_device()) as clk:
+        torch.cuda.synchronize()
+        barrier()
+        e0.record(stream)
+        for _ in range(args.steps):
+            step(C)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+    fmm.set_kernel_timing(False)
+    launches = fmm.launch_count() - n_launch0
+    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps)
+    gemm_ms, gemm_n = fmm.read_kernel_timing()
+    value = world * flops / (ms / 1e3) / 1e12
+
+    # dominant kernel roofline: executed BF16 MMA flops per GEMM launch
+    flat_R = f.R ** levels
+    mt = f.m_tilde ** levels
+    me = -(-n // mt)
+    pairs = s * (s + 1) // 2
+    kernel_flops = pairs * 2.0 * me * me * me
+    avg_launch_s = (gemm_ms / max(gemm_n, 1)) / 1e3
+    peak_sus, peak_burst, hbm, peak_kind = peaks()
+    achieved = kernel_flops / avg_launch_s / 1e12
+    traffic = None
+    tf = ROOT / "profiles" / "split_gemm_traffic.json"
+    if tf.exists():
+        try:
+            traffic = json.loads(tf.read_text()).get("bytes_per_launch_16384_x2")
+        except ValueError:
+            traffic = None
+    roofline = {"bound": "tensor", "achieved": achieved, "peak": peak_sus, "unit": "TFLOP/s",
+                "frac": achieved / peak_sus, "traffic": traffic,
+                "kernel": "split_gemm_kernel", "peak_kind": f"{peak_kind} bf16 sustained",
+                "flops_per_launch": kernel_flops, "avg_launch_ms": avg_launch_s * 1e3, "launches_timed": gemm_n}
+
+    extra = {}
+    if rank == 0 and not args.no_fp64:
+        # classical FP64 reference result and the plain FP64 FMM, once
+        Cc = C0.clone()
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        fmm.dgemm(A, B, Cc, None, 0, stream=stream)
+        t1.record(stream)
+        torch.cuda.synchronize()
+        ms_cls = t0.elapsed_time(t1)
+        Cf = C0.clone()
+        t0.record(stream)
+        fmm.dgemm(A, B, Cf, f, levels, stream=stream)
+        t1.record(stream)
+        torch.cuda.synchronize()
+        ms_fmm = t0.elapsed_time(t1)
+        Cs = C0.clone()
+        step(Cs)
+        torch.cuda.synchronize()
+        err_fmm = float((Cf - Cc).abs().max())
+        err_split = float((Cs - Cc).abs().max())
+        del Cf, Cs, Cc
+        extra = {
+            "fp64_fmm": {"tflops": flops / ms_fmm / 1e9, "ms": ms_fmm, "max_err_vs_classical": err_fmm},
+            "fp64_classical": {"tflops": flops / ms_cls / 1e9, "ms": ms_cls},
+            "split": {"slices": s, "max_err_vs_classical": err_split,
+                      "err_ratio_to_fp64_fmm": err_split / err_fmm if err_fmm > 0 else None},
+            "speedup_split_vs_fp64_fmm": (flops / ms / 1e9) / (flops / ms_fmm / 1e9),
+            "fp64_fmm_vs_classical": ms_cls / ms_fmm,
+        }
+
+    # end to end through the public API with pinned host buffers
+    e2e = None
+    if rank == 0 and args.e2e_steps > 0:
+        hA = torch.empty((n, n), dtype=torch.float64, pin_memory=True).t()
+        hB = torch.empty((n, n), dtype=torch.float64, pin_memory=True).t()
+        hC = torch.empty((n, n), dtype=torch.float64, pin_memory=True).t()
+        hA.copy_(A)
+        hB.copy_(B)
+        hC.copy_(C0)
+        dA, dB, dC = torch.empty_like(A), torch.empty_like(B), torch.empty_like(C0)
+        torch.cuda.synchronize()
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for _ in range(args.e2e_steps):
+            dA.copy_(hA, non_blocking=True)
+            dB.copy_(hB, non_blocking=True)
+            dC.copy_(hC, non_blocking=True)
+            fmm.split_dgemm(dA, dB, dC, f, levels, s, workspace=ws, stream=stream)
+            hC.copy_(dC, non_blocking=True)
+        t1.record(stream)
+        torch.cuda.synchronize()
+        ms_e2e = t0.elapsed_time(t1) / args.e2e_steps
+        e2e = {"value": flops / ms_e2e / 1e9, "unit": "TFLOP/s", "h2d_bytes_per_step": 3 * n * n * 8,
+               "d2h_bytes_per_step": n * n * 8, "ms_per_step": ms_e2e}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        eff, info = cpu_reference(args.alg, levels, n, 15.0,
+                                  [np.asfortranarray(hA.numpy()), np.asfortranarray(hB.numpy()),
+                                   np.asfortranarray(hC.numpy())])
+        cpu = {"value": eff, "unit": "TFLOP/s", "cores": info["cores"], "kind": "port",
+               "sample": (f"oracle FP64 FMM {args.alg} x{levels} at m=n=k={n}: products 0..{info['products']} "
+                          f"of {info['of']} ({info['seconds']:.1f} s), extrapolated")}
+
+    assert fmm.take_device_error() == 0
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+            "config": {"workload": f"split-BF16 FMM {args.alg} x{levels} levels, m=n=k={n}, {s} slices",
+                       "m": n, "n": n, "k": n, "alg": args.alg, "levels": levels, "slices": s,
+                       "l2": "inputs (3 x 2 GiB) larger than L2; no flush", "parallelism": f"replicas x{world}"},
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+            "clocks": clk.summary(), **extra,
+        }
+        print(json.dumps(out))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -101,6 +101,10 @@ def lib() -> ctypes.CDLL:
     L.fmm_gpu_split_dgemm.restype = ci
     L.fmm_gpu_split_dgemm.argtypes = [pf, ci, i64, i64, i64, dbl, vp, i64, vp, i64, dbl, vp, i64, ci, vp,
                                       ctypes.c_size_t, vp]
+    L.fmm_gpu_set_kernel_timing.restype = None
+    L.fmm_gpu_set_kernel_timing.argtypes = [ci]
+    L.fmm_gpu_read_kernel_timing.restype = ci
+    L.fmm_gpu_read_kernel_timing.argtypes = [ctypes.POINTER(dbl), ctypes.POINTER(ctypes.c_uint64)]
     L.fmm_gpu_launch_count.restype = ctypes.c_uint64
     L.fmm_gpu_launch_count.argtypes = []
     L.fmm_gpu_take_device_error.restype = ci
@@ -154,6 +158,19 @@ def bl_clock() -> float:
 def launch_count() -> int:
     """Kernels this library has launched since it was loaded."""
     return int(lib().fmm_gpu_launch_count())
+
+
+def set_kernel_timing(enable: bool) -> None:
+    """Record CUDA events around each split GEMM kernel launch."""
+    lib().fmm_gpu_set_kernel_timing(1 if enable else 0)
+
+
+def read_kernel_timing() -> tuple[float, int]:
+    """(total milliseconds, launches) of the timed GEMM launches since the last read."""
+    ms = ctypes.c_double(0.0)
+    n = ctypes.c_uint64(0)
+    _check(lib().fmm_gpu_read_kernel_timing(ctypes.byref(ms), ctypes.byref(n)), "read_kernel_timing")
+    return ms.value, int(n.value)
 
 
 def take_device_error() -> int:

@@ -51,6 +51,8 @@
 
 #include <algorithm>
 #include <mutex>
+#include <utility>
+#include <vector>
 
 namespace {
 
@@ -715,7 +717,57 @@ WsLayout ws_layout(const AlgView& alg, int64_t m, int64_t n, int64_t k, int s)
     return L;
 }
 
+/* opt-in event timing of the GEMM launches */
+std::mutex g_timing_mu;
+bool g_timing = false;
+std::vector<std::pair<cudaEvent_t, cudaEvent_t>> g_pending, g_pool;
+
+void timing_mark(cudaStream_t st, bool before)
+{
+    static thread_local std::pair<cudaEvent_t, cudaEvent_t> cur;
+    std::lock_guard<std::mutex> lk(g_timing_mu);
+    if (before) {
+        if (g_pool.empty()) {
+            cudaEvent_t a, b;
+            cudaEventCreate(&a);
+            cudaEventCreate(&b);
+            g_pool.push_back({a, b});
+        }
+        cur = g_pool.back();
+        g_pool.pop_back();
+        cudaEventRecord(cur.first, st);
+    } else {
+        cudaEventRecord(cur.second, st);
+        g_pending.push_back(cur);
+    }
+}
+
 }  // namespace
+
+extern "C" void fmm_gpu_set_kernel_timing(int enable)
+{
+    std::lock_guard<std::mutex> lk(g_timing_mu);
+    g_timing = enable != 0;
+}
+
+extern "C" int fmm_gpu_read_kernel_timing(double* total_ms, uint64_t* launches)
+{
+    std::lock_guard<std::mutex> lk(g_timing_mu);
+    double sum = 0.0;
+    int rc = FMM_OK;
+    for (auto& pr : g_pending) {
+        float ms = 0.f;
+        if (cudaEventSynchronize(pr.second) != cudaSuccess ||
+            cudaEventElapsedTime(&ms, pr.first, pr.second) != cudaSuccess)
+            rc = FMM_ERR_CUDA;
+        sum += ms;
+        g_pool.push_back(pr);
+    }
+    if (launches) *launches = g_pending.size();
+    if (total_ms) *total_ms = sum;
+    g_pending.clear();
+    return rc;
+}
 
 size_t fmm_split_ws_bytes(const AlgView& alg, int64_t m, int64_t n, int64_t k, int slices)
 {
@@ -797,7 +849,10 @@ int fmm_split_launch(const AlgView& alg, int64_t m, int64_t n, int64_t k, double
         launch_packs(s, alg.tab, r, A, lda, B, ldb, m, n, k, m_pad, n_pad, k_pad, e_row, f_col, sa, sb, st);
         ga.w_ent = alg.tab + (ht.w_ent - htab) + 2 * ht.w_off[r];
         ga.nw = nw;
+        const bool timed = g_timing;
+        if (timed) timing_mark(st, true);
         split_gemm_kernel<<<gemm_blocks, kGemmThreads, kGemmSmem, st>>>(tmA, tmB, ga);
+        if (timed) timing_mark(st, false);
         fmm_count_launch(4);
     }
     return cudaGetLastError() == cudaSuccess ? FMM_OK : FMM_ERR_CUDA;

@@ -126,9 +126,9 @@ def test_large_property_f64(fmm, torch_cuda, alg, levels):
     import torch
     n = 2048
     g = torch.Generator(device="cuda").manual_seed(5)
-    A = (torch.rand((n, n), generator=g, device="cuda", dtype=torch.float64) * 2 - 1)
-    B = (torch.rand((n, n), generator=g, device="cuda", dtype=torch.float64) * 2 - 1)
-    C0 = torch.zeros((n, n), device="cuda", dtype=torch.float64)
+    A = (torch.rand((n, n), generator=g, device="cuda", dtype=torch.float64) * 2 - 1).t()
+    B = (torch.rand((n, n), generator=g, device="cuda", dtype=torch.float64) * 2 - 1).t()
+    C0 = torch.zeros((n, n), device="cuda", dtype=torch.float64).t()
     Cc = C0.clone()
     fmm.dgemm(A, B, Cc, None, 0)
     f = fmm.new_fmm(COEFFS / f"{alg}.txt")

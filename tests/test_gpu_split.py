@@ -126,9 +126,9 @@ def test_split_large_accuracy_vs_fp64(fmm, torch_cuda):
     import torch
     n = 4096
     g = torch.Generator(device="cuda").manual_seed(9)
-    A = torch.rand((n, n), generator=g, device="cuda", dtype=torch.float64) * 2 - 1
-    B = torch.rand((n, n), generator=g, device="cuda", dtype=torch.float64) * 2 - 1
-    Cc = torch.zeros((n, n), device="cuda", dtype=torch.float64)
+    A = (torch.rand((n, n), generator=g, device="cuda", dtype=torch.float64) * 2 - 1).t()
+    B = (torch.rand((n, n), generator=g, device="cuda", dtype=torch.float64) * 2 - 1).t()
+    Cc = torch.zeros((n, n), device="cuda", dtype=torch.float64).t()
     fmm.dgemm(A, B, Cc, None, 0)
     f = fmm.strassen_fmm()
     Cf = torch.zeros_like(Cc)
