@@ -255,15 +255,15 @@ def main():
     fmm.set_kernel_timing(False)
     launches = fmm.launch_count() - n_launch0
     ms = max_over_ranks(e0.elapsed_time(e1) / args.steps)
-    gemm_ms, gemm_n = fmm.read_kernel_timing()
+    gemm_ms, gemm_n, gemm_products = fmm.read_kernel_timing()
     value = world * flops / (ms / 1e3) / 1e12
 
-    # dominant kernel roofline: executed BF16 MMA flops per GEMM launch
-    flat_R = f.R ** levels
+    # dominant kernel roofline: executed BF16 MMA flops per GEMM launch (a
+    # launch covers a group of products, each pairs * 2 * me^3)
     mt = f.m_tilde ** levels
     me = -(-n // mt)
     pairs = s * (s + 1) // 2
-    kernel_flops = pairs * 2.0 * me * me * me
+    kernel_flops = pairs * 2.0 * me * me * me * gemm_products / max(gemm_n, 1)
     avg_launch_s = (gemm_ms / max(gemm_n, 1)) / 1e3
     peak_sus, peak_burst, hbm, peak_kind = peaks()
     achieved = kernel_flops / avg_launch_s / 1e12
@@ -277,7 +277,8 @@ def main():
     roofline = {"bound": "tensor", "achieved": achieved, "peak": peak_sus, "unit": "TFLOP/s",
                 "frac": achieved / peak_sus, "traffic": traffic,
                 "kernel": "split_gemm_kernel", "peak_kind": f"{peak_kind} bf16 sustained",
-                "flops_per_launch": kernel_flops, "avg_launch_ms": avg_launch_s * 1e3, "launches_timed": gemm_n}
+                "flops_per_launch": kernel_flops, "avg_launch_ms": avg_launch_s * 1e3, "launches_timed": gemm_n,
+                "products_per_launch": gemm_products / max(gemm_n, 1)}
 
     extra = {}
     if rank == 0 and not args.no_fp64:

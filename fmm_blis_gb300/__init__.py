@@ -104,7 +104,8 @@ def lib() -> ctypes.CDLL:
     L.fmm_gpu_set_kernel_timing.restype = None
     L.fmm_gpu_set_kernel_timing.argtypes = [ci]
     L.fmm_gpu_read_kernel_timing.restype = ci
-    L.fmm_gpu_read_kernel_timing.argtypes = [ctypes.POINTER(dbl), ctypes.POINTER(ctypes.c_uint64)]
+    L.fmm_gpu_read_kernel_timing.argtypes = [ctypes.POINTER(dbl), ctypes.POINTER(ctypes.c_uint64),
+                                             ctypes.POINTER(ctypes.c_uint64)]
     L.fmm_gpu_launch_count.restype = ctypes.c_uint64
     L.fmm_gpu_launch_count.argtypes = []
     L.fmm_gpu_take_device_error.restype = ci
@@ -165,12 +166,15 @@ def set_kernel_timing(enable: bool) -> None:
     lib().fmm_gpu_set_kernel_timing(1 if enable else 0)
 
 
-def read_kernel_timing() -> tuple[float, int]:
-    """(total milliseconds, launches) of the timed GEMM launches since the last read."""
+def read_kernel_timing() -> tuple[float, int, int]:
+    """(total milliseconds, launches, products computed) of the timed GEMM
+    launches since the last read."""
     ms = ctypes.c_double(0.0)
     n = ctypes.c_uint64(0)
-    _check(lib().fmm_gpu_read_kernel_timing(ctypes.byref(ms), ctypes.byref(n)), "read_kernel_timing")
-    return ms.value, int(n.value)
+    p = ctypes.c_uint64(0)
+    _check(lib().fmm_gpu_read_kernel_timing(ctypes.byref(ms), ctypes.byref(n), ctypes.byref(p)),
+           "read_kernel_timing")
+    return ms.value, int(n.value), int(p.value)
 
 
 def take_device_error() -> int:

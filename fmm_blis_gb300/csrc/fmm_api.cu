@@ -60,6 +60,17 @@ std::vector<int> build_table(const fmm_t* f)
     t.insert(t.end(), eu.begin(), eu.end());
     t.insert(t.end(), ev.begin(), ev.end());
     t.insert(t.end(), ew.begin(), ew.end());
+    /* W by C sub-block: for each part p, its (product, coef) entries in
+     * increasing product order */
+    std::vector<int> off_p(c + 1), ep;
+    for (int q = 0; q < c; ++q) {
+        off_p[q] = (int)ep.size() / 2;
+        for (int r = 0; r < R; ++r)
+            if (int x = f->W[(size_t)q * R + r]) { ep.push_back(r); ep.push_back(x); }
+    }
+    off_p[c] = (int)ep.size() / 2;
+    t.insert(t.end(), off_p.begin(), off_p.end());
+    t.insert(t.end(), ep.begin(), ep.end());
     return t;
 }
 

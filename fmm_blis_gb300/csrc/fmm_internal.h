@@ -8,7 +8,9 @@
  *   [4 .. 4+R]           u_off : start of product r's U entries (R+1 values)
  *   [.. +R+1]            v_off
  *   [.. +R+1]            w_off
- *   then U entries (part, coef) pairs, V entries, W entries.
+ *   then U entries (part, coef) pairs, V entries, W entries,
+ *   then wp_off (m~n~ + 1 values) and the W entries grouped by C sub-block,
+ *   (product, coef) pairs in increasing product order.
  *
  * Only nonzero coefficients are stored, in increasing part order, so the
  * kernels add the A (B) sub-blocks in the same order as the reference's pack

@@ -57,17 +57,19 @@
 namespace {
 
 constexpr int kTileM = 128;
-constexpr int kTileN = 128;
+constexpr int kTileN = 256;             /* N = 256: 128 clocks per MMA hide the accumulator dependency */
 constexpr int kBK = 64;                 /* k elements per stage (128 bytes of BF16) */
-constexpr int kStages = 6;
+constexpr int kStages = 4;
 constexpr int kChunkKB = 4;             /* k-blocks per exact FP32 chunk: 256 terms */
-constexpr int kEpiWarps = 8;       /* two per TMEM lane quarter, 64 columns each */
-constexpr int kGemmThreads = 64 + 32 * kEpiWarps;
-constexpr uint32_t kTileBytes = kTileM * kBK * 2;  /* 16 KB, same for A and B */
-constexpr uint32_t kStageBytes = 2 * kTileBytes;
-constexpr int kTmemCols = 512;          /* 2 x 128 accumulator columns + 256 for Z */
-constexpr int kZLoCol = 256, kZHiCol = 384;
+constexpr int kEpiWarps = 8;           /* two per TMEM lane quarter */
+constexpr int kEpiCols = kTileN / 2;    /* columns per epilogue thread */
+constexpr int kGemmThreads = 64 + 32 * kEpiWarps;  /* TMA warp, MMA warp, epilogue warps */
+constexpr uint32_t kATileBytes = kTileM * kBK * 2;  /* 16 KB */
+constexpr uint32_t kBTileBytes = kTileN * kBK * 2;  /* 32 KB */
+constexpr uint32_t kStageBytes = kATileBytes + kBTileBytes;
+constexpr int kTmemCols = 512;          /* 2 x 256 accumulator columns */
 constexpr int kMaxKe = 16384;
+constexpr int kRasterGroup = 12;        /* tile rows per raster band */
 constexpr size_t kGemmSmem = (size_t)kStages * kStageBytes + 1024 + 256;
 
 __host__ __device__ __forceinline__ int64_t round_up(int64_t x, int64_t m) { return (x + m - 1) / m * m; }
@@ -138,6 +140,7 @@ struct Tab {
     int mt, kt, nt, R;
     const int* u_off; const int* v_off; const int* w_off;
     const int* u_ent; const int* v_ent; const int* w_ent;
+    const int* wp_off; const int* wp_ent;
 };
 
 __host__ __device__ __forceinline__ Tab tab_view(const int* tab)
@@ -150,6 +153,8 @@ __host__ __device__ __forceinline__ Tab tab_view(const int* tab)
     t.u_ent = t.w_off + (t.R + 1);
     t.v_ent = t.u_ent + 2 * t.u_off[t.R];
     t.w_ent = t.v_ent + 2 * t.v_off[t.R];
+    t.wp_off = t.w_ent + 2 * t.w_off[t.R];
+    t.wp_ent = t.wp_off + (t.mt * t.nt + 1);
     return t;
 }
 
@@ -416,55 +421,20 @@ struct GemmArgs {
     int s;                /* slices */
     int zlevel;           /* G: the level whose unit Z counts in */
     int nkb;              /* k_pad / 64 */
-    int tiles_m;
-    int m_pad, n_pad;
-    int64_t m, n;         /* full C sizes (sub-block geometry) */
-    int mt, nt;
-    const int* e_row;
-    const int* f_col;
-    const int* w_ent;     /* this product's W entries (part, coef) */
-    int nw;
-    double alpha;
-    double* C;
-    int64_t ldc;
+    int tiles_m, tiles_n; /* per product */
+    int m_pad, n_pad;     /* rows per slice in the A / B slice arrays */
+    int64_t* Z;           /* [product][n_pad][m_pad] int64 level accumulators */
     int* err;
 };
 
 __device__ __forceinline__ int level_pairs(int g, int s) { return min(s, g - 1) - max(1, g - s) + 1; }
 
-/* Z (TMEM, 64-bit as lo/hi columns, in units of level G) += the level-g sum
- * L of this thread's row and 64 columns, with D = G - g: exact left shift by
- * 8D for D >= 0, rounded right shift by -8D (ties up) for D < 0. */
-template <int D>
-__device__ __forceinline__ void fold_level(const int* L, uint32_t tz, bool first)
-{
-#pragma unroll
-    for (int h = 0; h < 4; ++h) {
-        uint32_t lo[16], hi[16];
-        const uint32_t zc = h * 16;
-        if (first) {
-#pragma unroll
-            for (int x = 0; x < 16; ++x) { lo[x] = 0; hi[x] = 0; }
-        } else {
-            SM103_TMEM_LD_X16(tz + kZLoCol + zc, lo);
-            SM103_TMEM_LD_X16(tz + kZHiCol + zc, hi);
-            sm103::tmem_wait_ld();
-        }
-#pragma unroll
-        for (int x = 0; x < 16; ++x) {
-            int64_t z = (int64_t)(((uint64_t)hi[x] << 32) | lo[x]);
-            const int64_t lv = L[h * 16 + x];
-            if (D >= 0) z += lv * ((int64_t)1 << (8 * D));
-            else z += (lv + ((int64_t)1 << (-8 * D - 1))) >> (-8 * D);
-            lo[x] = (uint32_t)(uint64_t)z;
-            hi[x] = (uint32_t)((uint64_t)z >> 32);
-        }
-        SM103_TMEM_ST_X16(tz + kZLoCol + zc, lo);
-        SM103_TMEM_ST_X16(tz + kZHiCol + zc, hi);
-    }
-    sm103::tmem_wait_st();
-}
-
+/* One CTA per work item (product r of the group, 128 x 256 output tile):
+ * warp 0 issues the TMA loads of the digit-slice tiles, warp 1 the
+ * tcgen05.mma (M=128, N=256, K=16: long enough per instruction to hide the
+ * accumulator dependency), warps 2..9 drain each exact 256-term chunk from
+ * the double-buffered TMEM accumulator into int32 level sums and fold each
+ * finished level into the product's 64-bit Z tile in global memory. */
 __global__ void __launch_bounds__(kGemmThreads, 1)
 split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                   const GemmArgs a)
@@ -472,7 +442,7 @@ split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint8_t* sA = smem;
-    uint8_t* sB = smem + kStages * kTileBytes;
+    uint8_t* sB = smem + kStages * kATileBytes;
     uint64_t* full = (uint64_t*)(smem + kStages * kStageBytes);
     uint64_t* empty = full + kStages;
     uint64_t* accf = empty + kStages;
@@ -482,7 +452,20 @@ split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
 
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-    const int tile_m = blockIdx.x % a.tiles_m, tile_n = blockIdx.x / a.tiles_m;
+    /* work item: product r (outermost, so resident CTAs share slices in L2),
+     * then a grouped raster of kRasterGroup tile rows */
+    const int per_prod = a.tiles_m * a.tiles_n;
+    const int r = blockIdx.x / per_prod;
+    int tile_m, tile_n;
+    {
+        const int id = blockIdx.x % per_prod;
+        const int per_group = kRasterGroup * a.tiles_n;
+        const int grp = id / per_group, first_m = grp * kRasterGroup;
+        const int gm = min(a.tiles_m - first_m, kRasterGroup);
+        const int in_grp = id % per_group;
+        tile_m = first_m + in_grp % gm;
+        tile_n = in_grp / gm;
+    }
 
     if (threadIdx.x == 0) {
         for (int i = 0; i < kStages; ++i) { sm103::mbar_init(&full[i], 1); sm103::mbar_init(&empty[i], 1); }
@@ -506,16 +489,18 @@ split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
             uint32_t ph = 0;
             uint32_t armed = 0;  /* stages armed in the current pass (bit mask) */
             bool ok = true;
+            const int arow = r * s * a.m_pad + tile_m * kTileM;
+            const int brow = r * s * a.n_pad + tile_n * kTileN;
             for (int g = 2; g <= s + 1 && ok; ++g)
                 for (int t = max(1, g - s); t <= min(s, g - 1) && ok; ++t) {
                     const int u = g - t;
                     for (int kb = 0; kb < nkb; ++kb) {
                         if (!sm103::mbar_wait(&empty[st], ph ^ 1, abort_flag, a.err, 1)) { ok = false; break; }
                         sm103::mbar_arrive_expect_tx(&full[st], kStageBytes);
-                        sm103::tma_load_2d(sA + st * kTileBytes, &tmA, &full[st], kb * kBK,
-                                           (t - 1) * a.m_pad + tile_m * kTileM);
-                        sm103::tma_load_2d(sB + st * kTileBytes, &tmB, &full[st], kb * kBK,
-                                           (u - 1) * a.n_pad + tile_n * kTileN);
+                        sm103::tma_load_2d(sA + st * kATileBytes, &tmA, &full[st], kb * kBK,
+                                           arow + (t - 1) * a.m_pad);
+                        sm103::tma_load_2d(sB + st * kBTileBytes, &tmB, &full[st], kb * kBK,
+                                           brow + (u - 1) * a.n_pad);
                         armed |= 1u << st;
                         if (++st == kStages) { st = 0; ph ^= 1; armed = 0; }
                     }
@@ -548,8 +533,8 @@ split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
                         }
                         if (!sm103::mbar_wait(&full[st], ph, abort_flag, a.err, 3)) { ok = false; break; }
                         sm103::tc_fence_after();
-                        const uint32_t a0 = sm103::smem_u32(sA + st * kTileBytes);
-                        const uint32_t b0 = sm103::smem_u32(sB + st * kTileBytes);
+                        const uint32_t a0 = sm103::smem_u32(sA + st * kATileBytes);
+                        const uint32_t b0 = sm103::smem_u32(sB + st * kBTileBytes);
 #pragma unroll
                         for (int kk = 0; kk < kBK / 16; ++kk)
                             sm103::mma_bf16(tmem + buf * kTileN, sm103::smem_desc_sw128(a0 + kk * 32),
@@ -572,29 +557,31 @@ split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         }
     } else {
         /* ---------------- epilogue warps ---------------- */
-        const int quarter = warp % 4;          /* TMEM lane quarter this warp may access */
-        const int colbase = ((warp - 2) / 4) * 64;
+        const int quarter = warp % 4;                  /* TMEM lane quarter this warp may access */
+        const int colbase = ((warp - 2) / 4) * kEpiCols;
         const int row = quarter * 32 + lane;
         const uint32_t tl = tmem + ((uint32_t)(quarter * 32) << 16);
+        int64_t* zrow = a.Z + (int64_t)r * a.n_pad * a.m_pad + (int64_t)(tile_n * kTileN + colbase) * a.m_pad +
+                        tile_m * kTileM + row;
         int buf = 0;
         uint32_t aph = 0;
         bool ok = true;
         for (int g = 2; g <= s + 1 && ok; ++g) {
-            int L[64];
+            int L[kEpiCols];
 #pragma unroll
-            for (int x = 0; x < 64; ++x) L[x] = 0;
+            for (int x = 0; x < kEpiCols; ++x) L[x] = 0;
             const int nchunks = (level_pairs(g, s) * nkb + kChunkKB - 1) / kChunkKB;
             for (int c = 0; c < nchunks; ++c) {
                 if (!sm103::mbar_wait(&accf[buf], aph, abort_flag, a.err, 4)) { ok = false; break; }
                 sm103::tc_fence_after();
 #pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    uint32_t v[32];
-                    SM103_TMEM_LD_X32(tl + buf * kTileN + colbase + h * 32, v);
+                for (int h = 0; h < kEpiCols / 8; ++h) {
+                    uint32_t v[8];
+                    SM103_TMEM_LD_X8(tl + buf * kTileN + colbase + h * 8, v);
                     sm103::tmem_wait_ld();
 #pragma unroll
-                    for (int x = 0; x < 32; ++x)
-                        L[h * 32 + x] += (int)__float_as_uint(__uint_as_float(v[x]) + 12582912.0f) - 0x4B400000;
+                    for (int x = 0; x < 8; ++x)
+                        L[h * 8 + x] += (int)__float_as_uint(__uint_as_float(v[x]) + 12582912.0f) - 0x4B400000;
                 }
                 sm103::tc_fence_before();
                 __syncwarp();
@@ -603,54 +590,24 @@ split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
                 if (buf == 0) aph ^= 1;
             }
             if (!ok) break;
-            /* fold L_g into Z (units of level G) */
-            const bool first = g == 2;
-            switch (a.zlevel - g) {
-            case 5: fold_level<5>(L, tl + colbase, first); break;
-            case 4: fold_level<4>(L, tl + colbase, first); break;
-            case 3: fold_level<3>(L, tl + colbase, first); break;
-            case 2: fold_level<2>(L, tl + colbase, first); break;
-            case 1: fold_level<1>(L, tl + colbase, first); break;
-            case 0: fold_level<0>(L, tl + colbase, first); break;
-            case -1: fold_level<-1>(L, tl + colbase, first); break;
-            case -2: fold_level<-2>(L, tl + colbase, first); break;
-            default: fold_level<-3>(L, tl + colbase, first); break;
-            }
-        }
-        if (ok) {
-            /* M_r tile = 2^(E_i + F_j - 46) * Z, added into the C sub-blocks */
-            const int64_t gi = (int64_t)tile_m * kTileM + row;
-            const int Ei = gi < a.m_pad ? a.e_row[gi] : 0;
-#pragma unroll 1
-            for (int h = 0; h < 4; ++h) {
-                uint32_t lo[16], hi[16];
-                const uint32_t zc = colbase + h * 16;
-                SM103_TMEM_LD_X16(tl + kZLoCol + zc, lo);
-                SM103_TMEM_LD_X16(tl + kZHiCol + zc, hi);
-                sm103::tmem_wait_ld();
-                const int64_t gj0 = (int64_t)tile_n * kTileN + zc;
-                double val[16];
+            /* fold L_g into the Z tile (units of level G): D = G - g, exact
+             * left shift by 8D for D >= 0, rounded right shift by -8D (ties
+             * up) for D < 0; the first level stores instead of adding */
+            {
+                const int D = a.zlevel - g;
+                const int64_t mul = D >= 0 ? ((int64_t)1 << (8 * (D >= 0 ? D : 0))) : 1;
+                const int rsh = D >= 0 ? 0 : -8 * D;
+                const int64_t rnd = D >= 0 ? 0 : ((int64_t)1 << (rsh - 1));
+                const bool first = g == 2;
 #pragma unroll
-                for (int x = 0; x < 16; ++x) {
-                    const int64_t z = (int64_t)(((uint64_t)hi[x] << 32) | lo[x]);
-                    val[x] = scale2((double)z, Ei + a.f_col[gj0 + x] + 2 - 8 * a.zlevel);
-                }
-                for (int e = 0; e < a.nw; ++e) {
-                    const int part = a.w_ent[2 * e];
-                    const double lam = a.alpha * (double)a.w_ent[2 * e + 1];
-                    int ro, rl, co, cl;
-                    fmm_part_geom32((int)a.m, a.mt, part / a.nt, &ro, &rl);
-                    fmm_part_geom32((int)a.n, a.nt, part % a.nt, &co, &cl);
-                    if (gi >= rl) continue;
-                    double* cb = a.C + ro + gi + (int64_t)co * a.ldc;
+                for (int h = 0; h < kEpiCols / 4; ++h) {
+                    int64_t zv[4];
 #pragma unroll
-                    for (int x = 0; x < 16; ++x) {
-                        const int64_t gj = gj0 + x;
-                        if (gj < cl) {
-                            double* p = cb + gj * a.ldc;
-                            *p = fma(lam, val[x], *p);
-                        }
-                    }
+                    for (int x = 0; x < 4; ++x) zv[x] = first ? 0 : zrow[(int64_t)(h * 4 + x) * a.m_pad];
+#pragma unroll
+                    for (int x = 0; x < 4; ++x)
+                        zrow[(int64_t)(h * 4 + x) * a.m_pad] = zv[x] + (((int64_t)L[h * 4 + x] * mul + rnd) >> rsh);
+                    asm volatile("" ::: "memory");
                 }
             }
         }
@@ -659,6 +616,82 @@ split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     __syncthreads();
     sm103::tc_fence_after();
     if (warp == 1) sm103::tmem_dealloc(tmem, kTmemCols);
+}
+
+/* (double)z * 2^e for |z| < 2^62 in integer arithmetic (round to nearest
+ * even, then exponent offset), identical to the FP64 conversion and
+ * power-of-two scaling whenever the result is a normal number; other cases
+ * take the FP64 route. Keeps the per-element FP64 work to the C updates. */
+__device__ __forceinline__ double i64_to_double_scaled(int64_t z, int e)
+{
+    if (z == 0) return 0.0;
+    const uint64_t sign = z < 0 ? 0x8000000000000000ull : 0ull;
+    uint64_t u = z < 0 ? (uint64_t)(-z) : (uint64_t)z;
+    int p = 63 - __clzll((long long)u);
+    uint64_t m;
+    if (p <= 52) {
+        m = u << (52 - p);
+    } else {
+        const int sh = p - 52;
+        m = u >> sh;
+        const uint64_t rem = u & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+        if (rem > half || (rem == half && (m & 1))) {
+            ++m;
+            if (m == (1ull << 53)) { m >>= 1; ++p; }
+        }
+    }
+    const int be = p + 1023 + e;
+    if (be < 1 || be > 2046) return scale2((double)z, e);
+    return __longlong_as_double((long long)(sign | ((uint64_t)be << 52) | (m & 0x000fffffffffffffull)));
+}
+
+/* Multi-C epilogue for a group of products [r0, r0 + nprod): each thread
+ * owns one element (i, j) of the sub-block grid; for every C sub-block p
+ * containing it, C_p[i,j] is updated in increasing product order with
+ * alpha*W[p,r] * M_r[i,j], M_r[i,j] = 2^(E_i + F_j + 2 - 8G) * Z_r[i,j]
+ * (plugin/ref_kernels/bli_gemm_fmm_ref.c:99-120, once per group instead of
+ * once per product). */
+constexpr int kScatterMaxEnt = 4096;
+
+__global__ void __launch_bounds__(256)
+scatter_kernel(const int* __restrict__ tab, int r0, int nprod, int64_t m, int64_t n,
+               int m_pad, int n_pad, int zlevel, double alpha, const int64_t* __restrict__ Z,
+               const int* __restrict__ e_row, const int* __restrict__ f_col, double* __restrict__ C,
+               int64_t ldc)
+{
+    __shared__ double lam[kScatterMaxEnt];
+    const Tab t = tab_view(tab);
+    const int P = t.mt * t.nt;
+    const int nent = t.wp_off[P];
+    for (int e = threadIdx.x; e < nent && e < kScatterMaxEnt; e += blockDim.x)
+        lam[e] = alpha * (double)t.wp_ent[2 * e + 1];
+    __syncthreads();
+    const int me = (int)((m + t.mt - 1) / t.mt), ne = (int)((n + t.nt - 1) / t.nt);
+    const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int i = (int)(idx % me), j = (int)(idx / me);
+    if (j >= ne) return;
+    const int64_t zij = (int64_t)j * m_pad + i;
+    const int64_t zstride = (int64_t)n_pad * m_pad;
+    for (int p = 0; p < P; ++p) {
+        int ro, rl, co, cl;
+        fmm_part_geom32((int)m, t.mt, p / t.nt, &ro, &rl);
+        fmm_part_geom32((int)n, t.nt, p % t.nt, &co, &cl);
+        if (i >= rl || j >= cl) continue;
+        const int eb = t.wp_off[p], ee = t.wp_off[p + 1];
+        double* cp = C + ro + i + (int64_t)(co + j) * ldc;
+        double c = *cp;
+        bool touched = false;
+        for (int e = eb; e < ee; ++e) {
+            const int r = t.wp_ent[2 * e] - r0;
+            if (r < 0) continue;
+            if (r >= nprod) break;
+            const int64_t z = Z[r * zstride + zij];
+            const double v = i64_to_double_scaled(z, e_row[r * m_pad + i] + f_col[r * n_pad + j] + 2 - 8 * zlevel);
+            c = fma(e < kScatterMaxEnt ? lam[e] : alpha * (double)t.wp_ent[2 * e + 1], v, c);
+            touched = true;
+        }
+        if (touched) *cp = c;
+    }
 }
 
 /* --------------------------------------------------------- host -------- */
@@ -679,13 +712,15 @@ PFN_cuTensorMapEncodeTiled_v12000 get_encode_fn()
 
 /* 2-D map over slices[rows_total][k_pad] BF16, box 64 (k) x 128 (rows),
  * 128-byte swizzle. */
-int make_slice_map(CUtensorMap* map, const void* base, int64_t k_pad, int64_t rows_total)
+/* 2-D map over slices[rows_total][k_pad] BF16, box 64 (k) x box_rows, 128-byte
+ * swizzle. */
+int make_slice_map(CUtensorMap* map, const void* base, int64_t k_pad, int64_t rows_total, int box_rows)
 {
     PFN_cuTensorMapEncodeTiled_v12000 enc = get_encode_fn();
     if (!enc) return FMM_ERR_CUDA;
     cuuint64_t dims[2] = {(cuuint64_t)k_pad, (cuuint64_t)rows_total};
     cuuint64_t strides[1] = {(cuuint64_t)(k_pad * 2)};
-    cuuint32_t box[2] = {(cuuint32_t)kBK, (cuuint32_t)kTileM};
+    cuuint32_t box[2] = {(cuuint32_t)kBK, (cuuint32_t)box_rows};
     cuuint32_t estr[2] = {1, 1};
     CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box,
                      estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
@@ -693,26 +728,65 @@ int make_slice_map(CUtensorMap* map, const void* base, int64_t k_pad, int64_t ro
     return r == CUDA_SUCCESS ? FMM_OK : FMM_ERR_CUDA;
 }
 
+/* Products are processed in groups: all products of a group are packed, then
+ * one GEMM launch covers every (product, tile) work item of the group, then
+ * one scatter pass updates C. The group size is the largest that keeps the
+ * per-group workspace (slices + Z) under kGroupBudget. */
+constexpr size_t kGroupBudget = (size_t)12 << 30;
+
+struct Dims {
+    int64_t me, ne, ke, m_pad, n_pad, k_pad;
+};
+
+Dims dims_of(const AlgView& alg, int64_t m, int64_t n, int64_t k)
+{
+    Dims d;
+    d.me = (m + alg.mt - 1) / alg.mt;
+    d.ne = (n + alg.nt - 1) / alg.nt;
+    d.ke = (k + alg.kt - 1) / alg.kt;
+    d.m_pad = round_up(std::max<int64_t>(d.me, 1), kTileM);
+    d.n_pad = round_up(std::max<int64_t>(d.ne, 1), kTileN);
+    d.k_pad = round_up(std::max<int64_t>(d.ke, 1), kBK);
+    return d;
+}
+
+size_t per_product_bytes(const Dims& d, int s)
+{
+    return 2 * (size_t)s * (size_t)(d.m_pad + d.n_pad) * (size_t)d.k_pad +
+           8 * (size_t)d.m_pad * (size_t)d.n_pad + 4 * (size_t)(d.m_pad + d.n_pad) + 1024;
+}
+
+int group_size(const AlgView& alg, const Dims& d, int s)
+{
+    const size_t per = per_product_bytes(d, s);
+    size_t g = kGroupBudget / per;
+    if (g < 1) g = 1;
+    if (g > (size_t)alg.R) g = (size_t)alg.R;
+    /* tensor-map row coordinates are 32-bit */
+    while (g > 1 && (int64_t)g * s * std::max(d.m_pad, d.n_pad) > 0x7fffffffLL) --g;
+    return (int)g;
+}
+
 struct WsLayout {
-    size_t amax, bmax, erow, fcol, sa, sb, total;
+    size_t amax, bmax, erow, fcol, sa, sb, z, total;
+    int group;
 };
 
 WsLayout ws_layout(const AlgView& alg, int64_t m, int64_t n, int64_t k, int s)
 {
-    const int64_t me = (m + alg.mt - 1) / alg.mt, ne = (n + alg.nt - 1) / alg.nt,
-                  ke = (k + alg.kt - 1) / alg.kt;
-    const int64_t m_pad = round_up(std::max<int64_t>(me, 1), kTileM);
-    const int64_t n_pad = round_up(std::max<int64_t>(ne, 1), kTileN);
-    const int64_t k_pad = round_up(std::max<int64_t>(ke, 1), kBK);
+    const Dims d = dims_of(alg, m, n, k);
+    const int G = group_size(alg, d, s);
     WsLayout L;
     size_t off = 0;
     auto take = [&](size_t bytes) { size_t o = off; off += (bytes + 255) / 256 * 256; return o; };
+    L.group = G;
     L.amax = take(sizeof(unsigned long long) * (size_t)alg.kt * (size_t)m);
     L.bmax = take(sizeof(unsigned long long) * (size_t)alg.kt * (size_t)n);
-    L.erow = take(sizeof(int) * (size_t)m_pad);
-    L.fcol = take(sizeof(int) * (size_t)n_pad);
-    L.sa = take(2 * (size_t)s * (size_t)m_pad * (size_t)k_pad);
-    L.sb = take(2 * (size_t)s * (size_t)n_pad * (size_t)k_pad);
+    L.erow = take(sizeof(int) * (size_t)G * (size_t)d.m_pad);
+    L.fcol = take(sizeof(int) * (size_t)G * (size_t)d.n_pad);
+    L.sa = take(2 * (size_t)G * s * (size_t)d.m_pad * (size_t)d.k_pad);
+    L.sb = take(2 * (size_t)G * s * (size_t)d.n_pad * (size_t)d.k_pad);
+    L.z = take(8 * (size_t)G * (size_t)d.m_pad * (size_t)d.n_pad);
     L.total = off;
     return L;
 }
@@ -721,6 +795,7 @@ WsLayout ws_layout(const AlgView& alg, int64_t m, int64_t n, int64_t k, int s)
 std::mutex g_timing_mu;
 bool g_timing = false;
 std::vector<std::pair<cudaEvent_t, cudaEvent_t>> g_pending, g_pool;
+uint64_t g_timed_products = 0;
 
 void timing_mark(cudaStream_t st, bool before)
 {
@@ -750,7 +825,7 @@ extern "C" void fmm_gpu_set_kernel_timing(int enable)
     g_timing = enable != 0;
 }
 
-extern "C" int fmm_gpu_read_kernel_timing(double* total_ms, uint64_t* launches)
+extern "C" int fmm_gpu_read_kernel_timing(double* total_ms, uint64_t* launches, uint64_t* products)
 {
     std::lock_guard<std::mutex> lk(g_timing_mu);
     double sum = 0.0;
@@ -764,8 +839,10 @@ extern "C" int fmm_gpu_read_kernel_timing(double* total_ms, uint64_t* launches)
         g_pool.push_back(pr);
     }
     if (launches) *launches = g_pending.size();
+    if (products) *products = g_timed_products;
     if (total_ms) *total_ms = sum;
     g_pending.clear();
+    g_timed_products = 0;
     return rc;
 }
 
@@ -783,14 +860,11 @@ int fmm_split_launch(const AlgView& alg, int64_t m, int64_t n, int64_t k, double
     if (rc != FMM_OK) return rc;
     if (m == 0 || n == 0 || k == 0 || alpha == 0.0) return FMM_OK;
     if (alg.max_nnz_u > kPackMaxEnt || alg.max_nnz_v > kPackMaxEnt) return FMM_ERR_UNSUPPORTED;
-    const int64_t me = (m + alg.mt - 1) / alg.mt, ne = (n + alg.nt - 1) / alg.nt,
-                  ke = (k + alg.kt - 1) / alg.kt;
-    if (ke > kMaxKe) return FMM_ERR_UNSUPPORTED;
-    const int64_t m_pad = round_up(me, kTileM), n_pad = round_up(ne, kTileN), k_pad = round_up(ke, kBK);
-    if ((m_pad / kTileM) * (n_pad / kTileN) > 0x7fffffffLL || m_pad * s > 0x7fffffffLL ||
-        n_pad * s > 0x7fffffffLL)
-        return FMM_ERR_UNSUPPORTED;
+    if (m > 0x7fffffffLL || n > 0x7fffffffLL) return FMM_ERR_UNSUPPORTED;
+    const Dims d = dims_of(alg, m, n, k);
+    if (d.ke > kMaxKe) return FMM_ERR_UNSUPPORTED;
     const WsLayout L = ws_layout(alg, m, n, k, s);
+    if ((int64_t)L.group * s * std::max(d.m_pad, d.n_pad) > 0x7fffffffLL) return FMM_ERR_UNSUPPORTED;
     if (ws == nullptr || ws_bytes < L.total) return FMM_ERR_WORKSPACE;
     if (((uintptr_t)ws & 255) != 0) return FMM_ERR_ARG;
 
@@ -801,6 +875,8 @@ int fmm_split_launch(const AlgView& alg, int64_t m, int64_t n, int64_t k, double
     int* f_col = (int*)(w + L.fcol);
     uint16_t* sa = (uint16_t*)(w + L.sa);
     uint16_t* sb = (uint16_t*)(w + L.sb);
+    int64_t* Z = (int64_t*)(w + L.z);
+    const int G = L.group;
 
     static bool attr_set = false;
     if (!attr_set) {
@@ -810,50 +886,57 @@ int fmm_split_launch(const AlgView& alg, int64_t m, int64_t n, int64_t k, double
         attr_set = true;
     }
     CUtensorMap tmA, tmB;
-    if (make_slice_map(&tmA, sa, k_pad, m_pad * s) != FMM_OK) return FMM_ERR_CUDA;
-    if (make_slice_map(&tmB, sb, k_pad, n_pad * s) != FMM_OK) return FMM_ERR_CUDA;
+    if (make_slice_map(&tmA, sa, d.k_pad, (int64_t)G * s * d.m_pad, kTileM) != FMM_OK) return FMM_ERR_CUDA;
+    if (make_slice_map(&tmB, sb, d.k_pad, (int64_t)G * s * d.n_pad, kTileN) != FMM_OK) return FMM_ERR_CUDA;
 
     /* per-sub-block row/column maxima, once per call */
     if (cudaMemsetAsync(amax, 0, sizeof(unsigned long long) * (size_t)alg.kt * (size_t)m, st) != cudaSuccess)
         return FMM_ERR_CUDA;
     {
         const int cpb = 256;
-        const int64_t kb_max = (k + alg.kt - 1) / alg.kt;
-        dim3 grid((unsigned)((m + 255) / 256), (unsigned)alg.kt, (unsigned)((kb_max + cpb - 1) / cpb));
+        dim3 grid((unsigned)((m + 255) / 256), (unsigned)alg.kt, (unsigned)((d.ke + cpb - 1) / cpb));
         amax_kernel<<<grid, 256, 0, st>>>(A, lda, m, k, alg.kt, amax, cpb);
         const int64_t warps = n * alg.kt;
         bmax_kernel<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, st>>>(B, ldb, k, n, alg.kt, bmax);
         fmm_count_launch(2);
     }
-    const int* htab = alg.htab;
-    const Tab ht = tab_view(htab);
     GemmArgs ga;
     ga.s = s;
-    ga.zlevel = k_pad <= 128 ? 7 : 6;
-    ga.nkb = (int)(k_pad / kBK);
-    ga.tiles_m = (int)(m_pad / kTileM);
-    ga.m_pad = (int)m_pad;
-    ga.n_pad = (int)n_pad;
-    ga.m = m; ga.n = n;
-    ga.mt = alg.mt; ga.nt = alg.nt;
-    ga.e_row = e_row; ga.f_col = f_col;
-    ga.alpha = alpha;
-    ga.C = C; ga.ldc = ldc;
+    ga.zlevel = d.k_pad <= 128 ? 7 : 6;
+    ga.nkb = (int)(d.k_pad / kBK);
+    ga.tiles_m = (int)(d.m_pad / kTileM);
+    ga.tiles_n = (int)(d.n_pad / kTileN);
+    ga.m_pad = (int)d.m_pad;
+    ga.n_pad = (int)d.n_pad;
+    ga.Z = Z;
     ga.err = fmm_device_error_word();
-    const unsigned gemm_blocks = (unsigned)((m_pad / kTileM) * (n_pad / kTileN));
-    for (int r = 0; r < alg.R; ++r) {
-        const int nw = ht.w_off[r + 1] - ht.w_off[r];
-        if (nw == 0) continue;
-        exps_kernel<<<(unsigned)((m_pad + n_pad + 255) / 256), 256, 0, st>>>(
-            alg.tab, r, m, n, k, m_pad, n_pad, amax, bmax, e_row, f_col);
-        launch_packs(s, alg.tab, r, A, lda, B, ldb, m, n, k, m_pad, n_pad, k_pad, e_row, f_col, sa, sb, st);
-        ga.w_ent = alg.tab + (ht.w_ent - htab) + 2 * ht.w_off[r];
-        ga.nw = nw;
+    const int64_t tiles = (int64_t)ga.tiles_m * ga.tiles_n;
+    for (int r0 = 0; r0 < alg.R; r0 += G) {
+        const int np = std::min(G, alg.R - r0);
+        for (int q = 0; q < np; ++q) {
+            const int r = r0 + q;
+            int* er = e_row + (int64_t)q * d.m_pad;
+            int* fc = f_col + (int64_t)q * d.n_pad;
+            exps_kernel<<<(unsigned)((d.m_pad + d.n_pad + 255) / 256), 256, 0, st>>>(
+                alg.tab, r, m, n, k, d.m_pad, d.n_pad, amax, bmax, er, fc);
+            launch_packs(s, alg.tab, r, A, lda, B, ldb, m, n, k, d.m_pad, d.n_pad, d.k_pad, er, fc,
+                         sa + (int64_t)q * s * d.m_pad * d.k_pad, sb + (int64_t)q * s * d.n_pad * d.k_pad, st);
+            fmm_count_launch(3);
+        }
+        if (np * tiles > 0x7fffffffLL) return FMM_ERR_UNSUPPORTED;
         const bool timed = g_timing;
-        if (timed) timing_mark(st, true);
-        split_gemm_kernel<<<gemm_blocks, kGemmThreads, kGemmSmem, st>>>(tmA, tmB, ga);
+        if (timed) {
+            timing_mark(st, true);
+            std::lock_guard<std::mutex> lk(g_timing_mu);
+            g_timed_products += (uint64_t)np;
+        }
+        split_gemm_kernel<<<(unsigned)(np * tiles), kGemmThreads, kGemmSmem, st>>>(tmA, tmB, ga);
         if (timed) timing_mark(st, false);
-        fmm_count_launch(4);
+        fmm_count_launch(1);
+        const int64_t elems = d.me * d.ne;
+        scatter_kernel<<<(unsigned)((elems + 255) / 256), 256, 0, st>>>(
+            alg.tab, r0, np, m, n, (int)d.m_pad, (int)d.n_pad, ga.zlevel, alpha, Z, e_row, f_col, C, ldc);
+        fmm_count_launch(1);
     }
     return cudaGetLastError() == cudaSuccess ? FMM_OK : FMM_ERR_CUDA;
 }

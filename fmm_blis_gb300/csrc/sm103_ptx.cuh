@@ -96,6 +96,14 @@ __device__ __forceinline__ void prefetch_tmap(const void* tmap)
     asm volatile("prefetch.tensormap [%0];" ::"l"(tmap) : "memory");
 }
 
+/* Per-warpgroup register reallocation (all four warps of a warpgroup execute
+ * it). The decreases and increases of a kernel must sum to no more than the
+ * registers the block was launched with. */
+template <int N>
+__device__ __forceinline__ void regs_dec() { asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(N)); }
+template <int N>
+__device__ __forceinline__ void regs_inc() { asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" ::"n"(N)); }
+
 /* ---- tcgen05 ---- */
 
 __device__ __forceinline__ void tmem_alloc(uint32_t* dst_smem, uint32_t ncols)
@@ -190,6 +198,12 @@ __host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N)
                  : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),       \
                    "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]),     \
                    "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])                            \
+                 : "r"(taddr))
+
+#define SM103_TMEM_LD_X8(taddr, r)                                                               \
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"          \
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),       \
+                   "=r"(r[6]), "=r"(r[7])                                                        \
                  : "r"(taddr))
 
 #define SM103_TMEM_ST_X16(taddr, r)                                                              \

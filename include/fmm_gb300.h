@@ -178,9 +178,11 @@ int fmm_gpu_split_dgemm(const fmm_t* fmm, int levels,
 /* Per-launch timing of the split form's tensor-core GEMM kernel: while
  * enabled, a CUDA event pair is recorded on the launch stream around each
  * launch; fmm_gpu_read_kernel_timing waits for them and returns the summed
- * milliseconds and the launch count since the last read. */
+ * milliseconds, the launch count and the number of FMM products those
+ * launches computed (one launch covers a group of products) since the last
+ * read. */
 void fmm_gpu_set_kernel_timing(int enable);
-int fmm_gpu_read_kernel_timing(double* total_ms, uint64_t* launches);
+int fmm_gpu_read_kernel_timing(double* total_ms, uint64_t* launches, uint64_t* products);
 
 /* Number of kernels the library launched since load (all entry points). */
 uint64_t fmm_gpu_launch_count(void);
