@@ -27,6 +27,7 @@ _STATUS = {
     3: "coefficient file malformed", 4: "allocation failed", 5: "CUDA call failed",
     6: "unsupported size or option", 7: "coefficients violate the Brent equations",
     8: "kernel reported an error (bounded wait expired)", 9: "workspace too small",
+    10: "problem larger than the static scratch of the allocation-free entry point",
 }
 
 
@@ -101,6 +102,8 @@ def lib() -> ctypes.CDLL:
     L.fmm_gpu_split_dgemm.restype = ci
     L.fmm_gpu_split_dgemm.argtypes = [pf, ci, i64, i64, i64, dbl, vp, i64, vp, i64, dbl, vp, i64, ci, vp,
                                       ctypes.c_size_t, vp]
+    L.fmm_gpu_split_dgemm_noalloc.restype = ci
+    L.fmm_gpu_split_dgemm_noalloc.argtypes = [pf, ci, i64, i64, i64, dbl, vp, i64, vp, i64, dbl, vp, i64, ci, vp]
     L.fmm_gpu_set_kernel_timing.restype = None
     L.fmm_gpu_set_kernel_timing.argtypes = [ci]
     L.fmm_gpu_read_kernel_timing.restype = ci
@@ -244,6 +247,23 @@ def split_dgemm(A, B, C, fmm: FmmT | None = None, levels: int = 1, slices: int =
                                    B.data_ptr(), ldb, beta, C.data_ptr(), ldc, slices,
                                    workspace.data_ptr(), workspace.numel(), _stream_ptr(stream))
     _check(st, "fmm_gpu_split_dgemm")
+
+
+def split_dgemm_noalloc(A, B, C, fmm: FmmT | None = None, levels: int = 1, slices: int = 6,
+                        alpha: float = 1.0, beta: float = 1.0, stream=None) -> None:
+    """split_dgemm without any device allocation: the workspace is the
+    library's static 64 MiB device scratch (FmmError status 10 when the
+    problem does not fit). Calls that overlap on the GPU race on the scratch."""
+    m, k = A.shape
+    k2, n = B.shape
+    if k2 != k or tuple(C.shape) != (m, n):
+        raise ValueError("shape mismatch")
+    lda, ldb, ldc = _colmajor_ld(A, m, "A"), _colmajor_ld(B, k, "B"), _colmajor_ld(C, m, "C")
+    pf = ctypes.byref(fmm) if fmm is not None else None
+    st = lib().fmm_gpu_split_dgemm_noalloc(pf, levels if fmm is not None else 0, m, n, k, alpha, A.data_ptr(),
+                                           lda, B.data_ptr(), ldb, beta, C.data_ptr(), ldc, slices,
+                                           _stream_ptr(stream))
+    _check(st, "fmm_gpu_split_dgemm_noalloc")
 
 
 def bli_strassen_ab_ex(alpha: float, A, B, beta: float, C, fmm: FmmT) -> None:

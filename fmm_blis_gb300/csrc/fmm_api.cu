@@ -74,11 +74,11 @@ std::vector<int> build_table(const fmm_t* f)
     return t;
 }
 
-void fill_view(CachedAlg* c)
+AlgView view_of(const std::vector<int>& table, const int* dtab)
 {
-    const int* t = c->table.data();
+    const int* t = table.data();
     AlgView v;
-    v.tab = c->dtab;
+    v.tab = dtab;
     v.htab = t;
     v.mt = t[0]; v.kt = t[1]; v.nt = t[2]; v.R = t[3];
     const int* ou = t + FMM_ALG_HDR;
@@ -93,9 +93,11 @@ void fill_view(CachedAlg* c)
     v.avg_nnz_u = (double)ou[v.R] / v.R;
     v.avg_nnz_v = (double)ov[v.R] / v.R;
     v.avg_nnz_w = (double)ow[v.R] / v.R;
-    v.tab_len = (int)c->table.size();
-    c->view = v;
+    v.tab_len = (int)table.size();
+    return v;
 }
+
+void fill_view(CachedAlg* c) { c->view = view_of(c->table, c->dtab); }
 
 bool valid_fmm(const fmm_t* f)
 {
@@ -161,6 +163,13 @@ int fmm_flatten(const fmm_t* fmm, int levels, fmm_t* flat, int* owned)
     }
     *flat = cur;
     *owned = 1;
+    return FMM_OK;
+}
+
+int fmm_alg_describe(const fmm_t* flat, std::vector<int>* table, AlgView* out)
+{
+    *table = build_table(flat);
+    *out = view_of(*table, nullptr);
     return FMM_OK;
 }
 

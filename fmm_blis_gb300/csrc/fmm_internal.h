@@ -22,6 +22,7 @@
 
 #include <stdint.h>
 #include <cuda_runtime.h>
+#include <vector>
 #include "../../include/fmm_gb300.h"
 
 #define FMM_ALG_HDR 4
@@ -57,6 +58,8 @@ __host__ __device__ __forceinline__ void fmm_part_geom32(int d, int t, int i, in
 /* Host helpers implemented in fmm_api.cu */
 int fmm_flatten(const fmm_t* fmm, int levels, fmm_t* flat, int* owned);
 int fmm_alg_get(const fmm_t* flat, AlgView* out);  /* upload/cache */
+/* host table and view without any device allocation (view.tab left NULL) */
+int fmm_alg_describe(const fmm_t* flat, std::vector<int>* table, AlgView* out);
 void fmm_count_launch(uint64_t n);
 int* fmm_device_error_word(void);                 /* device pointer */
 

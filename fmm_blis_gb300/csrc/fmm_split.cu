@@ -756,10 +756,10 @@ size_t per_product_bytes(const Dims& d, int s)
            8 * (size_t)d.m_pad * (size_t)d.n_pad + 4 * (size_t)(d.m_pad + d.n_pad) + 1024;
 }
 
-int group_size(const AlgView& alg, const Dims& d, int s)
+int group_size(const AlgView& alg, const Dims& d, int s, size_t budget)
 {
     const size_t per = per_product_bytes(d, s);
-    size_t g = kGroupBudget / per;
+    size_t g = budget / per;
     if (g < 1) g = 1;
     if (g > (size_t)alg.R) g = (size_t)alg.R;
     /* tensor-map row coordinates are 32-bit */
@@ -772,10 +772,10 @@ struct WsLayout {
     int group;
 };
 
-WsLayout ws_layout(const AlgView& alg, int64_t m, int64_t n, int64_t k, int s)
+WsLayout ws_layout(const AlgView& alg, int64_t m, int64_t n, int64_t k, int s, size_t budget = kGroupBudget)
 {
     const Dims d = dims_of(alg, m, n, k);
-    const int G = group_size(alg, d, s);
+    const int G = group_size(alg, d, s, budget);
     WsLayout L;
     size_t off = 0;
     auto take = [&](size_t bytes) { size_t o = off; off += (bytes + 255) / 256 * 256; return o; };
@@ -851,9 +851,10 @@ size_t fmm_split_ws_bytes(const AlgView& alg, int64_t m, int64_t n, int64_t k, i
     return ws_layout(alg, m, n, k, slices).total;
 }
 
-int fmm_split_launch(const AlgView& alg, int64_t m, int64_t n, int64_t k, double alpha,
-                     const double* A, int64_t lda, const double* B, int64_t ldb, double beta,
-                     double* C, int64_t ldc, int s, void* ws, size_t ws_bytes, cudaStream_t st)
+static int split_launch_budget(const AlgView& alg, int64_t m, int64_t n, int64_t k, double alpha,
+                               const double* A, int64_t lda, const double* B, int64_t ldb, double beta,
+                               double* C, int64_t ldc, int s, void* ws, size_t ws_bytes, size_t budget,
+                               cudaStream_t st)
 {
     if (s < 2 || s > 8) return FMM_ERR_ARG;
     int rc = fmm_scale_c(m, n, beta, C, ldc, st);
@@ -863,7 +864,7 @@ int fmm_split_launch(const AlgView& alg, int64_t m, int64_t n, int64_t k, double
     if (m > 0x7fffffffLL || n > 0x7fffffffLL) return FMM_ERR_UNSUPPORTED;
     const Dims d = dims_of(alg, m, n, k);
     if (d.ke > kMaxKe) return FMM_ERR_UNSUPPORTED;
-    const WsLayout L = ws_layout(alg, m, n, k, s);
+    const WsLayout L = ws_layout(alg, m, n, k, s, budget);
     if ((int64_t)L.group * s * std::max(d.m_pad, d.n_pad) > 0x7fffffffLL) return FMM_ERR_UNSUPPORTED;
     if (ws == nullptr || ws_bytes < L.total) return FMM_ERR_WORKSPACE;
     if (((uintptr_t)ws & 255) != 0) return FMM_ERR_ARG;
@@ -939,4 +940,83 @@ int fmm_split_launch(const AlgView& alg, int64_t m, int64_t n, int64_t k, double
         fmm_count_launch(1);
     }
     return cudaGetLastError() == cudaSuccess ? FMM_OK : FMM_ERR_CUDA;
+}
+
+int fmm_split_launch(const AlgView& alg, int64_t m, int64_t n, int64_t k, double alpha,
+                     const double* A, int64_t lda, const double* B, int64_t ldb, double beta,
+                     double* C, int64_t ldc, int s, void* ws, size_t ws_bytes, cudaStream_t st)
+{
+    return split_launch_budget(alg, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, s, ws, ws_bytes,
+                               kGroupBudget, st);
+}
+
+/* ---------------------------------------------------------------------------
+ * Allocation-free entry point.
+ *
+ * For callers that must not allocate device memory while they run: code
+ * inside a CUDA graph capture or a stream callback, plug-ins that run on
+ * memory handed to them by a host application with its own allocator, or
+ * processes whose device memory is already fully reserved. Such callers
+ * cannot use fmm_gpu_split_dgemm, whose workspace they would have to obtain,
+ * nor the table cache, which allocates on first use of an algorithm. This
+ * variant keeps the algorithm table and the whole workspace in one
+ * file-scope device array of kNoAllocScratchBytes (64 MiB), which every GPU
+ * that loads the library holds until the process exits.
+ * ------------------------------------------------------------------------- */
+constexpr size_t kNoAllocScratchBytes = (size_t)64 << 20;
+static __device__ __align__(256) uint8_t g_noalloc_scratch[kNoAllocScratchBytes];
+
+namespace {
+std::mutex g_noalloc_mu;
+uint8_t* g_noalloc_ptr[64];
+}  // namespace
+
+extern "C" int fmm_gpu_split_dgemm_noalloc(const fmm_t* fmm, int levels, int64_t m, int64_t n, int64_t k,
+                                           double alpha, const double* A, int64_t lda, const double* B,
+                                           int64_t ldb, double beta, double* C, int64_t ldc, int slices,
+                                           void* stream)
+{
+    if (m < 0 || n < 0 || k < 0 || slices < 2 || slices > 8) return FMM_ERR_ARG;
+    if (lda < (m > 1 ? m : 1) || ldb < (k > 1 ? k : 1) || ldc < (m > 1 ? m : 1)) return FMM_ERR_ARG;
+    if (m > 0 && n > 0 && C == nullptr) return FMM_ERR_ARG;
+    if (m > 0 && n > 0 && k > 0 && (A == nullptr || B == nullptr)) return FMM_ERR_ARG;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return FMM_ERR_CUDA;
+    uint8_t* scratch;
+    {
+        /* once per device, with that device current: the device address of
+         * the static array (its host-side name is only a stand-in) */
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        if (g_noalloc_ptr[dev] == nullptr) {
+            void* p = nullptr;
+            if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || p == nullptr) return FMM_ERR_CUDA;
+            g_noalloc_ptr[dev] = (uint8_t*)p;
+        }
+        scratch = g_noalloc_ptr[dev];
+    }
+    fmm_t flat;
+    int owned = 0;
+    int rc = fmm_flatten(fmm, levels, &flat, &owned);
+    if (rc != FMM_OK) return rc;
+    std::vector<int> table;
+    AlgView alg;
+    rc = fmm_alg_describe(&flat, &table, &alg);
+    if (owned) free_fmm(flat);
+    if (rc != FMM_OK) return rc;
+    const size_t tab_bytes = (sizeof(int) * table.size() + 255) / 256 * 256;
+    if (tab_bytes >= kNoAllocScratchBytes) return FMM_ERR_SCRATCH;
+    const size_t ws_bytes = kNoAllocScratchBytes - tab_bytes;
+    if (m > 0 && n > 0 && k > 0 && alpha != 0.0 && ws_layout(alg, m, n, k, slices, ws_bytes).total > ws_bytes)
+        return FMM_ERR_SCRATCH;
+    if (fmm_device_error_word() == nullptr) return FMM_ERR_CUDA;
+    cudaStream_t st = (cudaStream_t)stream;
+    /* the table goes to the front of the scratch (the pageable source is
+     * consumed before cudaMemcpyAsync returns) */
+    if (cudaMemcpyAsync(scratch, table.data(), sizeof(int) * table.size(), cudaMemcpyHostToDevice, st) !=
+        cudaSuccess)
+        return FMM_ERR_CUDA;
+    alg.tab = (const int*)scratch;
+    alg.htab = table.data();
+    return split_launch_budget(alg, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, slices, scratch + tab_bytes,
+                               ws_bytes, ws_bytes, st);
 }

@@ -76,7 +76,8 @@ enum fmm_status {
     FMM_ERR_UNSUPPORTED = 6, /* size or option outside what the kernels handle */
     FMM_ERR_BRENT = 7,       /* coefficients do not satisfy the Brent equations */
     FMM_ERR_DEVICE = 8,      /* a kernel reported an error status (bounded wait expired) */
-    FMM_ERR_WORKSPACE = 9    /* caller workspace too small */
+    FMM_ERR_WORKSPACE = 9,   /* caller workspace too small */
+    FMM_ERR_SCRATCH = 10     /* problem larger than the static scratch of fmm_gpu_split_dgemm_noalloc */
 };
 
 /* ------------------------------------------------ coefficient algorithms -- */
@@ -174,6 +175,25 @@ int fmm_gpu_split_dgemm(const fmm_t* fmm, int levels,
                         double beta, double* C, int64_t ldc,
                         int slices, void* workspace, size_t workspace_bytes,
                         void* stream);
+
+/* fmm_gpu_split_dgemm for callers that must not allocate device memory
+ * while they run (code inside a CUDA graph capture or a stream callback,
+ * plug-ins working in memory a host application hands them, processes whose
+ * device memory is fully reserved): it calls no cudaMalloc, cudaFree or other
+ * device allocator. No counterpart in the reference. The algorithm table and
+ * the workspace live in one static device array of 64 MiB that every GPU
+ * loading the library keeps until exit; a problem whose workspace (slices and
+ * level accumulators for at least one product) does not fit returns
+ * FMM_ERR_SCRATCH. The first call on a device looks up the array's device
+ * address; make that first call before any stream capture. All calls share
+ * the array and each call rewrites what it uses, so calls whose GPU work
+ * overlaps (other streams, other threads) race: serialize them. */
+int fmm_gpu_split_dgemm_noalloc(const fmm_t* fmm, int levels,
+                                int64_t m, int64_t n, int64_t k,
+                                double alpha, const double* A, int64_t lda,
+                                const double* B, int64_t ldb,
+                                double beta, double* C, int64_t ldc,
+                                int slices, void* stream);
 
 /* Per-launch timing of the split form's tensor-core GEMM kernel: while
  * enabled, a CUDA event pair is recorded on the launch stream around each
