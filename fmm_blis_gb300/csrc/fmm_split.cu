@@ -61,8 +61,8 @@ constexpr int kTileN = 256;             /* N = 256: 128 clocks per MMA hide the 
 constexpr int kBK = 64;                 /* k elements per stage (128 bytes of BF16) */
 constexpr int kStages = 4;
 constexpr int kChunkKB = 4;             /* k-blocks per exact FP32 chunk: 256 terms */
-constexpr int kEpiWarps = 8;           /* two per TMEM lane quarter */
-constexpr int kEpiCols = kTileN / 2;    /* columns per epilogue thread */
+constexpr int kEpiWarps = 16;          /* four per TMEM lane quarter */
+constexpr int kEpiCols = kTileN / 4;    /* columns per epilogue thread */
 constexpr int kGemmThreads = 64 + 32 * kEpiWarps;  /* TMA warp, MMA warp, epilogue warps */
 constexpr uint32_t kATileBytes = kTileM * kBK * 2;  /* 16 KB */
 constexpr uint32_t kBTileBytes = kTileN * kBK * 2;  /* 32 KB */
@@ -592,22 +592,37 @@ split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
             if (!ok) break;
             /* fold L_g into the Z tile (units of level G): D = G - g, exact
              * left shift by 8D for D >= 0, rounded right shift by -8D (ties
-             * up) for D < 0; the first level stores instead of adding */
+             * up) for D < 0. The first level stores; later levels add with
+             * fire-and-forget 64-bit reductions (two's-complement addition
+             * is exact and order-free), so the warps go straight back to
+             * draining the accumulator. */
             {
                 const int D = a.zlevel - g;
-                const int64_t mul = D >= 0 ? ((int64_t)1 << (8 * (D >= 0 ? D : 0))) : 1;
-                const int rsh = D >= 0 ? 0 : -8 * D;
-                const int64_t rnd = D >= 0 ? 0 : ((int64_t)1 << (rsh - 1));
-                const bool first = g == 2;
+                const uint32_t lsh = D >= 0 ? 8 * D : 0;
+                const uint32_t rsh = D >= 0 ? 0 : -8 * D;
+                const uint64_t rnd = D >= 0 ? 0 : (1ull << (rsh - 1));
+                uint64_t zp = (uint64_t)zrow;
+                const uint64_t zstep = (uint64_t)a.m_pad * 8;
+                if (g == 2) {
 #pragma unroll
-                for (int h = 0; h < kEpiCols / 4; ++h) {
-                    int64_t zv[4];
+                    for (int x = 0; x < kEpiCols; ++x)
+                        asm volatile("{\n\t.reg .b64 t;\n\t"
+                                     "cvt.s64.s32 t, %1;\n\t"
+                                     "shl.b64 t, t, %2;\n\t"
+                                     "st.global.u64 [%0], t;\n\t"
+                                     "add.u64 %0, %0, %3;\n\t}"
+                                     : "+l"(zp) : "r"(L[x]), "r"(lsh), "l"(zstep) : "memory");
+                } else {
 #pragma unroll
-                    for (int x = 0; x < 4; ++x) zv[x] = first ? 0 : zrow[(int64_t)(h * 4 + x) * a.m_pad];
-#pragma unroll
-                    for (int x = 0; x < 4; ++x)
-                        zrow[(int64_t)(h * 4 + x) * a.m_pad] = zv[x] + (((int64_t)L[h * 4 + x] * mul + rnd) >> rsh);
-                    asm volatile("" ::: "memory");
+                    for (int x = 0; x < kEpiCols; ++x)
+                        asm volatile("{\n\t.reg .b64 t;\n\t"
+                                     "cvt.s64.s32 t, %1;\n\t"
+                                     "shl.b64 t, t, %2;\n\t"
+                                     "add.s64 t, t, %4;\n\t"
+                                     "shr.s64 t, t, %3;\n\t"
+                                     "red.global.add.u64 [%0], t;\n\t"
+                                     "add.u64 %0, %0, %5;\n\t}"
+                                     : "+l"(zp) : "r"(L[x]), "r"(lsh), "r"(rsh), "l"(rnd), "l"(zstep) : "memory");
                 }
             }
         }
