@@ -47,6 +47,7 @@
 #include "sm103_ptx.cuh"
 
 #include <cuda.h>
+#include <cuda_bf16.h>
 #include <cudaTypedefs.h>
 
 #include <algorithm>
@@ -87,31 +88,60 @@ __device__ __forceinline__ int exp_above(double b)
 }
 
 /* Balanced base-256 digits of x relative to 2^E (|x| < 2^E): X =
- * round(x * 2^(8s-E-1)) (ties away from zero), |X| <= 2^(8s-1), then
- * d[s-1], ..., d[1] in [-128, 127] from the bottom and d[0] in [-128, 128]. */
+ * round(x * 2^(8s-E-1)) (ties away from zero), |X| <= 2^(8s-1), split as
+ * d[s-1], ..., d[1] in [-128, 127] from the bottom and d[0] in [-128, 128];
+ * every digit has at most 8 significant bits, so it is exact in BF16. */
+/* The same digits in one step: Y = X + sum_{j < S-1} 128 * 256^j. Adding 128
+ * at every lower byte position turns the balanced digits into plain bytes, so
+ * the low S-1 bytes of Y are d[S-1] + 128, ..., d[1] + 128 and floor(Y /
+ * 256^(S-1)) is d[0]: the balanced digits above, without a digit loop. Y is
+ * kept modulo 2^64 (its low bytes are exact); d[0] is (X >> 8(S-1)) plus the
+ * carry out of the low bytes, which stays exact for the 64-bit X of S = 8. */
+struct Digits {
+    int64_t X;
+    uint64_t Y;
+};
+
 template <int S>
-__device__ __forceinline__ void split_digits(double x, int E, int* d)
+__device__ __forceinline__ Digits split_offset(double x, int E)
 {
-    constexpr int s = S;
     const uint64_t bits = (uint64_t)__double_as_longlong(x);
     const bool neg = (bits >> 63) != 0;
     const int bexp = (int)((bits >> 52) & 0x7ff);
     uint64_t mant = bits & 0x000fffffffffffffull;
     int ex;
     if (bexp == 0) ex = -1074; else { mant |= 0x0010000000000000ull; ex = bexp - 1075; }
-    const int sh = ex + 8 * s - E - 1;
+    const int sh = ex + 8 * S - E - 1;
     int64_t X;
     if (mant == 0 || sh < -62) X = 0;
     else if (sh >= 0) X = (int64_t)(mant << sh);
     else X = (int64_t)((mant + (1ull << (-sh - 1))) >> (-sh));
     if (neg) X = -X;
-#pragma unroll
-    for (int t = s - 1; t >= 1; --t) {
-        const int dd = (int)((X + 128) & 255) - 128;
-        d[t] = dd;
-        X = (X - dd) >> 8;
-    }
-    d[0] = (int)X;
+    constexpr uint64_t kOff = S > 1 ? (0x8080808080808080ull >> (8 * (9 - S))) : 0ull;
+    return Digits{X, (uint64_t)X + kOff};
+}
+
+/* digit t (0 = most significant) as an exact float */
+template <int S>
+__device__ __forceinline__ float digit_f(const Digits& g, int t)
+{
+    constexpr int sh = 8 * (S - 1);
+    constexpr uint64_t kOff = S > 1 ? (0x8080808080808080ull >> (8 * (9 - S))) : 0ull;
+    constexpr uint64_t kMask = (1ull << sh) - 1;
+    int d;
+    if (t == 0) d = (int)(g.X >> sh) + (int)((((uint64_t)g.X & kMask) + kOff) >> sh);
+    else d = (int)((g.Y >> (8 * (S - 1 - t))) & 255u) - 128;
+    /* exact int -> float for |d| < 2^22 */
+    return __int_as_float(0x4B400000 + d) - 12582912.0f;
+}
+
+/* c * v for a small integer coefficient, exact like the FP64 product: sign
+ * flips for c = +-1 (no FP64 instruction), the FP64 product otherwise. */
+__device__ __forceinline__ double coef_mul(float c, double v)
+{
+    if (c == 1.0f) return v;
+    if (c == -1.0f) return __longlong_as_double(__double_as_longlong(v) ^ (long long)0x8000000000000000ull);
+    return (double)c * v;
 }
 
 /* v * 2^e, in at most two exact power-of-two multiplications. */
@@ -125,13 +155,6 @@ __device__ __forceinline__ double scale2(double v, int e)
         e += 1000;
     }
     return v * __longlong_as_double((long long)(e + 1023) << 52);
-}
-
-__device__ __forceinline__ uint16_t bf16_of_int(int d)
-{
-    /* exact: |d| <= 128 has at most 8 significant bits */
-    const uint32_t f = __float_as_uint((float)d);
-    return (uint16_t)(f >> 16);
 }
 
 /* ------------------------------------------------- table access -------- */
@@ -304,7 +327,7 @@ pack_a_kernel(const int* __restrict__ tab, int r, const double* __restrict__ A, 
             for (int e = 0; e < ne_; ++e) {
                 const PEnt x = ent[e];
                 const double v = (gi < x.rows && gp < x.cols) ? x.base[gi + gp * lda] : 0.0;
-                sum = e == 0 ? (double)x.coef * v : fma((double)x.coef, v, sum);
+                sum = e == 0 ? coef_mul(x.coef, v) : fma((double)x.coef, v, sum);
             }
         }
         Sf[lp][li] = sum;
@@ -315,15 +338,17 @@ pack_a_kernel(const int* __restrict__ tab, int r, const double* __restrict__ A, 
     for (int rr = threadIdx.x / 8; rr < 64; rr += 32) {
         const int64_t gi = i0 + rr;
         const int E = e_row[gi];
-        int dig[8][S];
+        Digits Y[8];
 #pragma unroll
-        for (int x = 0; x < 8; ++x) split_digits<S>(Sf[kg * 8 + x][rr], E, dig[x]);
+        for (int x = 0; x < 8; ++x) Y[x] = split_offset<S>(Sf[kg * 8 + x][rr], E);
 #pragma unroll
         for (int tt = 0; tt < S; ++tt) {
             uint32_t w[4];
 #pragma unroll
-            for (int h = 0; h < 4; ++h)
-                w[h] = (uint32_t)bf16_of_int(dig[2 * h][tt]) | ((uint32_t)bf16_of_int(dig[2 * h + 1][tt]) << 16);
+            for (int h = 0; h < 4; ++h) {
+                const __nv_bfloat162 b2 = __floats2bfloat162_rn(digit_f<S>(Y[2 * h], tt), digit_f<S>(Y[2 * h + 1], tt));
+                w[h] = *reinterpret_cast<const uint32_t*>(&b2);
+            }
             uint4* dst = (uint4*)(sa + ((int64_t)tt * m_pad + gi) * k_pad + p0 + kg * 8);
             *dst = make_uint4(w[0], w[1], w[2], w[3]);
         }
@@ -369,20 +394,22 @@ pack_b_kernel(const int* __restrict__ tab, int r, const double* __restrict__ B, 
             for (int y = 0; y < 8; ++y) {
                 const int64_t gp = p0 + y;
                 const double v = (gp < ke && gp < x.rows && gj < x.cols) ? x.base[gp + gj * ldb] : 0.0;
-                v8[y] = e == 0 ? c * v : fma(c, v, v8[y]);
+                v8[y] = e == 0 ? coef_mul(x.coef, v) : fma(c, v, v8[y]);
             }
         }
     }
     const int F = f_col[gj];
-    int dig[8][S];
+    Digits Y[8];
 #pragma unroll
-    for (int x = 0; x < 8; ++x) split_digits<S>(v8[x], F, dig[x]);
+    for (int x = 0; x < 8; ++x) Y[x] = split_offset<S>(v8[x], F);
 #pragma unroll
     for (int tt = 0; tt < S; ++tt) {
         uint32_t w[4];
 #pragma unroll
-        for (int h = 0; h < 4; ++h)
-            w[h] = (uint32_t)bf16_of_int(dig[2 * h][tt]) | ((uint32_t)bf16_of_int(dig[2 * h + 1][tt]) << 16);
+        for (int h = 0; h < 4; ++h) {
+            const __nv_bfloat162 b2 = __floats2bfloat162_rn(digit_f<S>(Y[2 * h], tt), digit_f<S>(Y[2 * h + 1], tt));
+            w[h] = *reinterpret_cast<const uint32_t*>(&b2);
+        }
         uint4* dst = (uint4*)(sb + ((int64_t)tt * n_pad + gj) * k_pad + p0);
         *dst = make_uint4(w[0], w[1], w[2], w[3]);
     }
@@ -416,6 +443,33 @@ void launch_packs(int s, const int* tab, int r, const double* A, int64_t lda, co
 }
 
 /* ------------------------------------------------------ GEMM kernel ---- */
+
+/* (double)z * 2^e for |z| < 2^62 in integer arithmetic (round to nearest
+ * even, then exponent offset), identical to the FP64 conversion and
+ * power-of-two scaling whenever the result is a normal number; other cases
+ * take the FP64 route. Keeps the per-element FP64 work to the C updates. */
+__device__ __forceinline__ double i64_to_double_scaled(int64_t z, int e)
+{
+    if (z == 0) return 0.0;
+    const uint64_t sign = z < 0 ? 0x8000000000000000ull : 0ull;
+    uint64_t u = z < 0 ? (uint64_t)(-z) : (uint64_t)z;
+    int p = 63 - __clzll((long long)u);
+    uint64_t m;
+    if (p <= 52) {
+        m = u << (52 - p);
+    } else {
+        const int sh = p - 52;
+        m = u >> sh;
+        const uint64_t rem = u & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+        if (rem > half || (rem == half && (m & 1))) {
+            ++m;
+            if (m == (1ull << 53)) { m >>= 1; ++p; }
+        }
+    }
+    const int be = p + 1023 + e;
+    if (be < 1 || be > 2046) return scale2((double)z, e);
+    return __longlong_as_double((long long)(sign | ((uint64_t)be << 52) | (m & 0x000fffffffffffffull)));
+}
 
 struct GemmArgs {
     int s;                /* slices */
@@ -633,40 +687,13 @@ split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     if (warp == 1) sm103::tmem_dealloc(tmem, kTmemCols);
 }
 
-/* (double)z * 2^e for |z| < 2^62 in integer arithmetic (round to nearest
- * even, then exponent offset), identical to the FP64 conversion and
- * power-of-two scaling whenever the result is a normal number; other cases
- * take the FP64 route. Keeps the per-element FP64 work to the C updates. */
-__device__ __forceinline__ double i64_to_double_scaled(int64_t z, int e)
-{
-    if (z == 0) return 0.0;
-    const uint64_t sign = z < 0 ? 0x8000000000000000ull : 0ull;
-    uint64_t u = z < 0 ? (uint64_t)(-z) : (uint64_t)z;
-    int p = 63 - __clzll((long long)u);
-    uint64_t m;
-    if (p <= 52) {
-        m = u << (52 - p);
-    } else {
-        const int sh = p - 52;
-        m = u >> sh;
-        const uint64_t rem = u & ((1ull << sh) - 1), half = 1ull << (sh - 1);
-        if (rem > half || (rem == half && (m & 1))) {
-            ++m;
-            if (m == (1ull << 53)) { m >>= 1; ++p; }
-        }
-    }
-    const int be = p + 1023 + e;
-    if (be < 1 || be > 2046) return scale2((double)z, e);
-    return __longlong_as_double((long long)(sign | ((uint64_t)be << 52) | (m & 0x000fffffffffffffull)));
-}
-
-/* Multi-C epilogue for a group of products [r0, r0 + nprod): each thread
- * owns one element (i, j) of the sub-block grid; for every C sub-block p
- * containing it, C_p[i,j] is updated in increasing product order with
- * alpha*W[p,r] * M_r[i,j], M_r[i,j] = 2^(E_i + F_j + 2 - 8G) * Z_r[i,j]
+/* Multi-C epilogue for a group of products [r0, r0 + nprod): one thread per
+ * (C sub-block p = blockIdx.y, element (i, j) of p) adds alpha*W[p,r] *
+ * M_r[i,j] for the group's products in increasing order, with M_r[i,j] =
+ * 2^(E_i + F_j + 2 - 8G) * Z_r[i,j] converted in integer arithmetic
  * (plugin/ref_kernels/bli_gemm_fmm_ref.c:99-120, once per group instead of
  * once per product). */
-constexpr int kScatterMaxEnt = 4096;
+constexpr int kScatterMaxEnt = 1024;
 
 __global__ void __launch_bounds__(256)
 scatter_kernel(const int* __restrict__ tab, int r0, int nprod, int64_t m, int64_t n,
@@ -675,38 +702,55 @@ scatter_kernel(const int* __restrict__ tab, int r0, int nprod, int64_t m, int64_
                int64_t ldc)
 {
     __shared__ double lam[kScatterMaxEnt];
+    __shared__ int prod[kScatterMaxEnt];
+    __shared__ int nsel;
     const Tab t = tab_view(tab);
-    const int P = t.mt * t.nt;
-    const int nent = t.wp_off[P];
-    for (int e = threadIdx.x; e < nent && e < kScatterMaxEnt; e += blockDim.x)
-        lam[e] = alpha * (double)t.wp_ent[2 * e + 1];
-    __syncthreads();
-    const int me = (int)((m + t.mt - 1) / t.mt), ne = (int)((n + t.nt - 1) / t.nt);
-    const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    const int i = (int)(idx % me), j = (int)(idx / me);
-    if (j >= ne) return;
-    const int64_t zij = (int64_t)j * m_pad + i;
-    const int64_t zstride = (int64_t)n_pad * m_pad;
-    for (int p = 0; p < P; ++p) {
-        int ro, rl, co, cl;
-        fmm_part_geom32((int)m, t.mt, p / t.nt, &ro, &rl);
-        fmm_part_geom32((int)n, t.nt, p % t.nt, &co, &cl);
-        if (i >= rl || j >= cl) continue;
-        const int eb = t.wp_off[p], ee = t.wp_off[p + 1];
-        double* cp = C + ro + i + (int64_t)(co + j) * ldc;
-        double c = *cp;
-        bool touched = false;
-        for (int e = eb; e < ee; ++e) {
+    const int p = blockIdx.y;
+    int ro, rl, co, cl;
+    fmm_part_geom32((int)m, t.mt, p / t.nt, &ro, &rl);
+    fmm_part_geom32((int)n, t.nt, p % t.nt, &co, &cl);
+    if (rl <= 0 || cl <= 0) return;   /* empty sub-block (dimension smaller than its split) */
+    /* this part's entries that fall in the group, in product order */
+    if (threadIdx.x == 0) {
+        int q = 0;
+        for (int e = t.wp_off[p]; e < t.wp_off[p + 1] && q < kScatterMaxEnt; ++e) {
             const int r = t.wp_ent[2 * e] - r0;
             if (r < 0) continue;
             if (r >= nprod) break;
-            const int64_t z = Z[r * zstride + zij];
-            const double v = i64_to_double_scaled(z, e_row[r * m_pad + i] + f_col[r * n_pad + j] + 2 - 8 * zlevel);
-            c = fma(e < kScatterMaxEnt ? lam[e] : alpha * (double)t.wp_ent[2 * e + 1], v, c);
-            touched = true;
+            prod[q] = r;
+            lam[q] = alpha * (double)t.wp_ent[2 * e + 1];
+            ++q;
         }
-        if (touched) *cp = c;
+        nsel = q;
     }
+    __syncthreads();
+    const int ne = nsel;
+    const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ne == 0 || idx >= (uint32_t)rl * (uint32_t)cl) return;
+    const int i = (int)(idx % (uint32_t)rl), j = (int)(idx / (uint32_t)rl);
+    double* cp = C + ro + i + (int64_t)(co + j) * ldc;
+    double c = *cp;
+    const int64_t zij = (int64_t)j * m_pad + i;
+    const int64_t zstride = (int64_t)n_pad * m_pad;
+    const int ebase = 2 - 8 * zlevel;
+    int q = 0;
+    for (; q + 4 <= ne; q += 4) {
+        int64_t z[4];
+        int ex[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int r = prod[q + u];
+            z[u] = Z[r * zstride + zij];
+            ex[u] = e_row[r * m_pad + i] + f_col[r * n_pad + j] + ebase;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) c = fma(lam[q + u], i64_to_double_scaled(z[u], ex[u]), c);
+    }
+    for (; q < ne; ++q) {
+        const int r = prod[q];
+        c = fma(lam[q], i64_to_double_scaled(Z[r * zstride + zij], e_row[r * m_pad + i] + f_col[r * n_pad + j] + ebase), c);
+    }
+    *cp = c;
 }
 
 /* --------------------------------------------------------- host -------- */
@@ -747,7 +791,7 @@ int make_slice_map(CUtensorMap* map, const void* base, int64_t k_pad, int64_t ro
  * one GEMM launch covers every (product, tile) work item of the group, then
  * one scatter pass updates C. The group size is the largest that keeps the
  * per-group workspace (slices + Z) under kGroupBudget. */
-constexpr size_t kGroupBudget = (size_t)12 << 30;
+constexpr size_t kGroupBudget = (size_t)32 << 30;
 
 struct Dims {
     int64_t me, ne, ke, m_pad, n_pad, k_pad;
@@ -787,10 +831,8 @@ struct WsLayout {
     int group;
 };
 
-WsLayout ws_layout(const AlgView& alg, int64_t m, int64_t n, int64_t k, int s, size_t budget = kGroupBudget)
+WsLayout ws_layout_g(const AlgView& alg, const Dims& d, int64_t m, int64_t n, int s, int G)
 {
-    const Dims d = dims_of(alg, m, n, k);
-    const int G = group_size(alg, d, s, budget);
     WsLayout L;
     size_t off = 0;
     auto take = [&](size_t bytes) { size_t o = off; off += (bytes + 255) / 256 * 256; return o; };
@@ -803,6 +845,17 @@ WsLayout ws_layout(const AlgView& alg, int64_t m, int64_t n, int64_t k, int s, s
     L.sb = take(2 * (size_t)G * s * (size_t)d.n_pad * (size_t)d.k_pad);
     L.z = take(8 * (size_t)G * (size_t)d.m_pad * (size_t)d.n_pad);
     L.total = off;
+    return L;
+}
+
+/* Layout for the largest product group whose whole workspace fits in
+ * `budget` bytes (at least one product). */
+WsLayout ws_layout(const AlgView& alg, int64_t m, int64_t n, int64_t k, int s, size_t budget = kGroupBudget)
+{
+    const Dims d = dims_of(alg, m, n, k);
+    int G = group_size(alg, d, s, budget);
+    WsLayout L = ws_layout_g(alg, d, m, n, s, G);
+    while (G > 1 && L.total > budget) L = ws_layout_g(alg, d, m, n, s, --G);
     return L;
 }
 
@@ -879,6 +932,12 @@ static int split_launch_budget(const AlgView& alg, int64_t m, int64_t n, int64_t
     if (m > 0x7fffffffLL || n > 0x7fffffffLL) return FMM_ERR_UNSUPPORTED;
     const Dims d = dims_of(alg, m, n, k);
     if (d.ke > kMaxKe) return FMM_ERR_UNSUPPORTED;
+    {
+        /* the scatter keeps one C part's W entries of a group in shared memory */
+        const Tab ht = tab_view(alg.htab);
+        for (int p = 0; p < alg.mt * alg.nt; ++p)
+            if (ht.wp_off[p + 1] - ht.wp_off[p] > kScatterMaxEnt) return FMM_ERR_UNSUPPORTED;
+    }
     const WsLayout L = ws_layout(alg, m, n, k, s, budget);
     if ((int64_t)L.group * s * std::max(d.m_pad, d.n_pad) > 0x7fffffffLL) return FMM_ERR_UNSUPPORTED;
     if (ws == nullptr || ws_bytes < L.total) return FMM_ERR_WORKSPACE;
@@ -949,8 +1008,9 @@ static int split_launch_budget(const AlgView& alg, int64_t m, int64_t n, int64_t
         split_gemm_kernel<<<(unsigned)(np * tiles), kGemmThreads, kGemmSmem, st>>>(tmA, tmB, ga);
         if (timed) timing_mark(st, false);
         fmm_count_launch(1);
-        const int64_t elems = d.me * d.ne;
-        scatter_kernel<<<(unsigned)((elems + 255) / 256), 256, 0, st>>>(
+        const int64_t elems = d.me * d.ne;   /* the largest part's extent */
+        if (elems > 0xffffffffLL) return FMM_ERR_UNSUPPORTED;
+        scatter_kernel<<<dim3((unsigned)((elems + 255) / 256), (unsigned)(alg.mt * alg.nt)), 256, 0, st>>>(
             alg.tab, r0, np, m, n, (int)d.m_pad, (int)d.n_pad, ga.zlevel, alpha, Z, e_row, f_col, C, ldc);
         fmm_count_launch(1);
     }
@@ -961,8 +1021,9 @@ int fmm_split_launch(const AlgView& alg, int64_t m, int64_t n, int64_t k, double
                      const double* A, int64_t lda, const double* B, int64_t ldb, double beta,
                      double* C, int64_t ldc, int s, void* ws, size_t ws_bytes, cudaStream_t st)
 {
+    /* the group size follows the workspace the caller provides */
     return split_launch_budget(alg, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, s, ws, ws_bytes,
-                               kGroupBudget, st);
+                               ws_bytes, st);
 }
 
 /* ---------------------------------------------------------------------------

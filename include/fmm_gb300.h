@@ -156,7 +156,11 @@ int fmm_gpu_strassen_ab(double alpha, const double* A, int64_t lda,
 
 /* ------------------------------------ GPU, split-precision (Ozaki) form -- */
 
-/* Bytes of device workspace fmm_gpu_split_dgemm needs for this problem. */
+/* Bytes of device workspace recommended for fmm_gpu_split_dgemm: products
+ * are processed in groups (all products of a group are packed, multiplied in
+ * one launch and added into C in one pass), and this size holds the largest
+ * group that fits in 32 GiB. Any smaller workspace that holds one product's
+ * digit slices and level accumulators also works, with smaller groups. */
 size_t fmm_gpu_split_workspace_size(const fmm_t* fmm, int levels,
                                     int64_t m, int64_t n, int64_t k,
                                     int slices);
@@ -166,8 +170,9 @@ size_t fmm_gpu_split_workspace_size(const fmm_t* fmm, int levels,
  * into `slices` BF16 digit slices of 8 bits; all slice pairs (s,t) with
  * s + t <= slices + 1 are multiplied on the tcgen05 tensor cores with exact
  * integer-valued FP32 accumulation, and recombined in FP64. slices in 2..8.
- * `workspace` must hold fmm_gpu_split_workspace_size bytes (256-byte
- * aligned). Asynchronous on `stream`. */
+ * `workspace` (256-byte aligned) holds at least one product's slices and
+ * level accumulators; fmm_gpu_split_workspace_size gives the recommended
+ * size. Asynchronous on `stream`. */
 int fmm_gpu_split_dgemm(const fmm_t* fmm, int levels,
                         int64_t m, int64_t n, int64_t k,
                         double alpha, const double* A, int64_t lda,
