@@ -21,7 +21,7 @@
  *   3. gemm:   tcgen05.mma (kind::f16, BF16 x BF16 -> FP32 in TMEM) over the
  *              slice pairs (t,u) with t+u = g for the levels g = 2..s+1. Every
  *              product of two digits is an integer of magnitude <= 2^14, so a
- *              256-term chunk sums to an integer of magnitude <= 2^22 that
+ *              1024-term chunk sums to an integer of magnitude <= 2^24 that
  *              FP32 holds exactly; the epilogue warps drain each chunk from
  *              TMEM (double-buffered, so the tensor core keeps running),
  *              convert it exactly to int32 and add it to the level sum L_g.
@@ -61,7 +61,7 @@ constexpr int kTileM = 128;
 constexpr int kTileN = 256;             /* N = 256: 128 clocks per MMA hide the accumulator dependency */
 constexpr int kBK = 64;                 /* k elements per stage (128 bytes of BF16) */
 constexpr int kStages = 4;
-constexpr int kChunkKB = 4;             /* k-blocks per exact FP32 chunk: 256 terms */
+constexpr int kChunkKB = 16;            /* k-blocks per exact FP32 chunk: 1024 terms, |sum| <= 2^24 */
 constexpr int kEpiWarps = 16;          /* four per TMEM lane quarter */
 constexpr int kEpiCols = kTileN / 4;    /* columns per epilogue thread */
 constexpr int kGemmThreads = 64 + 32 * kEpiWarps;  /* TMA warp, MMA warp, epilogue warps */
@@ -486,7 +486,7 @@ __device__ __forceinline__ int level_pairs(int g, int s) { return min(s, g - 1) 
 /* One CTA per work item (product r of the group, 128 x 256 output tile):
  * warp 0 issues the TMA loads of the digit-slice tiles, warp 1 the
  * tcgen05.mma (M=128, N=256, K=16: long enough per instruction to hide the
- * accumulator dependency), warps 2..9 drain each exact 256-term chunk from
+ * accumulator dependency), warps 2..17 drain each exact 1024-term chunk from
  * the double-buffered TMEM accumulator into int32 level sums and fold each
  * finished level into the product's 64-bit Z tile in global memory. */
 __global__ void __launch_bounds__(kGemmThreads, 1)
@@ -635,7 +635,7 @@ split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
                     sm103::tmem_wait_ld();
 #pragma unroll
                     for (int x = 0; x < 8; ++x)
-                        L[h * 8 + x] += (int)__float_as_uint(__uint_as_float(v[x]) + 12582912.0f) - 0x4B400000;
+                        L[h * 8 + x] += __float2int_rn(__uint_as_float(v[x]));   /* exact: integer, |v| <= 2^24 */
                 }
                 sm103::tc_fence_before();
                 __syncwarp();

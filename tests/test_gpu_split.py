@@ -80,7 +80,8 @@ def test_split_long_k_chunks(fmm, orc, algs, torch_cuda):
 
 def test_split_worst_case_chunk_sums(fmm, orc, algs, torch_cuda):
     """All-equal operands: every digit product has the same sign, so each
-    256-term chunk reaches the largest magnitude the exact FP32 path allows."""
+    1024-term chunk reaches 2^24, the largest magnitude the exact FP32 path
+    allows."""
     A = np.asfortranarray(np.full((128, 2048), -0.99999999999))
     B = np.asfortranarray(np.full((2048, 128), 0.99999999999))
     C = np.zeros((128, 128), order="F")
