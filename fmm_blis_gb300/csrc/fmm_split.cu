@@ -51,6 +51,7 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <cstring>
 #include <mutex>
 #include <utility>
 #include <vector>
@@ -471,27 +472,71 @@ __device__ __forceinline__ double i64_to_double_scaled(int64_t z, int e)
     return __longlong_as_double((long long)(sign | ((uint64_t)be << 52) | (m & 0x000fffffffffffffull)));
 }
 
-struct GemmArgs {
+/* One problem of a GEMM launch: the digit slices of a product group of one
+ * FMM GEMM and where its level accumulators go. */
+struct GemmProblem {
+    CUtensorMap tmA;      /* A slices [product][s][m_pad][k_pad], box 64 x 128 */
+    CUtensorMap tmB;      /* B slices [product][s][n_pad][k_pad], box 64 x 256 */
+    int64_t* Z;           /* [product][n_pad][m_pad] int64 level accumulators */
     int s;                /* slices */
     int zlevel;           /* G: the level whose unit Z counts in */
     int nkb;              /* k_pad / 64 */
-    int tiles_m, tiles_n; /* per product */
     int m_pad, n_pad;     /* rows per slice in the A / B slice arrays */
-    int64_t* Z;           /* [product][n_pad][m_pad] int64 level accumulators */
+    int tiles_m, tiles_n; /* per product */
+    int item_begin;       /* first work item of this problem in the launch */
+};
+
+constexpr int kMaxLaunchProblems = 32;
+
+/* Everything a launch needs, passed by value (tensor maps included), so a
+ * launch copies nothing to the device and can be captured in a graph. */
+struct GemmLaunch {
+    int nprob;
+    int nitems;           /* sum over problems of products * tiles */
     int* err;
+    GemmProblem prob[kMaxLaunchProblems];
 };
 
 __device__ __forceinline__ int level_pairs(int g, int s) { return min(s, g - 1) - max(1, g - s) + 1; }
 
-/* One CTA per work item (product r of the group, 128 x 256 output tile):
- * warp 0 issues the TMA loads of the digit-slice tiles, warp 1 the
- * tcgen05.mma (M=128, N=256, K=16: long enough per instruction to hide the
- * accumulator dependency), warps 2..17 drain each exact 1024-term chunk from
- * the double-buffered TMEM accumulator into int32 level sums and fold each
- * finished level into the product's 64-bit Z tile in global memory. */
+/* Work item b -> problem, product and tile: problems in order, products in
+ * order within a problem, then a grouped raster of kRasterGroup tile rows so
+ * the CTAs resident together share slice panels in L2. */
+struct Item {
+    int p, r, tile_m, tile_n;
+};
+
+__device__ __forceinline__ Item decode_item(const GemmLaunch& L, int b)
+{
+    int p = 0;
+    while (p + 1 < L.nprob && L.prob[p + 1].item_begin <= b) ++p;
+    const GemmProblem& P = L.prob[p];
+    const int local = b - P.item_begin;
+    const int per_prod = P.tiles_m * P.tiles_n;
+    Item it;
+    it.p = p;
+    it.r = local / per_prod;
+    const int id = local % per_prod;
+    const int per_group = kRasterGroup * P.tiles_n;
+    const int grp = id / per_group, first_m = grp * kRasterGroup;
+    const int gm = min(P.tiles_m - first_m, kRasterGroup);
+    const int in_grp = id % per_group;
+    it.tile_m = first_m + in_grp % gm;
+    it.tile_n = in_grp / gm;
+    return it;
+}
+
+/* Persistent GEMM over a list of work items (problem, product of its group,
+ * 128 x 256 output tile); CTA c takes items c, c + gridDim.x, ... One CTA per
+ * SM: warp 0 issues the TMA loads of the digit-slice tiles, warp 1 the
+ * tcgen05.mma (M=128, N=256, K=16: 128 clocks per MMA hide the accumulator
+ * dependency), warps 2..17 drain each exact 1024-term chunk from the
+ * double-buffered TMEM accumulator into int32 level sums and fold finished
+ * levels into the product's 64-bit Z tile in global memory. The pipeline,
+ * TMEM allocation and barrier phases run on across items, so one item's last
+ * fold overlaps the next item's first MMAs. */
 __global__ void __launch_bounds__(kGemmThreads, 1)
-split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                  const GemmArgs a)
+split_gemm_kernel(const __grid_constant__ GemmLaunch L)
 {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -506,20 +551,6 @@ split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
 
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-    /* work item: product r (outermost, so resident CTAs share slices in L2),
-     * then a grouped raster of kRasterGroup tile rows */
-    const int per_prod = a.tiles_m * a.tiles_n;
-    const int r = blockIdx.x / per_prod;
-    int tile_m, tile_n;
-    {
-        const int id = blockIdx.x % per_prod;
-        const int per_group = kRasterGroup * a.tiles_n;
-        const int grp = id / per_group, first_m = grp * kRasterGroup;
-        const int gm = min(a.tiles_m - first_m, kRasterGroup);
-        const int in_grp = id % per_group;
-        tile_m = first_m + in_grp % gm;
-        tile_n = in_grp / gm;
-    }
 
     if (threadIdx.x == 0) {
         for (int i = 0; i < kStages; ++i) { sm103::mbar_init(&full[i], 1); sm103::mbar_init(&empty[i], 1); }
@@ -529,12 +560,10 @@ split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         sm103::fence_mbar_init();
     }
     if (warp == 1) { sm103::tmem_alloc(tmem_slot, kTmemCols); sm103::tmem_relinquish(); }
-    if (warp == 0 && lane == 0) { sm103::prefetch_tmap(&tmA); sm103::prefetch_tmap(&tmB); }
     sm103::tc_fence_before();
     __syncthreads();
     sm103::tc_fence_after();
     const uint32_t tmem = *tmem_slot;
-    const int s = a.s, nkb = a.nkb;
 
     if (warp == 0) {
         /* ---------------- TMA producer ---------------- */
@@ -543,22 +572,29 @@ split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
             uint32_t ph = 0;
             uint32_t armed = 0;  /* stages armed in the current pass (bit mask) */
             bool ok = true;
-            const int arow = r * s * a.m_pad + tile_m * kTileM;
-            const int brow = r * s * a.n_pad + tile_n * kTileN;
-            for (int g = 2; g <= s + 1 && ok; ++g)
-                for (int t = max(1, g - s); t <= min(s, g - 1) && ok; ++t) {
-                    const int u = g - t;
-                    for (int kb = 0; kb < nkb; ++kb) {
-                        if (!sm103::mbar_wait(&empty[st], ph ^ 1, abort_flag, a.err, 1)) { ok = false; break; }
-                        sm103::mbar_arrive_expect_tx(&full[st], kStageBytes);
-                        sm103::tma_load_2d(sA + st * kATileBytes, &tmA, &full[st], kb * kBK,
-                                           arow + (t - 1) * a.m_pad);
-                        sm103::tma_load_2d(sB + st * kBTileBytes, &tmB, &full[st], kb * kBK,
-                                           brow + (u - 1) * a.n_pad);
-                        armed |= 1u << st;
-                        if (++st == kStages) { st = 0; ph ^= 1; armed = 0; }
+            int last_p = -1;
+            for (int b = blockIdx.x; b < L.nitems && ok; b += gridDim.x) {
+                const Item it = decode_item(L, b);
+                const GemmProblem& P = L.prob[it.p];
+                if (it.p != last_p) { sm103::prefetch_tmap(&P.tmA); sm103::prefetch_tmap(&P.tmB); last_p = it.p; }
+                const int s = P.s, nkb = P.nkb;
+                const int arow = it.r * s * P.m_pad + it.tile_m * kTileM;
+                const int brow = it.r * s * P.n_pad + it.tile_n * kTileN;
+                for (int g = 2; g <= s + 1 && ok; ++g)
+                    for (int t = max(1, g - s); t <= min(s, g - 1) && ok; ++t) {
+                        const int u = g - t;
+                        for (int kb = 0; kb < nkb; ++kb) {
+                            if (!sm103::mbar_wait(&empty[st], ph ^ 1, abort_flag, L.err, 1)) { ok = false; break; }
+                            sm103::mbar_arrive_expect_tx(&full[st], kStageBytes);
+                            sm103::tma_load_2d(sA + st * kATileBytes, &P.tmA, &full[st], kb * kBK,
+                                               arow + (t - 1) * P.m_pad);
+                            sm103::tma_load_2d(sB + st * kBTileBytes, &P.tmB, &full[st], kb * kBK,
+                                               brow + (u - 1) * P.n_pad);
+                            armed |= 1u << st;
+                            if (++st == kStages) { st = 0; ph ^= 1; armed = 0; }
+                        }
                     }
-                }
+            }
             if (!ok) {
                 /* let every load already issued land before the CTA exits */
                 for (int i = 0; i < kStages; ++i) {
@@ -576,33 +612,37 @@ split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
             int st = 0, buf = 0;
             uint32_t ph = 0, aph = 0;
             bool ok = true;
-            for (int g = 2; g <= s + 1 && ok; ++g) {
-                const int level_kb = level_pairs(g, s) * nkb;
-                int jl = 0;
-                for (int t = max(1, g - s); t <= min(s, g - 1) && ok; ++t)
-                    for (int kb = 0; kb < nkb; ++kb) {
-                        if (jl % kChunkKB == 0) {
-                            if (!sm103::mbar_wait(&acce[buf], aph ^ 1, abort_flag, a.err, 2)) { ok = false; break; }
+            for (int b = blockIdx.x; b < L.nitems && ok; b += gridDim.x) {
+                const Item it = decode_item(L, b);
+                const int s = L.prob[it.p].s, nkb = L.prob[it.p].nkb;
+                for (int g = 2; g <= s + 1 && ok; ++g) {
+                    const int level_kb = level_pairs(g, s) * nkb;
+                    int jl = 0;
+                    for (int t = max(1, g - s); t <= min(s, g - 1) && ok; ++t)
+                        for (int kb = 0; kb < nkb; ++kb) {
+                            if (jl % kChunkKB == 0) {
+                                if (!sm103::mbar_wait(&acce[buf], aph ^ 1, abort_flag, L.err, 2)) { ok = false; break; }
+                                sm103::tc_fence_after();
+                            }
+                            if (!sm103::mbar_wait(&full[st], ph, abort_flag, L.err, 3)) { ok = false; break; }
                             sm103::tc_fence_after();
-                        }
-                        if (!sm103::mbar_wait(&full[st], ph, abort_flag, a.err, 3)) { ok = false; break; }
-                        sm103::tc_fence_after();
-                        const uint32_t a0 = sm103::smem_u32(sA + st * kATileBytes);
-                        const uint32_t b0 = sm103::smem_u32(sB + st * kBTileBytes);
+                            const uint32_t a0 = sm103::smem_u32(sA + st * kATileBytes);
+                            const uint32_t b0 = sm103::smem_u32(sB + st * kBTileBytes);
 #pragma unroll
-                        for (int kk = 0; kk < kBK / 16; ++kk)
-                            sm103::mma_bf16(tmem + buf * kTileN, sm103::smem_desc_sw128(a0 + kk * 32),
-                                            sm103::smem_desc_sw128(b0 + kk * 32), idesc,
-                                            (jl % kChunkKB != 0 || kk != 0) ? 1u : 0u);
-                        sm103::mma_commit(&empty[st]);
-                        if (++st == kStages) { st = 0; ph ^= 1; }
-                        ++jl;
-                        if (jl % kChunkKB == 0 || jl == level_kb) {
-                            sm103::mma_commit(&accf[buf]);
-                            buf ^= 1;
-                            if (buf == 0) aph ^= 1;
+                            for (int kk = 0; kk < kBK / 16; ++kk)
+                                sm103::mma_bf16(tmem + buf * kTileN, sm103::smem_desc_sw128(a0 + kk * 32),
+                                                sm103::smem_desc_sw128(b0 + kk * 32), idesc,
+                                                (jl % kChunkKB != 0 || kk != 0) ? 1u : 0u);
+                            sm103::mma_commit(&empty[st]);
+                            if (++st == kStages) { st = 0; ph ^= 1; }
+                            ++jl;
+                            if (jl % kChunkKB == 0 || jl == level_kb) {
+                                sm103::mma_commit(&accf[buf]);
+                                buf ^= 1;
+                                if (buf == 0) aph ^= 1;
+                            }
                         }
-                    }
+                }
             }
             /* all issued MMAs complete before TMEM is released */
             sm103::mma_commit(drain);
@@ -615,68 +655,74 @@ split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         const int colbase = ((warp - 2) / 4) * kEpiCols;
         const int row = quarter * 32 + lane;
         const uint32_t tl = tmem + ((uint32_t)(quarter * 32) << 16);
-        int64_t* zrow = a.Z + (int64_t)r * a.n_pad * a.m_pad + (int64_t)(tile_n * kTileN + colbase) * a.m_pad +
-                        tile_m * kTileM + row;
         int buf = 0;
         uint32_t aph = 0;
         bool ok = true;
-        for (int g = 2; g <= s + 1 && ok; ++g) {
-            int L[kEpiCols];
+        for (int b = blockIdx.x; b < L.nitems && ok; b += gridDim.x) {
+            const Item it = decode_item(L, b);
+            const GemmProblem& P = L.prob[it.p];
+            const int s = P.s, nkb = P.nkb;
+            int64_t* zrow = P.Z + (int64_t)it.r * P.n_pad * P.m_pad +
+                            (int64_t)(it.tile_n * kTileN + colbase) * P.m_pad + it.tile_m * kTileM + row;
+            const struct { int zlevel, m_pad; } a = {P.zlevel, P.m_pad};
+            for (int g = 2; g <= s + 1 && ok; ++g) {
+                int lsum[kEpiCols];
 #pragma unroll
-            for (int x = 0; x < kEpiCols; ++x) L[x] = 0;
-            const int nchunks = (level_pairs(g, s) * nkb + kChunkKB - 1) / kChunkKB;
-            for (int c = 0; c < nchunks; ++c) {
-                if (!sm103::mbar_wait(&accf[buf], aph, abort_flag, a.err, 4)) { ok = false; break; }
-                sm103::tc_fence_after();
+                for (int x = 0; x < kEpiCols; ++x) lsum[x] = 0;
+                const int nchunks = (level_pairs(g, s) * nkb + kChunkKB - 1) / kChunkKB;
+                for (int c = 0; c < nchunks; ++c) {
+                    if (!sm103::mbar_wait(&accf[buf], aph, abort_flag, L.err, 4)) { ok = false; break; }
+                    sm103::tc_fence_after();
 #pragma unroll
-                for (int h = 0; h < kEpiCols / 8; ++h) {
-                    uint32_t v[8];
-                    SM103_TMEM_LD_X8(tl + buf * kTileN + colbase + h * 8, v);
-                    sm103::tmem_wait_ld();
+                    for (int h = 0; h < kEpiCols / 8; ++h) {
+                        uint32_t v[8];
+                        SM103_TMEM_LD_X8(tl + buf * kTileN + colbase + h * 8, v);
+                        sm103::tmem_wait_ld();
 #pragma unroll
-                    for (int x = 0; x < 8; ++x)
-                        L[h * 8 + x] += __float2int_rn(__uint_as_float(v[x]));   /* exact: integer, |v| <= 2^24 */
+                        for (int x = 0; x < 8; ++x)
+                            lsum[h * 8 + x] += __float2int_rn(__uint_as_float(v[x]));   /* exact: integer, |v| <= 2^24 */
+                    }
+                    sm103::tc_fence_before();
+                    __syncwarp();
+                    if (lane == 0) sm103::mbar_arrive(&acce[buf]);
+                    buf ^= 1;
+                    if (buf == 0) aph ^= 1;
                 }
-                sm103::tc_fence_before();
-                __syncwarp();
-                if (lane == 0) sm103::mbar_arrive(&acce[buf]);
-                buf ^= 1;
-                if (buf == 0) aph ^= 1;
-            }
-            if (!ok) break;
-            /* fold L_g into the Z tile (units of level G): D = G - g, exact
-             * left shift by 8D for D >= 0, rounded right shift by -8D (ties
-             * up) for D < 0. The first level stores; later levels add with
-             * fire-and-forget 64-bit reductions (two's-complement addition
-             * is exact and order-free), so the warps go straight back to
-             * draining the accumulator. */
-            {
-                const int D = a.zlevel - g;
-                const uint32_t lsh = D >= 0 ? 8 * D : 0;
-                const uint32_t rsh = D >= 0 ? 0 : -8 * D;
-                const uint64_t rnd = D >= 0 ? 0 : (1ull << (rsh - 1));
-                uint64_t zp = (uint64_t)zrow;
-                const uint64_t zstep = (uint64_t)a.m_pad * 8;
-                if (g == 2) {
+                if (!ok) break;
+                /* fold L_g into the Z tile (units of level G): D = G - g, exact
+                 * left shift by 8D for D >= 0, rounded right shift by -8D (ties
+                 * up) for D < 0. The first level stores; later levels add with
+                 * fire-and-forget 64-bit reductions (two's-complement addition
+                 * is exact and order-free), so the warps go straight back to
+                 * draining the accumulator. */
+                {
+                    const int D = a.zlevel - g;
+                    const uint32_t lsh = D >= 0 ? 8 * D : 0;
+                    const uint32_t rsh = D >= 0 ? 0 : -8 * D;
+                    const uint64_t rnd = D >= 0 ? 0 : (1ull << (rsh - 1));
+                    uint64_t zp = (uint64_t)zrow;
+                    const uint64_t zstep = (uint64_t)a.m_pad * 8;
+                    if (g == 2) {
 #pragma unroll
-                    for (int x = 0; x < kEpiCols; ++x)
-                        asm volatile("{\n\t.reg .b64 t;\n\t"
-                                     "cvt.s64.s32 t, %1;\n\t"
-                                     "shl.b64 t, t, %2;\n\t"
-                                     "st.global.u64 [%0], t;\n\t"
-                                     "add.u64 %0, %0, %3;\n\t}"
-                                     : "+l"(zp) : "r"(L[x]), "r"(lsh), "l"(zstep) : "memory");
-                } else {
+                        for (int x = 0; x < kEpiCols; ++x)
+                            asm volatile("{\n\t.reg .b64 t;\n\t"
+                                         "cvt.s64.s32 t, %1;\n\t"
+                                         "shl.b64 t, t, %2;\n\t"
+                                         "st.global.u64 [%0], t;\n\t"
+                                         "add.u64 %0, %0, %3;\n\t}"
+                                         : "+l"(zp) : "r"(lsum[x]), "r"(lsh), "l"(zstep) : "memory");
+                    } else {
 #pragma unroll
-                    for (int x = 0; x < kEpiCols; ++x)
-                        asm volatile("{\n\t.reg .b64 t;\n\t"
-                                     "cvt.s64.s32 t, %1;\n\t"
-                                     "shl.b64 t, t, %2;\n\t"
-                                     "add.s64 t, t, %4;\n\t"
-                                     "shr.s64 t, t, %3;\n\t"
-                                     "red.global.add.u64 [%0], t;\n\t"
-                                     "add.u64 %0, %0, %5;\n\t}"
-                                     : "+l"(zp) : "r"(L[x]), "r"(lsh), "r"(rsh), "l"(rnd), "l"(zstep) : "memory");
+                        for (int x = 0; x < kEpiCols; ++x)
+                            asm volatile("{\n\t.reg .b64 t;\n\t"
+                                         "cvt.s64.s32 t, %1;\n\t"
+                                         "shl.b64 t, t, %2;\n\t"
+                                         "add.s64 t, t, %4;\n\t"
+                                         "shr.s64 t, t, %3;\n\t"
+                                         "red.global.add.u64 [%0], t;\n\t"
+                                         "add.u64 %0, %0, %5;\n\t}"
+                                         : "+l"(zp) : "r"(lsum[x]), "r"(lsh), "r"(rsh), "l"(rnd), "l"(zstep) : "memory");
+                    }
                 }
             }
         }
@@ -960,9 +1006,13 @@ static int split_launch_budget(const AlgView& alg, int64_t m, int64_t n, int64_t
             return FMM_ERR_CUDA;
         attr_set = true;
     }
-    CUtensorMap tmA, tmB;
-    if (make_slice_map(&tmA, sa, d.k_pad, (int64_t)G * s * d.m_pad, kTileM) != FMM_OK) return FMM_ERR_CUDA;
-    if (make_slice_map(&tmB, sb, d.k_pad, (int64_t)G * s * d.n_pad, kTileN) != FMM_OK) return FMM_ERR_CUDA;
+    GemmLaunch gl;
+    memset(&gl, 0, sizeof(gl));
+    gl.nprob = 1;
+    gl.err = fmm_device_error_word();
+    GemmProblem& gp = gl.prob[0];
+    if (make_slice_map(&gp.tmA, sa, d.k_pad, (int64_t)G * s * d.m_pad, kTileM) != FMM_OK) return FMM_ERR_CUDA;
+    if (make_slice_map(&gp.tmB, sb, d.k_pad, (int64_t)G * s * d.n_pad, kTileN) != FMM_OK) return FMM_ERR_CUDA;
 
     /* per-sub-block row/column maxima, once per call */
     if (cudaMemsetAsync(amax, 0, sizeof(unsigned long long) * (size_t)alg.kt * (size_t)m, st) != cudaSuccess)
@@ -975,17 +1025,19 @@ static int split_launch_budget(const AlgView& alg, int64_t m, int64_t n, int64_t
         bmax_kernel<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, st>>>(B, ldb, k, n, alg.kt, bmax);
         fmm_count_launch(2);
     }
-    GemmArgs ga;
-    ga.s = s;
-    ga.zlevel = d.k_pad <= 128 ? 7 : 6;
-    ga.nkb = (int)(d.k_pad / kBK);
-    ga.tiles_m = (int)(d.m_pad / kTileM);
-    ga.tiles_n = (int)(d.n_pad / kTileN);
-    ga.m_pad = (int)d.m_pad;
-    ga.n_pad = (int)d.n_pad;
-    ga.Z = Z;
-    ga.err = fmm_device_error_word();
-    const int64_t tiles = (int64_t)ga.tiles_m * ga.tiles_n;
+    gp.s = s;
+    gp.zlevel = d.k_pad <= 128 ? 7 : 6;
+    gp.nkb = (int)(d.k_pad / kBK);
+    gp.tiles_m = (int)(d.m_pad / kTileM);
+    gp.tiles_n = (int)(d.n_pad / kTileN);
+    gp.m_pad = (int)d.m_pad;
+    gp.n_pad = (int)d.n_pad;
+    gp.Z = Z;
+    gp.item_begin = 0;
+    const int64_t tiles = (int64_t)gp.tiles_m * gp.tiles_n;
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     for (int r0 = 0; r0 < alg.R; r0 += G) {
         const int np = std::min(G, alg.R - r0);
         for (int q = 0; q < np; ++q) {
@@ -999,19 +1051,20 @@ static int split_launch_budget(const AlgView& alg, int64_t m, int64_t n, int64_t
             fmm_count_launch(3);
         }
         if (np * tiles > 0x7fffffffLL) return FMM_ERR_UNSUPPORTED;
+        gl.nitems = (int)(np * tiles);
         const bool timed = g_timing;
         if (timed) {
             timing_mark(st, true);
             std::lock_guard<std::mutex> lk(g_timing_mu);
             g_timed_products += (uint64_t)np;
         }
-        split_gemm_kernel<<<(unsigned)(np * tiles), kGemmThreads, kGemmSmem, st>>>(tmA, tmB, ga);
+        split_gemm_kernel<<<(unsigned)std::min<int64_t>(gl.nitems, sms), kGemmThreads, kGemmSmem, st>>>(gl);
         if (timed) timing_mark(st, false);
         fmm_count_launch(1);
         const int64_t elems = d.me * d.ne;   /* the largest part's extent */
         if (elems > 0xffffffffLL) return FMM_ERR_UNSUPPORTED;
         scatter_kernel<<<dim3((unsigned)((elems + 255) / 256), (unsigned)(alg.mt * alg.nt)), 256, 0, st>>>(
-            alg.tab, r0, np, m, n, (int)d.m_pad, (int)d.n_pad, ga.zlevel, alpha, Z, e_row, f_col, C, ldc);
+            alg.tab, r0, np, m, n, (int)d.m_pad, (int)d.n_pad, gp.zlevel, alpha, Z, e_row, f_col, C, ldc);
         fmm_count_launch(1);
     }
     return cudaGetLastError() == cudaSuccess ? FMM_OK : FMM_ERR_CUDA;
