@@ -37,6 +37,18 @@ class FmmError(RuntimeError):
         super().__init__(f"{what}: {_STATUS.get(status, 'unknown status')} (status {status})")
 
 
+class BatchProblem(ctypes.Structure):
+    """fmm_batch_problem (include/fmm_gb300.h)."""
+
+    _fields_ = [
+        ("fmm", ctypes.c_void_p), ("levels", ctypes.c_int), ("slices", ctypes.c_int),
+        ("m", ctypes.c_int64), ("n", ctypes.c_int64), ("k", ctypes.c_int64),
+        ("alpha", ctypes.c_double), ("A", ctypes.c_void_p), ("lda", ctypes.c_int64),
+        ("B", ctypes.c_void_p), ("ldb", ctypes.c_int64),
+        ("beta", ctypes.c_double), ("C", ctypes.c_void_p), ("ldc", ctypes.c_int64),
+    ]
+
+
 class FmmT(ctypes.Structure):
     """Same layout as the reference's fmm_t (plugin/bli_plugin_fmm_blis.h:58-68)."""
 
@@ -102,6 +114,10 @@ def lib() -> ctypes.CDLL:
     L.fmm_gpu_split_dgemm.restype = ci
     L.fmm_gpu_split_dgemm.argtypes = [pf, ci, i64, i64, i64, dbl, vp, i64, vp, i64, dbl, vp, i64, ci, vp,
                                       ctypes.c_size_t, vp]
+    L.fmm_gpu_batch_workspace_size.restype = ctypes.c_size_t
+    L.fmm_gpu_batch_workspace_size.argtypes = [ci, ctypes.POINTER(BatchProblem)]
+    L.fmm_gpu_batch_dgemm.restype = ci
+    L.fmm_gpu_batch_dgemm.argtypes = [ci, ctypes.POINTER(BatchProblem), vp, ctypes.c_size_t, vp]
     L.fmm_gpu_split_dgemm_noalloc.restype = ci
     L.fmm_gpu_split_dgemm_noalloc.argtypes = [pf, ci, i64, i64, i64, dbl, vp, i64, vp, i64, dbl, vp, i64, ci, vp]
     L.fmm_gpu_set_kernel_timing.restype = None
@@ -191,7 +207,11 @@ def _colmajor_ld(t, rows: int, name: str) -> int:
         raise TypeError(f"{name} must be float64")
     if not t.is_cuda:
         raise TypeError(f"{name} must be a CUDA tensor")
-    if t.dim() != 2 or (t.shape[0] > 1 and t.stride(0) != 1):
+    if t.dim() != 2:
+        raise ValueError(f"{name} must be a 2-D tensor")
+    if t.numel() == 0:
+        return max(rows, 1)
+    if t.shape[0] > 1 and t.stride(0) != 1:
         raise ValueError(f"{name} must be a column-major 2-D tensor (stride(0) == 1)")
     return max(int(t.stride(1)), max(rows, 1))
 
@@ -264,6 +284,46 @@ def split_dgemm_noalloc(A, B, C, fmm: FmmT | None = None, levels: int = 1, slice
                                            lda, B.data_ptr(), ldb, beta, C.data_ptr(), ldc, slices,
                                            _stream_ptr(stream))
     _check(st, "fmm_gpu_split_dgemm_noalloc")
+
+
+def make_batch(problems):
+    """problems: iterable of dicts with keys A, B, C (column-major CUDA
+    tensors), and optional fmm (FmmT or None), levels, slices (0: plain FP64
+    form), alpha, beta. Returns a ctypes array of fmm_batch_problem."""
+    probs = list(problems)
+    arr = (BatchProblem * max(len(probs), 1))()
+    for i, p in enumerate(probs):
+        A, B, C = p["A"], p["B"], p["C"]
+        m, k = A.shape
+        n = B.shape[1]
+        f = p.get("fmm")
+        arr[i].fmm = ctypes.cast(ctypes.pointer(f), ctypes.c_void_p) if f is not None else None
+        arr[i].levels = p.get("levels", 1) if f is not None else 0
+        arr[i].slices = p.get("slices", 6)
+        arr[i].m, arr[i].n, arr[i].k = m, n, k
+        arr[i].alpha, arr[i].beta = p.get("alpha", 1.0), p.get("beta", 1.0)
+        arr[i].A, arr[i].lda = A.data_ptr(), _colmajor_ld(A, m, "A")
+        arr[i].B, arr[i].ldb = B.data_ptr(), _colmajor_ld(B, k, "B")
+        arr[i].C, arr[i].ldc = C.data_ptr(), _colmajor_ld(C, m, "C")
+    return arr, len(probs)
+
+
+def batch_workspace_size(batch) -> int:
+    arr, count = batch
+    return int(lib().fmm_gpu_batch_workspace_size(count, arr))
+
+
+def batch_dgemm(problems, workspace=None, stream=None) -> None:
+    """Runs independent GEMMs as one batch (see fmm_gpu_batch_dgemm)."""
+    import torch
+    arr, count = make_batch(problems) if not isinstance(problems, tuple) else problems
+    if count == 0:
+        return
+    if workspace is None:
+        need = int(lib().fmm_gpu_batch_workspace_size(count, arr))
+        workspace = torch.empty(max(need, 256), dtype=torch.uint8, device="cuda")
+    _check(lib().fmm_gpu_batch_dgemm(count, arr, workspace.data_ptr(), workspace.numel(), _stream_ptr(stream)),
+           "fmm_gpu_batch_dgemm")
 
 
 def bli_strassen_ab_ex(alpha: float, A, B, beta: float, C, fmm: FmmT) -> None:

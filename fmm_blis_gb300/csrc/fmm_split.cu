@@ -965,40 +965,157 @@ size_t fmm_split_ws_bytes(const AlgView& alg, int64_t m, int64_t n, int64_t k, i
     return ws_layout(alg, m, n, k, slices).total;
 }
 
-static int split_launch_budget(const AlgView& alg, int64_t m, int64_t n, int64_t k, double alpha,
-                               const double* A, int64_t lda, const double* B, int64_t ldb, double beta,
-                               double* C, int64_t ldc, int s, void* ws, size_t ws_bytes, size_t budget,
-                               cudaStream_t st)
+/* One split-form GEMM problem being executed: its algorithm, geometry,
+ * operands and the part of the workspace it uses. */
+struct SplitJob {
+    AlgView alg;
+    Dims d;
+    int64_t m, n, k;
+    double alpha, beta;
+    const double* A;
+    int64_t lda;
+    const double* B;
+    int64_t ldb;
+    double* C;
+    int64_t ldc;
+    int s;
+    bool trivial;  /* nothing beyond C := beta*C */
+    WsLayout L;
+    uint8_t* w;
+};
+
+static int job_init(SplitJob& j, const AlgView& alg, int64_t m, int64_t n, int64_t k, double alpha,
+                    const double* A, int64_t lda, const double* B, int64_t ldb, double beta, double* C,
+                    int64_t ldc, int s)
 {
     if (s < 2 || s > 8) return FMM_ERR_ARG;
-    int rc = fmm_scale_c(m, n, beta, C, ldc, st);
-    if (rc != FMM_OK) return rc;
-    if (m == 0 || n == 0 || k == 0 || alpha == 0.0) return FMM_OK;
+    j.alg = alg;
+    j.m = m; j.n = n; j.k = k;
+    j.alpha = alpha; j.beta = beta;
+    j.A = A; j.lda = lda; j.B = B; j.ldb = ldb; j.C = C; j.ldc = ldc;
+    j.s = s;
+    j.w = nullptr;
+    j.trivial = m == 0 || n == 0 || k == 0 || alpha == 0.0;
+    if (j.trivial) return FMM_OK;
     if (alg.max_nnz_u > kPackMaxEnt || alg.max_nnz_v > kPackMaxEnt) return FMM_ERR_UNSUPPORTED;
     if (m > 0x7fffffffLL || n > 0x7fffffffLL) return FMM_ERR_UNSUPPORTED;
-    const Dims d = dims_of(alg, m, n, k);
-    if (d.ke > kMaxKe) return FMM_ERR_UNSUPPORTED;
-    {
-        /* the scatter keeps one C part's W entries of a group in shared memory */
-        const Tab ht = tab_view(alg.htab);
-        for (int p = 0; p < alg.mt * alg.nt; ++p)
-            if (ht.wp_off[p + 1] - ht.wp_off[p] > kScatterMaxEnt) return FMM_ERR_UNSUPPORTED;
-    }
-    const WsLayout L = ws_layout(alg, m, n, k, s, budget);
-    if ((int64_t)L.group * s * std::max(d.m_pad, d.n_pad) > 0x7fffffffLL) return FMM_ERR_UNSUPPORTED;
-    if (ws == nullptr || ws_bytes < L.total) return FMM_ERR_WORKSPACE;
+    j.d = dims_of(alg, m, n, k);
+    if (j.d.ke > kMaxKe) return FMM_ERR_UNSUPPORTED;
+    if (j.d.me * j.d.ne > 0xffffffffLL) return FMM_ERR_UNSUPPORTED;
+    /* the scatter keeps one C part's W entries of a group in shared memory */
+    const Tab ht = tab_view(alg.htab);
+    for (int p = 0; p < alg.mt * alg.nt; ++p)
+        if (ht.wp_off[p + 1] - ht.wp_off[p] > kScatterMaxEnt) return FMM_ERR_UNSUPPORTED;
+    return FMM_OK;
+}
+
+/* workspace of the job for a product group within `budget` bytes */
+static int job_bind(SplitJob& j, void* ws, size_t ws_bytes, size_t budget)
+{
+    if (j.trivial) return FMM_OK;
+    j.L = ws_layout(j.alg, j.m, j.n, j.k, j.s, budget);
+    if ((int64_t)j.L.group * j.s * std::max(j.d.m_pad, j.d.n_pad) > 0x7fffffffLL) return FMM_ERR_UNSUPPORTED;
+    if (ws == nullptr || ws_bytes < j.L.total) return FMM_ERR_WORKSPACE;
     if (((uintptr_t)ws & 255) != 0) return FMM_ERR_ARG;
+    j.w = (uint8_t*)ws;
+    return FMM_OK;
+}
 
-    uint8_t* w = (uint8_t*)ws;
-    unsigned long long* amax = (unsigned long long*)(w + L.amax);
-    unsigned long long* bmax = (unsigned long long*)(w + L.bmax);
-    int* e_row = (int*)(w + L.erow);
-    int* f_col = (int*)(w + L.fcol);
-    uint16_t* sa = (uint16_t*)(w + L.sa);
-    uint16_t* sb = (uint16_t*)(w + L.sb);
-    int64_t* Z = (int64_t*)(w + L.z);
-    const int G = L.group;
+/* workspace of the job for a group of exactly G products */
+static int job_bind_group(SplitJob& j, void* ws, size_t ws_bytes, int G)
+{
+    if (j.trivial) return FMM_OK;
+    j.L = ws_layout_g(j.alg, j.d, j.m, j.n, j.s, G);
+    if ((int64_t)j.L.group * j.s * std::max(j.d.m_pad, j.d.n_pad) > 0x7fffffffLL) return FMM_ERR_UNSUPPORTED;
+    if (ws == nullptr || ws_bytes < j.L.total) return FMM_ERR_WORKSPACE;
+    if (((uintptr_t)ws & 255) != 0) return FMM_ERR_ARG;
+    j.w = (uint8_t*)ws;
+    return FMM_OK;
+}
 
+/* C := beta*C and the per-sub-block row/column maxima of A and B */
+static int job_prologue(SplitJob& j, cudaStream_t st)
+{
+    int rc = fmm_scale_c(j.m, j.n, j.beta, j.C, j.ldc, st);
+    if (rc != FMM_OK || j.trivial) return rc;
+    unsigned long long* amax = (unsigned long long*)(j.w + j.L.amax);
+    unsigned long long* bmax = (unsigned long long*)(j.w + j.L.bmax);
+    if (cudaMemsetAsync(amax, 0, sizeof(unsigned long long) * (size_t)j.alg.kt * (size_t)j.m, st) != cudaSuccess)
+        return FMM_ERR_CUDA;
+    const int cpb = 256;
+    dim3 grid((unsigned)((j.m + 255) / 256), (unsigned)j.alg.kt, (unsigned)((j.d.ke + cpb - 1) / cpb));
+    amax_kernel<<<grid, 256, 0, st>>>(j.A, j.lda, j.m, j.k, j.alg.kt, amax, cpb);
+    const int64_t warps = j.n * j.alg.kt;
+    bmax_kernel<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, st>>>(j.B, j.ldb, j.k, j.n, j.alg.kt, bmax);
+    fmm_count_launch(2);
+    return FMM_OK;
+}
+
+/* exponents and digit slices of products [r0, r0 + np); np never exceeds
+ * the group the job's workspace was laid out for */
+static int job_pack(SplitJob& j, int r0, int np, cudaStream_t st)
+{
+    if (np > j.L.group) return FMM_ERR_WORKSPACE;
+    const Dims& d = j.d;
+    unsigned long long* amax = (unsigned long long*)(j.w + j.L.amax);
+    unsigned long long* bmax = (unsigned long long*)(j.w + j.L.bmax);
+    int* e_row = (int*)(j.w + j.L.erow);
+    int* f_col = (int*)(j.w + j.L.fcol);
+    uint16_t* sa = (uint16_t*)(j.w + j.L.sa);
+    uint16_t* sb = (uint16_t*)(j.w + j.L.sb);
+    for (int q = 0; q < np; ++q) {
+        const int r = r0 + q;
+        int* er = e_row + (int64_t)q * d.m_pad;
+        int* fc = f_col + (int64_t)q * d.n_pad;
+        exps_kernel<<<(unsigned)((d.m_pad + d.n_pad + 255) / 256), 256, 0, st>>>(
+            j.alg.tab, r, j.m, j.n, j.k, d.m_pad, d.n_pad, amax, bmax, er, fc);
+        launch_packs(j.s, j.alg.tab, r, j.A, j.lda, j.B, j.ldb, j.m, j.n, j.k, d.m_pad, d.n_pad, d.k_pad, er, fc,
+                     sa + (int64_t)q * j.s * d.m_pad * d.k_pad, sb + (int64_t)q * j.s * d.n_pad * d.k_pad, st);
+        fmm_count_launch(3);
+    }
+    return FMM_OK;
+}
+
+static int job_zlevel(const SplitJob& j) { return j.d.k_pad <= 128 ? 7 : 6; }
+
+/* the job's product group as one problem of a GEMM launch */
+static int job_fill(const SplitJob& j, GemmProblem& gp, int np, int item_begin)
+{
+    const Dims& d = j.d;
+    const int G = j.L.group;
+    if (make_slice_map(&gp.tmA, j.w + j.L.sa, d.k_pad, (int64_t)G * j.s * d.m_pad, kTileM) != FMM_OK)
+        return FMM_ERR_CUDA;
+    if (make_slice_map(&gp.tmB, j.w + j.L.sb, d.k_pad, (int64_t)G * j.s * d.n_pad, kTileN) != FMM_OK)
+        return FMM_ERR_CUDA;
+    gp.Z = (int64_t*)(j.w + j.L.z);
+    gp.s = j.s;
+    gp.zlevel = job_zlevel(j);
+    gp.nkb = (int)(d.k_pad / kBK);
+    gp.m_pad = (int)d.m_pad;
+    gp.n_pad = (int)d.n_pad;
+    gp.tiles_m = (int)(d.m_pad / kTileM);
+    gp.tiles_n = (int)(d.n_pad / kTileN);
+    gp.item_begin = item_begin;
+    (void)np;
+    return FMM_OK;
+}
+
+static int64_t job_items(const SplitJob& j, int np)
+{
+    return (int64_t)np * (j.d.m_pad / kTileM) * (j.d.n_pad / kTileN);
+}
+
+static void job_scatter(const SplitJob& j, int r0, int np, cudaStream_t st)
+{
+    const int64_t elems = j.d.me * j.d.ne;   /* the largest part's extent */
+    scatter_kernel<<<dim3((unsigned)((elems + 255) / 256), (unsigned)(j.alg.mt * j.alg.nt)), 256, 0, st>>>(
+        j.alg.tab, r0, np, j.m, j.n, (int)j.d.m_pad, (int)j.d.n_pad, job_zlevel(j), j.alpha,
+        (const int64_t*)(j.w + j.L.z), (const int*)(j.w + j.L.erow), (const int*)(j.w + j.L.fcol), j.C, j.ldc);
+    fmm_count_launch(1);
+}
+
+static int launch_gemm(GemmLaunch& gl, int64_t nitems, int nprod_timed, cudaStream_t st)
+{
     static bool attr_set = false;
     if (!attr_set) {
         if (cudaFuncSetAttribute(split_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1006,69 +1123,140 @@ static int split_launch_budget(const AlgView& alg, int64_t m, int64_t n, int64_t
             return FMM_ERR_CUDA;
         attr_set = true;
     }
-    GemmLaunch gl;
-    memset(&gl, 0, sizeof(gl));
-    gl.nprob = 1;
+    if (nitems > 0x7fffffffLL) return FMM_ERR_UNSUPPORTED;
+    if (nitems == 0) return FMM_OK;
+    gl.nitems = (int)nitems;
     gl.err = fmm_device_error_word();
-    GemmProblem& gp = gl.prob[0];
-    if (make_slice_map(&gp.tmA, sa, d.k_pad, (int64_t)G * s * d.m_pad, kTileM) != FMM_OK) return FMM_ERR_CUDA;
-    if (make_slice_map(&gp.tmB, sb, d.k_pad, (int64_t)G * s * d.n_pad, kTileN) != FMM_OK) return FMM_ERR_CUDA;
-
-    /* per-sub-block row/column maxima, once per call */
-    if (cudaMemsetAsync(amax, 0, sizeof(unsigned long long) * (size_t)alg.kt * (size_t)m, st) != cudaSuccess)
-        return FMM_ERR_CUDA;
-    {
-        const int cpb = 256;
-        dim3 grid((unsigned)((m + 255) / 256), (unsigned)alg.kt, (unsigned)((d.ke + cpb - 1) / cpb));
-        amax_kernel<<<grid, 256, 0, st>>>(A, lda, m, k, alg.kt, amax, cpb);
-        const int64_t warps = n * alg.kt;
-        bmax_kernel<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, st>>>(B, ldb, k, n, alg.kt, bmax);
-        fmm_count_launch(2);
-    }
-    gp.s = s;
-    gp.zlevel = d.k_pad <= 128 ? 7 : 6;
-    gp.nkb = (int)(d.k_pad / kBK);
-    gp.tiles_m = (int)(d.m_pad / kTileM);
-    gp.tiles_n = (int)(d.n_pad / kTileN);
-    gp.m_pad = (int)d.m_pad;
-    gp.n_pad = (int)d.n_pad;
-    gp.Z = Z;
-    gp.item_begin = 0;
-    const int64_t tiles = (int64_t)gp.tiles_m * gp.tiles_n;
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const bool timed = g_timing;
+    if (timed) {
+        timing_mark(st, true);
+        std::lock_guard<std::mutex> lk(g_timing_mu);
+        g_timed_products += (uint64_t)nprod_timed;
+    }
+    split_gemm_kernel<<<(unsigned)std::min<int64_t>(nitems, sms), kGemmThreads, kGemmSmem, st>>>(gl);
+    if (timed) timing_mark(st, false);
+    fmm_count_launch(1);
+    return FMM_OK;
+}
+
+static int split_launch_budget(const AlgView& alg, int64_t m, int64_t n, int64_t k, double alpha,
+                               const double* A, int64_t lda, const double* B, int64_t ldb, double beta,
+                               double* C, int64_t ldc, int s, void* ws, size_t ws_bytes, size_t budget,
+                               cudaStream_t st)
+{
+    SplitJob j;
+    int rc = job_init(j, alg, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, s);
+    if (rc != FMM_OK) return rc;
+    if (!j.trivial && (rc = job_bind(j, ws, ws_bytes, budget)) != FMM_OK) return rc;
+    if ((rc = job_prologue(j, st)) != FMM_OK || j.trivial) return rc;
+    const int G = j.L.group;
     for (int r0 = 0; r0 < alg.R; r0 += G) {
         const int np = std::min(G, alg.R - r0);
-        for (int q = 0; q < np; ++q) {
-            const int r = r0 + q;
-            int* er = e_row + (int64_t)q * d.m_pad;
-            int* fc = f_col + (int64_t)q * d.n_pad;
-            exps_kernel<<<(unsigned)((d.m_pad + d.n_pad + 255) / 256), 256, 0, st>>>(
-                alg.tab, r, m, n, k, d.m_pad, d.n_pad, amax, bmax, er, fc);
-            launch_packs(s, alg.tab, r, A, lda, B, ldb, m, n, k, d.m_pad, d.n_pad, d.k_pad, er, fc,
-                         sa + (int64_t)q * s * d.m_pad * d.k_pad, sb + (int64_t)q * s * d.n_pad * d.k_pad, st);
-            fmm_count_launch(3);
-        }
-        if (np * tiles > 0x7fffffffLL) return FMM_ERR_UNSUPPORTED;
-        gl.nitems = (int)(np * tiles);
-        const bool timed = g_timing;
-        if (timed) {
-            timing_mark(st, true);
-            std::lock_guard<std::mutex> lk(g_timing_mu);
-            g_timed_products += (uint64_t)np;
-        }
-        split_gemm_kernel<<<(unsigned)std::min<int64_t>(gl.nitems, sms), kGemmThreads, kGemmSmem, st>>>(gl);
-        if (timed) timing_mark(st, false);
-        fmm_count_launch(1);
-        const int64_t elems = d.me * d.ne;   /* the largest part's extent */
-        if (elems > 0xffffffffLL) return FMM_ERR_UNSUPPORTED;
-        scatter_kernel<<<dim3((unsigned)((elems + 255) / 256), (unsigned)(alg.mt * alg.nt)), 256, 0, st>>>(
-            alg.tab, r0, np, m, n, (int)d.m_pad, (int)d.n_pad, gp.zlevel, alpha, Z, e_row, f_col, C, ldc);
-        fmm_count_launch(1);
+        if ((rc = job_pack(j, r0, np, st)) != FMM_OK) return rc;
+        GemmLaunch gl;
+        memset(&gl, 0, sizeof(gl));
+        gl.nprob = 1;
+        if ((rc = job_fill(j, gl.prob[0], np, 0)) != FMM_OK) return rc;
+        if ((rc = launch_gemm(gl, job_items(j, np), np, st)) != FMM_OK) return rc;
+        job_scatter(j, r0, np, st);
     }
     return cudaGetLastError() == cudaSuccess ? FMM_OK : FMM_ERR_CUDA;
 }
+
+/* Batched split-form GEMMs: problems are taken in order into waves of at
+ * most kMaxLaunchProblems whose whole workspaces (all products at once) fit
+ * together; per wave every problem is packed, one persistent GEMM launch
+ * covers all their (problem, product, tile) items, then each problem's C is
+ * updated. A problem too large to share the workspace runs alone with
+ * product groups. Every problem's result equals its single-call result. */
+int fmm_split_batch(int count, const SplitJob* jobs_in, void* ws, size_t ws_bytes, cudaStream_t st)
+{
+    std::vector<SplitJob> jobs(jobs_in, jobs_in + count);
+    std::vector<size_t> full(count, 0);
+    for (int i = 0; i < count; ++i)
+        if (!jobs[i].trivial) {
+            const WsLayout Lf = ws_layout_g(jobs[i].alg, jobs[i].d, jobs[i].m, jobs[i].n, jobs[i].s, jobs[i].alg.R);
+            full[i] = Lf.total;
+        }
+    int i = 0;
+    while (i < count) {
+        if (jobs[i].trivial) {
+            int rc = job_prologue(jobs[i], st);
+            if (rc != FMM_OK) return rc;
+            ++i;
+            continue;
+        }
+        if (full[i] > ws_bytes) {
+            SplitJob& j = jobs[i];
+            int rc = split_launch_budget(j.alg, j.m, j.n, j.k, j.alpha, j.A, j.lda, j.B, j.ldb, j.beta, j.C, j.ldc,
+                                         j.s, ws, ws_bytes, ws_bytes, st);
+            if (rc != FMM_OK) return rc;
+            ++i;
+            continue;
+        }
+        /* gather a wave */
+        int e = i;
+        size_t used = 0;
+        while (e < count && e - i < kMaxLaunchProblems && !jobs[e].trivial && used + full[e] <= ws_bytes &&
+               (int64_t)jobs[e].alg.R * jobs[e].s * std::max(jobs[e].d.m_pad, jobs[e].d.n_pad) <= 0x7fffffffLL) {
+            used += (full[e] + 255) / 256 * 256;
+            ++e;
+        }
+        if (e == i) return FMM_ERR_WORKSPACE;
+        GemmLaunch gl;
+        memset(&gl, 0, sizeof(gl));
+        gl.nprob = e - i;
+        size_t off = 0;
+        int64_t items = 0;
+        int prods = 0;
+        for (int q = i; q < e; ++q) {
+            SplitJob& j = jobs[q];
+            int rc = job_bind_group(j, (uint8_t*)ws + off, full[q], j.alg.R);
+            if (rc != FMM_OK) return rc;
+            off += (full[q] + 255) / 256 * 256;
+            if ((rc = job_prologue(j, st)) != FMM_OK) return rc;
+            if ((rc = job_pack(j, 0, j.alg.R, st)) != FMM_OK) return rc;
+            if ((rc = job_fill(j, gl.prob[q - i], j.alg.R, (int)items)) != FMM_OK) return rc;
+            items += job_items(j, j.alg.R);
+            prods += j.alg.R;
+        }
+        int rc = launch_gemm(gl, items, prods, st);
+        if (rc != FMM_OK) return rc;
+        for (int q = i; q < e; ++q) job_scatter(jobs[q], 0, jobs[q].alg.R, st);
+        i = e;
+    }
+    return cudaGetLastError() == cudaSuccess ? FMM_OK : FMM_ERR_CUDA;
+}
+
+/* workspace the batch would use with everything in one wave where possible */
+size_t fmm_split_batch_ws(int count, const SplitJob* jobs)
+{
+    size_t sum = 0, mx = 0;
+    for (int i = 0; i < count; ++i) {
+        if (jobs[i].trivial) continue;
+        const size_t f = ws_layout_g(jobs[i].alg, jobs[i].d, jobs[i].m, jobs[i].n, jobs[i].s, jobs[i].alg.R).total;
+        sum += (f + 255) / 256 * 256;
+        const size_t one = ws_layout(jobs[i].alg, jobs[i].m, jobs[i].n, jobs[i].k, jobs[i].s, 1).total;
+        mx = std::max(mx, one);
+    }
+    return std::max(std::min(sum, kGroupBudget), mx);
+}
+
+int fmm_split_job_make(SplitJob** out, const AlgView& alg, int64_t m, int64_t n, int64_t k, double alpha,
+                       const double* A, int64_t lda, const double* B, int64_t ldb, double beta, double* C,
+                       int64_t ldc, int s)
+{
+    SplitJob* j = new SplitJob;
+    int rc = job_init(*j, alg, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, s);
+    if (rc != FMM_OK) { delete j; return rc; }
+    *out = j;
+    return FMM_OK;
+}
+
+void fmm_split_job_free(SplitJob* j) { delete j; }
 
 int fmm_split_launch(const AlgView& alg, int64_t m, int64_t n, int64_t k, double alpha,
                      const double* A, int64_t lda, const double* B, int64_t ldb, double beta,
@@ -1148,4 +1336,73 @@ extern "C" int fmm_gpu_split_dgemm_noalloc(const fmm_t* fmm, int levels, int64_t
     alg.htab = table.data();
     return split_launch_budget(alg, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, slices, scratch + tab_bytes,
                                ws_bytes, ws_bytes, st);
+}
+
+/* ---------------------------------------------------------------------------
+ * Batched entry point (include/fmm_gb300.h).
+ * ------------------------------------------------------------------------- */
+namespace {
+
+int batch_jobs(int count, const fmm_batch_problem* probs, std::vector<SplitJob>& jobs,
+               std::vector<int>& f64_idx, std::vector<AlgView>& f64_alg)
+{
+    if (count < 0 || (count > 0 && probs == nullptr)) return FMM_ERR_ARG;
+    for (int i = 0; i < count; ++i) {
+        const fmm_batch_problem& p = probs[i];
+        if (p.m < 0 || p.n < 0 || p.k < 0) return FMM_ERR_ARG;
+        if (p.lda < (p.m > 1 ? p.m : 1) || p.ldb < (p.k > 1 ? p.k : 1) || p.ldc < (p.m > 1 ? p.m : 1))
+            return FMM_ERR_ARG;
+        if (p.m > 0 && p.n > 0 && p.C == nullptr) return FMM_ERR_ARG;
+        if (p.m > 0 && p.n > 0 && p.k > 0 && (p.A == nullptr || p.B == nullptr)) return FMM_ERR_ARG;
+        if (p.slices != 0 && (p.slices < 2 || p.slices > 8)) return FMM_ERR_ARG;
+        fmm_t flat;
+        int owned = 0;
+        int rc = fmm_flatten(p.fmm, p.fmm ? p.levels : 0, &flat, &owned);
+        if (rc != FMM_OK) return rc;
+        AlgView alg;
+        rc = fmm_alg_get(&flat, &alg);
+        if (owned) free_fmm(flat);
+        if (rc != FMM_OK) return rc;
+        if (p.slices == 0) {
+            f64_idx.push_back(i);
+            f64_alg.push_back(alg);
+            continue;
+        }
+        SplitJob j;
+        rc = job_init(j, alg, p.m, p.n, p.k, p.alpha, p.A, p.lda, p.B, p.ldb, p.beta, p.C, p.ldc, p.slices);
+        if (rc != FMM_OK) return rc;
+        jobs.push_back(j);
+    }
+    return FMM_OK;
+}
+
+}  // namespace
+
+extern "C" size_t fmm_gpu_batch_workspace_size(int count, const fmm_batch_problem* probs)
+{
+    std::vector<SplitJob> jobs;
+    std::vector<int> fi;
+    std::vector<AlgView> fa;
+    if (batch_jobs(count, probs, jobs, fi, fa) != FMM_OK) return 0;
+    if (jobs.empty()) return 256;
+    return fmm_split_batch_ws((int)jobs.size(), jobs.data());
+}
+
+extern "C" int fmm_gpu_batch_dgemm(int count, const fmm_batch_problem* probs, void* workspace,
+                                   size_t workspace_bytes, void* stream)
+{
+    std::vector<SplitJob> jobs;
+    std::vector<int> fi;
+    std::vector<AlgView> fa;
+    int rc = batch_jobs(count, probs, jobs, fi, fa);
+    if (rc != FMM_OK) return rc;
+    if (fmm_device_error_word() == nullptr) return FMM_ERR_CUDA;
+    cudaStream_t st = (cudaStream_t)stream;
+    for (size_t q = 0; q < fi.size(); ++q) {
+        const fmm_batch_problem& p = probs[fi[q]];
+        rc = fmm_f64_launch(fa[q], p.m, p.n, p.k, p.alpha, p.A, p.lda, p.B, p.ldb, p.beta, p.C, p.ldc, st);
+        if (rc != FMM_OK) return rc;
+    }
+    if (jobs.empty()) return FMM_OK;
+    return fmm_split_batch((int)jobs.size(), jobs.data(), workspace, workspace_bytes, st);
 }

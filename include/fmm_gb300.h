@@ -181,6 +181,40 @@ int fmm_gpu_split_dgemm(const fmm_t* fmm, int levels,
                         int slices, void* workspace, size_t workspace_bytes,
                         void* stream);
 
+/* ------------------------------------------------------- GPU, batched -- */
+
+/* One GEMM of a batch: C := beta*C + alpha*A*B with `levels` levels of `fmm`
+ * (NULL: classical), in the split form with `slices` digit slices, or in the
+ * plain FP64 form when slices == 0. Device pointers, column-major. */
+typedef struct fmm_batch_problem_s {
+    const fmm_t* fmm;
+    int levels;
+    int slices;
+    int64_t m, n, k;
+    double alpha;
+    const double* A;
+    int64_t lda;
+    const double* B;
+    int64_t ldb;
+    double beta;
+    double* C;
+    int64_t ldc;
+} fmm_batch_problem;
+
+/* Recommended workspace for fmm_gpu_batch_dgemm (capped at 32 GiB; any size
+ * that holds the largest problem's one-product workspace works). */
+size_t fmm_gpu_batch_workspace_size(int count, const fmm_batch_problem* problems);
+
+/* Runs `count` independent GEMMs (their C regions must not overlap). Split-
+ * form problems go in waves: every problem of a wave is packed, one
+ * persistent tensor-core launch covers all their (problem, product, tile)
+ * work items, then each C is updated; each problem's result is bit-identical
+ * to its fmm_gpu_split_dgemm result. Plain FP64 problems run in order through
+ * the FP64 kernel. No counterpart in the reference (which runs one GEMM per
+ * call). Asynchronous on `stream`. */
+int fmm_gpu_batch_dgemm(int count, const fmm_batch_problem* problems,
+                        void* workspace, size_t workspace_bytes, void* stream);
+
 /* fmm_gpu_split_dgemm for callers that must not allocate device memory
  * while they run (code inside a CUDA graph capture or a stream callback,
  * plug-ins working in memory a host application hands them, processes whose

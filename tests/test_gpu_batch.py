@@ -1,0 +1,75 @@
+"""Batched execution (fmm_gpu_batch_dgemm): every problem of a batch of
+uneven GEMMs -- mixed algorithms, levels, slice counts and plain FP64
+problems -- must give bit for bit what its own single call gives."""
+import numpy as np
+import pytest
+
+from conftest import COEFFS, rand
+from gpu_util import to_dev, to_host
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    import torch
+    assert torch.cuda.is_available()
+    return torch
+
+
+def single(fmm, p):
+    dC = to_dev(p["C0"])
+    if p["slices"]:
+        fmm.split_dgemm(p["A"], p["B"], dC, p["fmm"], p["levels"], p["slices"], alpha=p["alpha"], beta=p["beta"])
+    else:
+        fmm.dgemm(p["A"], p["B"], dC, p["fmm"], p["levels"], alpha=p["alpha"], beta=p["beta"])
+    return to_host(dC)
+
+
+def make_problems(fmm, seed, count):
+    rng = np.random.default_rng(seed)
+    algs = {a: fmm.new_fmm(COEFFS / f"{a}.txt") for a in ("222", "232", "333")}
+    probs = []
+    for i in range(count):
+        m, n, k = (int(x) for x in np.exp(rng.uniform(np.log(8), np.log(700), 3)))
+        choice = rng.integers(0, 5)
+        f, levels = [(None, 0), (algs["222"], 1), (algs["222"], 2), (algs["232"], 1), (algs["333"], 1)][choice]
+        slices = int(rng.choice([0, 3, 5, 6, 7])) if i % 4 else 0
+        C0 = rand(m, n, 1000 + i)
+        probs.append({"A": to_dev(rand(m, k, 2000 + i)), "B": to_dev(rand(k, n, 3000 + i)), "C0": C0,
+                      "C": to_dev(C0), "fmm": f, "levels": levels, "slices": slices,
+                      "alpha": float(rng.choice([1.0, -0.5])), "beta": float(rng.choice([1.0, 0.0, 2.0]))})
+    return probs, algs
+
+
+@pytest.mark.parametrize("ws_scale", [1.0, 0.02])
+def test_batch_bitexact_vs_single_calls(fmm, torch_cuda, ws_scale):
+    import torch
+    probs, algs = make_problems(fmm, 7, 40)
+    try:
+        batch = fmm.make_batch(probs)
+        need = fmm.batch_workspace_size(batch)
+        ws = torch.empty(max(int(need * ws_scale), 1 << 20), dtype=torch.uint8, device="cuda")
+        if ws_scale < 1.0:
+            # small workspace: many waves, the largest problems run alone
+            ws = torch.empty(max(int(need * ws_scale), 64 << 20), dtype=torch.uint8, device="cuda")
+        fmm.batch_dgemm(batch, workspace=ws)
+        torch.cuda.synchronize()
+        for i, p in enumerate(probs):
+            want = single(fmm, p)
+            assert np.array_equal(to_host(p["C"]), want), f"problem {i}"
+        assert fmm.take_device_error() == 0
+    finally:
+        for f in algs.values():
+            fmm.free_fmm(f)
+
+
+def test_batch_empty_and_degenerate(fmm, torch_cuda):
+    import torch
+    fmm.batch_dgemm([])
+    C0 = rand(5, 4, 1)
+    p = {"A": to_dev(np.zeros((5, 0), order="F")), "B": to_dev(np.zeros((0, 4), order="F")), "C": to_dev(C0),
+         "fmm": fmm.strassen_fmm(), "levels": 1, "slices": 6, "beta": 3.0}
+    fmm.batch_dgemm([p])
+    torch.cuda.synchronize()
+    assert np.array_equal(to_host(p["C"]), 3.0 * C0)
