@@ -339,8 +339,7 @@ def main():
     cpu = None
     if rank == 0 and not args.no_cpu:
         eff, info = cpu_reference(args.alg, levels, n, 15.0,
-                                  [np.asfortranarray(hA.numpy()), np.asfortranarray(hB.numpy()),
-                                   np.asfortranarray(hC.numpy())])
+                                  [np.asfortranarray(X.cpu().numpy()) for X in (A, B, C0)])
         cpu = {"value": eff, "unit": "TFLOP/s", "cores": info["cores"], "kind": "port",
                "sample": (f"oracle FP64 FMM {args.alg} x{levels} at m=n=k={n}: products 0..{info['products']} "
                           f"of {info['of']} ({info['seconds']:.1f} s), extrapolated")}
