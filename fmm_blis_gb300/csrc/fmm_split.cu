@@ -122,27 +122,31 @@ __device__ __forceinline__ Digits split_offset(double x, int E)
     return Digits{X, (uint64_t)X + kOff};
 }
 
-/* digit t (0 = most significant) as an exact float */
+/* digit t (0 = most significant) as an exact float. A lower digit is byte
+ * S-1-t of Y minus 128: the byte is placed in the mantissa of 2^23 (one byte
+ * permute) and 2^23 + 128 is subtracted, both exact. The top digit goes
+ * through the same 2^23-offset conversion from its integer value. With t a
+ * compile-time constant after unrolling, the byte choice folds away. */
 template <int S>
 __device__ __forceinline__ float digit_f(const Digits& g, int t)
 {
     constexpr int sh = 8 * (S - 1);
     constexpr uint64_t kOff = S > 1 ? (0x8080808080808080ull >> (8 * (9 - S))) : 0ull;
     constexpr uint64_t kMask = (1ull << sh) - 1;
-    int d;
-    if (t == 0) d = (int)(g.X >> sh) + (int)((((uint64_t)g.X & kMask) + kOff) >> sh);
-    else d = (int)((g.Y >> (8 * (S - 1 - t))) & 255u) - 128;
-    /* exact int -> float for |d| < 2^22 */
-    return __int_as_float(0x4B400000 + d) - 12582912.0f;
+    if (t == 0) {
+        const int d = (int)(g.X >> sh) + (int)((((uint64_t)g.X & kMask) + kOff) >> sh);
+        return __int_as_float(0x4B400000 + d) - 12582912.0f;   /* exact for |d| < 2^22 */
+    }
+    const int bi = S - 1 - t;
+    const uint32_t w = bi < 4 ? (uint32_t)g.Y : (uint32_t)(g.Y >> 32);
+    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u + (unsigned)(bi & 3))) - 8388736.0f;
 }
 
-/* c * v for a small integer coefficient, exact like the FP64 product: sign
- * flips for c = +-1 (no FP64 instruction), the FP64 product otherwise. */
-__device__ __forceinline__ double coef_mul(float c, double v)
+/* two floats that are exact in BF16 (at most 8 significant bits) as a packed
+ * bf16x2 word, first value in the low half: their upper 16 bits */
+__device__ __forceinline__ uint32_t pack_bf16x2_exact(float lo, float hi)
 {
-    if (c == 1.0f) return v;
-    if (c == -1.0f) return __longlong_as_double(__double_as_longlong(v) ^ (long long)0x8000000000000000ull);
-    return (double)c * v;
+    return __byte_perm(__float_as_uint(lo), __float_as_uint(hi), 0x7632u);
 }
 
 /* v * 2^e, in at most two exact power-of-two multiplications. */
@@ -232,14 +236,19 @@ __global__ void bmax_kernel(const double* __restrict__ B, int64_t ldb, int64_t k
     if (lane == 0) bmax[(int64_t)b * n + j] = mx;
 }
 
-/* Row exponents of S_r (rows < m_pad) and column exponents of T_r. */
-__global__ void exps_kernel(const int* __restrict__ tab, int r, int64_t m, int64_t n, int64_t k,
+/* Row exponents of S_r (rows < m_pad) and column exponents of T_r for the
+ * products r = r0 + blockIdx.y of a group, into e_row[q][m_pad] and
+ * f_col[q][n_pad]. */
+__global__ void exps_kernel(const int* __restrict__ tab, int r0, int64_t m, int64_t n, int64_t k,
                             int64_t m_pad, int64_t n_pad,
                             const unsigned long long* __restrict__ amax,
                             const unsigned long long* __restrict__ bmax,
                             int* __restrict__ e_row, int* __restrict__ f_col)
 {
     const Tab t = tab_view(tab);
+    const int r = r0 + (int)blockIdx.y;
+    e_row += (int64_t)blockIdx.y * m_pad;
+    f_col += (int64_t)blockIdx.y * n_pad;
     const int64_t me = (m + t.mt - 1) / t.mt, ne = (n + t.nt - 1) / t.nt;
     const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (idx < m_pad) {
@@ -284,18 +293,46 @@ __global__ void exps_kernel(const int* __restrict__ tab, int r, int64_t m, int64
 
 constexpr int kPackMaxEnt = 256;
 
+/* one sub-block term of a packing sum: base pointer, extent, coefficient as
+ * a double and its kind (0: +1, 1: -1, 2: other), so the per-element code
+ * does no conversion and no FP64 compare */
 struct PEnt {
     const double* base;
+    double coef;
     int rows, cols;
-    float coef;
+    int kind;
     int pad;
 };
 
-/* A side: tile of 64 rows x 64 k of S_r; digits written row-major (K-major)
- * into slices sa[t][m_pad][k_pad]. */
+__device__ __forceinline__ PEnt make_pent(const double* base, int64_t rows, int64_t cols, int c)
+{
+    PEnt x;
+    x.base = base;
+    x.coef = (double)c;
+    x.rows = (int)rows;
+    x.cols = (int)cols;
+    x.kind = c == 1 ? 0 : (c == -1 ? 1 : 2);
+    x.pad = 0;
+    return x;
+}
+
+/* first term of a packing sum: c * v, exact like the FP64 product; sign flips
+ * for c = +-1 keep it off the FP64 pipe */
+__device__ __forceinline__ double first_term(const PEnt& x, double v)
+{
+    if (x.kind == 0) return v;
+    if (x.kind == 1) return __longlong_as_double(__double_as_longlong(v) ^ (long long)0x8000000000000000ull);
+    return x.coef * v;
+}
+
+/* A side, all products r0 .. r0+np-1 of a group in one launch: CTA (q, tile)
+ * forms the tile of 64 rows x 64 k of S_r, r = r0 + q, and writes its digits
+ * row-major (K-major) into slices sa[q][t][m_pad][k_pad]. The product index
+ * runs fastest in the block order, so the products at one tile position run
+ * together and read their shared A sub-block tiles through L2 once. */
 template <int S>
 __global__ void __launch_bounds__(256)
-pack_a_kernel(const int* __restrict__ tab, int r, const double* __restrict__ A, int64_t lda,
+pack_a_kernel(const int* __restrict__ tab, int r0, int np, const double* __restrict__ A, int64_t lda,
               int64_t m, int64_t k, int64_t m_pad, int64_t k_pad,
               const int* __restrict__ e_row, uint16_t* __restrict__ sa)
 {
@@ -303,19 +340,18 @@ pack_a_kernel(const int* __restrict__ tab, int r, const double* __restrict__ A, 
     __shared__ PEnt ent[kPackMaxEnt];
     const Tab t = tab_view(tab);
     const int64_t me = (m + t.mt - 1) / t.mt, ke = (k + t.kt - 1) / t.kt;
-    const int64_t i0 = (int64_t)blockIdx.x * 64, p0 = (int64_t)blockIdx.y * 64;
+    const int q = (int)(blockIdx.x % (unsigned)np);
+    const int r = r0 + q;
+    const int64_t i0 = (int64_t)(blockIdx.x / (unsigned)np) * 64, p0 = (int64_t)blockIdx.y * 64;
+    e_row += (int64_t)q * m_pad;
+    sa += (int64_t)q * S * m_pad * k_pad;
     const int eb = t.u_off[r], ne_ = t.u_off[r + 1] - eb;
     for (int e = threadIdx.x; e < ne_; e += blockDim.x) {
         const int part = t.u_ent[2 * (eb + e)];
         int64_t ro, rl, co, cl;
         fmm_part_geom(m, t.mt, part / t.kt, &ro, &rl);
         fmm_part_geom(k, t.kt, part % t.kt, &co, &cl);
-        PEnt x;
-        x.base = A + ro + co * lda;
-        x.rows = (int)rl; x.cols = (int)cl;
-        x.coef = (float)t.u_ent[2 * (eb + e) + 1];
-        x.pad = 0;
-        ent[e] = x;
+        ent[e] = make_pent(A + ro + co * lda, rl, cl, t.u_ent[2 * (eb + e) + 1]);
     }
     __syncthreads();
     const int li = threadIdx.x % 64;
@@ -324,11 +360,15 @@ pack_a_kernel(const int* __restrict__ tab, int r, const double* __restrict__ A, 
         const int lp = threadIdx.x / 64 + 4 * q;
         const int64_t gi = i0 + li, gp = p0 + lp;
         double sum = 0.0;
-        if (gi < me && gp < ke) {
-            for (int e = 0; e < ne_; ++e) {
-                const PEnt x = ent[e];
+        if (ne_ > 0 && gi < me && gp < ke) {
+            {
+                const PEnt& x = ent[0];
+                sum = first_term(x, (gi < x.rows && gp < x.cols) ? x.base[gi + gp * lda] : 0.0);
+            }
+            for (int e = 1; e < ne_; ++e) {
+                const PEnt& x = ent[e];
                 const double v = (gi < x.rows && gp < x.cols) ? x.base[gi + gp * lda] : 0.0;
-                sum = e == 0 ? coef_mul(x.coef, v) : fma((double)x.coef, v, sum);
+                sum = fma(x.coef, v, sum);
             }
         }
         Sf[lp][li] = sum;
@@ -346,56 +386,61 @@ pack_a_kernel(const int* __restrict__ tab, int r, const double* __restrict__ A, 
         for (int tt = 0; tt < S; ++tt) {
             uint32_t w[4];
 #pragma unroll
-            for (int h = 0; h < 4; ++h) {
-                const __nv_bfloat162 b2 = __floats2bfloat162_rn(digit_f<S>(Y[2 * h], tt), digit_f<S>(Y[2 * h + 1], tt));
-                w[h] = *reinterpret_cast<const uint32_t*>(&b2);
-            }
+            for (int h = 0; h < 4; ++h) w[h] = pack_bf16x2_exact(digit_f<S>(Y[2 * h], tt), digit_f<S>(Y[2 * h + 1], tt));
             uint4* dst = (uint4*)(sa + ((int64_t)tt * m_pad + gi) * k_pad + p0 + kg * 8);
             *dst = make_uint4(w[0], w[1], w[2], w[3]);
         }
     }
 }
 
-/* B side: tile of 32 columns x 64 k of T_r (column j of T_r is contiguous in
- * k already); digits written into slices sb[t][n_pad][k_pad]. */
+/* B side, all products of a group: CTA (q, tile) forms the tile of 32
+ * columns x 64 k of T_r, r = r0 + q (column j of T_r is contiguous in k
+ * already), and writes its digits into slices sb[q][t][n_pad][k_pad];
+ * product index fastest, as on the A side. */
 template <int S>
 __global__ void __launch_bounds__(256)
-pack_b_kernel(const int* __restrict__ tab, int r, const double* __restrict__ B, int64_t ldb,
+pack_b_kernel(const int* __restrict__ tab, int r0, int np, const double* __restrict__ B, int64_t ldb,
               int64_t k, int64_t n, int64_t n_pad, int64_t k_pad,
               const int* __restrict__ f_col, uint16_t* __restrict__ sb)
 {
     __shared__ PEnt ent[kPackMaxEnt];
     const Tab t = tab_view(tab);
     const int64_t ne = (n + t.nt - 1) / t.nt, ke = (k + t.kt - 1) / t.kt;
+    const int q = (int)(blockIdx.x % (unsigned)np);
+    const int r = r0 + q;
+    f_col += (int64_t)q * n_pad;
+    sb += (int64_t)q * S * n_pad * k_pad;
     const int eb = t.v_off[r], ne_ = t.v_off[r + 1] - eb;
     for (int e = threadIdx.x; e < ne_; e += blockDim.x) {
         const int part = t.v_ent[2 * (eb + e)];
         int64_t ro, rl, co, cl;
         fmm_part_geom(k, t.kt, part / t.nt, &ro, &rl);
         fmm_part_geom(n, t.nt, part % t.nt, &co, &cl);
-        PEnt x;
-        x.base = B + ro + co * ldb;
-        x.rows = (int)rl; x.cols = (int)cl;
-        x.coef = (float)t.v_ent[2 * (eb + e) + 1];
-        x.pad = 0;
-        ent[e] = x;
+        ent[e] = make_pent(B + ro + co * ldb, rl, cl, t.v_ent[2 * (eb + e) + 1]);
     }
     __syncthreads();
     const int kg = threadIdx.x % 8;
-    const int64_t gj = (int64_t)blockIdx.x * 32 + threadIdx.x / 8;
+    const int64_t gj = (int64_t)(blockIdx.x / (unsigned)np) * 32 + threadIdx.x / 8;
     const int64_t p0 = (int64_t)blockIdx.y * 64 + kg * 8;
     double v8[8];
 #pragma unroll
     for (int x = 0; x < 8; ++x) v8[x] = 0.0;
-    if (gj < ne) {
-        for (int e = 0; e < ne_; ++e) {
-            const PEnt x = ent[e];
-            const double c = (double)x.coef;
+    if (ne_ > 0 && gj < ne) {
+        {
+            const PEnt& x = ent[0];
+#pragma unroll
+            for (int y = 0; y < 8; ++y) {
+                const int64_t gp = p0 + y;
+                v8[y] = first_term(x, (gp < ke && gp < x.rows && gj < x.cols) ? x.base[gp + gj * ldb] : 0.0);
+            }
+        }
+        for (int e = 1; e < ne_; ++e) {
+            const PEnt& x = ent[e];
 #pragma unroll
             for (int y = 0; y < 8; ++y) {
                 const int64_t gp = p0 + y;
                 const double v = (gp < ke && gp < x.rows && gj < x.cols) ? x.base[gp + gj * ldb] : 0.0;
-                v8[y] = e == 0 ? coef_mul(x.coef, v) : fma(c, v, v8[y]);
+                v8[y] = fma(x.coef, v, v8[y]);
             }
         }
     }
@@ -407,39 +452,37 @@ pack_b_kernel(const int* __restrict__ tab, int r, const double* __restrict__ B, 
     for (int tt = 0; tt < S; ++tt) {
         uint32_t w[4];
 #pragma unroll
-        for (int h = 0; h < 4; ++h) {
-            const __nv_bfloat162 b2 = __floats2bfloat162_rn(digit_f<S>(Y[2 * h], tt), digit_f<S>(Y[2 * h + 1], tt));
-            w[h] = *reinterpret_cast<const uint32_t*>(&b2);
-        }
+        for (int h = 0; h < 4; ++h) w[h] = pack_bf16x2_exact(digit_f<S>(Y[2 * h], tt), digit_f<S>(Y[2 * h + 1], tt));
         uint4* dst = (uint4*)(sb + ((int64_t)tt * n_pad + gj) * k_pad + p0);
         *dst = make_uint4(w[0], w[1], w[2], w[3]);
     }
 }
 
 template <int S>
-void launch_packs_t(const int* tab, int r, const double* A, int64_t lda, const double* B, int64_t ldb,
+void launch_packs_t(const int* tab, int r, int np, const double* A, int64_t lda, const double* B, int64_t ldb,
                     int64_t m, int64_t n, int64_t k, int64_t m_pad, int64_t n_pad, int64_t k_pad,
                     const int* e_row, const int* f_col, uint16_t* sa, uint16_t* sb, cudaStream_t st)
 {
-    pack_a_kernel<S><<<dim3((unsigned)(m_pad / 64), (unsigned)(k_pad / 64)), 256, 0, st>>>(
-        tab, r, A, lda, m, k, m_pad, k_pad, e_row, sa);
-    pack_b_kernel<S><<<dim3((unsigned)(n_pad / 32), (unsigned)(k_pad / 64)), 256, 0, st>>>(
-        tab, r, B, ldb, k, n, n_pad, k_pad, f_col, sb);
+    pack_a_kernel<S><<<dim3((unsigned)(np * (m_pad / 64)), (unsigned)(k_pad / 64)), 256, 0, st>>>(
+        tab, r, np, A, lda, m, k, m_pad, k_pad, e_row, sa);
+    pack_b_kernel<S><<<dim3((unsigned)(np * (n_pad / 32)), (unsigned)(k_pad / 64)), 256, 0, st>>>(
+        tab, r, np, B, ldb, k, n, n_pad, k_pad, f_col, sb);
 }
 
-void launch_packs(int s, const int* tab, int r, const double* A, int64_t lda, const double* B,
+/* digit slices of the products r .. r+np-1 (exponents already in place) */
+void launch_packs(int s, const int* tab, int r, int np, const double* A, int64_t lda, const double* B,
                   int64_t ldb, int64_t m, int64_t n, int64_t k, int64_t m_pad, int64_t n_pad,
                   int64_t k_pad, const int* e_row, const int* f_col, uint16_t* sa, uint16_t* sb,
                   cudaStream_t st)
 {
     switch (s) {
-    case 2: launch_packs_t<2>(tab, r, A, lda, B, ldb, m, n, k, m_pad, n_pad, k_pad, e_row, f_col, sa, sb, st); break;
-    case 3: launch_packs_t<3>(tab, r, A, lda, B, ldb, m, n, k, m_pad, n_pad, k_pad, e_row, f_col, sa, sb, st); break;
-    case 4: launch_packs_t<4>(tab, r, A, lda, B, ldb, m, n, k, m_pad, n_pad, k_pad, e_row, f_col, sa, sb, st); break;
-    case 5: launch_packs_t<5>(tab, r, A, lda, B, ldb, m, n, k, m_pad, n_pad, k_pad, e_row, f_col, sa, sb, st); break;
-    case 6: launch_packs_t<6>(tab, r, A, lda, B, ldb, m, n, k, m_pad, n_pad, k_pad, e_row, f_col, sa, sb, st); break;
-    case 7: launch_packs_t<7>(tab, r, A, lda, B, ldb, m, n, k, m_pad, n_pad, k_pad, e_row, f_col, sa, sb, st); break;
-    default: launch_packs_t<8>(tab, r, A, lda, B, ldb, m, n, k, m_pad, n_pad, k_pad, e_row, f_col, sa, sb, st); break;
+    case 2: launch_packs_t<2>(tab, r, np, A, lda, B, ldb, m, n, k, m_pad, n_pad, k_pad, e_row, f_col, sa, sb, st); break;
+    case 3: launch_packs_t<3>(tab, r, np, A, lda, B, ldb, m, n, k, m_pad, n_pad, k_pad, e_row, f_col, sa, sb, st); break;
+    case 4: launch_packs_t<4>(tab, r, np, A, lda, B, ldb, m, n, k, m_pad, n_pad, k_pad, e_row, f_col, sa, sb, st); break;
+    case 5: launch_packs_t<5>(tab, r, np, A, lda, B, ldb, m, n, k, m_pad, n_pad, k_pad, e_row, f_col, sa, sb, st); break;
+    case 6: launch_packs_t<6>(tab, r, np, A, lda, B, ldb, m, n, k, m_pad, n_pad, k_pad, e_row, f_col, sa, sb, st); break;
+    case 7: launch_packs_t<7>(tab, r, np, A, lda, B, ldb, m, n, k, m_pad, n_pad, k_pad, e_row, f_col, sa, sb, st); break;
+    default: launch_packs_t<8>(tab, r, np, A, lda, B, ldb, m, n, k, m_pad, n_pad, k_pad, e_row, f_col, sa, sb, st); break;
     }
 }
 
@@ -449,6 +492,13 @@ void launch_packs(int s, const int* tab, int r, const double* A, int64_t lda, co
  * even, then exponent offset), identical to the FP64 conversion and
  * power-of-two scaling whenever the result is a normal number; other cases
  * take the FP64 route. Keeps the per-element FP64 work to the C updates. */
+/* the FP64 route for results outside the normal range, kept out of line so
+ * the common path carries no FP64 instruction */
+__device__ __noinline__ double i64_to_double_scaled_slow(int64_t z, int e)
+{
+    return scale2((double)z, e);
+}
+
 __device__ __forceinline__ double i64_to_double_scaled(int64_t z, int e)
 {
     if (z == 0) return 0.0;
@@ -468,7 +518,7 @@ __device__ __forceinline__ double i64_to_double_scaled(int64_t z, int e)
         }
     }
     const int be = p + 1023 + e;
-    if (be < 1 || be > 2046) return scale2((double)z, e);
+    if (be < 1 || be > 2046) return i64_to_double_scaled_slow(z, e);
     return __longlong_as_double((long long)(sign | ((uint64_t)be << 52) | (m & 0x000fffffffffffffull)));
 }
 
@@ -1063,16 +1113,15 @@ static int job_pack(SplitJob& j, int r0, int np, cudaStream_t st)
     int* f_col = (int*)(j.w + j.L.fcol);
     uint16_t* sa = (uint16_t*)(j.w + j.L.sa);
     uint16_t* sb = (uint16_t*)(j.w + j.L.sb);
-    for (int q = 0; q < np; ++q) {
-        const int r = r0 + q;
-        int* er = e_row + (int64_t)q * d.m_pad;
-        int* fc = f_col + (int64_t)q * d.n_pad;
-        exps_kernel<<<(unsigned)((d.m_pad + d.n_pad + 255) / 256), 256, 0, st>>>(
-            j.alg.tab, r, j.m, j.n, j.k, d.m_pad, d.n_pad, amax, bmax, er, fc);
-        launch_packs(j.s, j.alg.tab, r, j.A, j.lda, j.B, j.ldb, j.m, j.n, j.k, d.m_pad, d.n_pad, d.k_pad, er, fc,
-                     sa + (int64_t)q * j.s * d.m_pad * d.k_pad, sb + (int64_t)q * j.s * d.n_pad * d.k_pad, st);
-        fmm_count_launch(3);
-    }
+    if (np <= 0) return FMM_OK;
+    /* one launch per kernel for the whole group (grid y holds the product of
+     * the exponent pass; the pack grids' x extent np * tiles stays far below
+     * 2^31 since np * s * max(m_pad, n_pad) < 2^31) */
+    exps_kernel<<<dim3((unsigned)((d.m_pad + d.n_pad + 255) / 256), (unsigned)np), 256, 0, st>>>(
+        j.alg.tab, r0, j.m, j.n, j.k, d.m_pad, d.n_pad, amax, bmax, e_row, f_col);
+    launch_packs(j.s, j.alg.tab, r0, np, j.A, j.lda, j.B, j.ldb, j.m, j.n, j.k, d.m_pad, d.n_pad, d.k_pad, e_row,
+                 f_col, sa, sb, st);
+    fmm_count_launch(3);
     return FMM_OK;
 }
 
