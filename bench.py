@@ -54,6 +54,8 @@ def parse():
     p.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison runs")
     p.add_argument("--no-cpu", action="store_true", help="skip the host-core baseline")
     p.add_argument("--e2e-steps", type=int, default=2)
+    p.add_argument("--form", choices=["split", "fp64"], default="split",
+                   help="split: split-BF16 FMM (the headline); fp64: the plain FP64 FMM drop-in")
     return p.parse_args()
 
 
@@ -188,6 +190,111 @@ def run_reference(args):
     print(json.dumps(out))
 
 
+L2_BYTES = 129 * 2 ** 20
+
+
+def l2_flush_buffer(torch, dev, operand_bytes):
+    """A buffer to overwrite between timed steps when the operands would stay
+    resident in L2 (less than twice its size); None otherwise."""
+    if operand_bytes >= 2 * L2_BYTES:
+        return None
+    return torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
+
+
+def timed_steps(torch, stream, steps, fn, flush):
+    """Total device milliseconds of `steps` calls of fn on `stream`: one event
+    pair around the loop, or, with a flush buffer, one pair per step with the
+    buffer overwritten (outside the events) between steps."""
+    if flush is None:
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+    pairs = []
+    for _ in range(steps):
+        flush.fill_(1.0)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fn()
+        b.record(stream)
+        pairs.append((a, b))
+    torch.cuda.synchronize()
+    return sum(a.elapsed_time(b) for a, b in pairs)
+
+
+def run_fp64(args, fmm, f, dev, world, rank, barrier, max_over_ranks):
+    """The plain FP64 FMM drop-in as the timed step (one kernel launch per
+    step, C := C + A*B); the classical FP64 GEMM of this library at the same
+    shape is timed once beside it. The FP64 FMA pipe bounds this form: the
+    roofline peak is 2 FMA/clock/SM at the maximum SM clock."""
+    import torch
+
+    n, levels = args.n, args.levels
+    flops = 2.0 * n ** 3
+    g = torch.Generator(device=dev).manual_seed(1234 + rank)
+    A = (torch.rand((n, n), generator=g, device=dev, dtype=torch.float64) * 2 - 1).t()
+    B = (torch.rand((n, n), generator=g, device=dev, dtype=torch.float64) * 2 - 1).t()
+    C0 = (torch.rand((n, n), generator=g, device=dev, dtype=torch.float64) * 2 - 1).t()
+    C = C0.clone()
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        fmm.dgemm(A, B, C, f, levels, stream=stream)
+    torch.cuda.synchronize()
+    barrier()
+    # operands smaller than twice L2: per-step events with an L2 flush between
+    flush = l2_flush_buffer(torch, dev, 3 * n * n * 8)
+    n_launch0 = fmm.launch_count()
+    with Clocks(torch.cuda.current_device()) as clk:
+        total = timed_steps(torch, stream, args.steps, lambda: fmm.dgemm(A, B, C, f, levels, stream=stream), flush)
+        barrier()
+    launches = fmm.launch_count() - n_launch0
+    ms = max_over_ranks(total / args.steps)
+    value = world * flops / (ms / 1e3) / 1e12
+    mt, kt, nt, R = f.m_tilde ** levels, f.k_tilde ** levels, f.n_tilde ** levels, f.R ** levels
+    executed = 2.0 * (-(-n // mt)) * (-(-n // nt)) * (-(-n // kt)) * R
+    clk_sum = clk.summary()
+    sm_max = clk_sum.get("sm_max_mhz") or 2070.0
+    peak = 2.0 * 2.0 * 152 * sm_max * 1e6 / 1e12      # 2 FMA/clk/SM, 2 flops per FMA
+    achieved = executed / (ms / 1e3) / 1e12
+    extra = {}
+    if rank == 0 and not args.no_fp64:
+        Cc = C0.clone()
+        Cf = C0.clone()
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        fmm.dgemm(A, B, Cc, None, 0, stream=stream)
+        t1.record(stream)
+        torch.cuda.synchronize()
+        ms_cls = t0.elapsed_time(t1)
+        fmm.dgemm(A, B, Cf, f, levels, stream=stream)
+        torch.cuda.synchronize()
+        amax, bmax = float(A.abs().max()), float(B.abs().max())
+        err = float((Cf - Cc).abs().max())
+        extra = {"fp64_classical": {"tflops": flops / ms_cls / 1e9, "ms": ms_cls},
+                 "fp64_fmm_vs_classical": ms_cls / ms,
+                 "max_err_vs_classical": err,
+                 "err_over_eps_k_amax_bmax": err / (2.0 ** -52 * n * amax * bmax)}
+    assert fmm.take_device_error() == 0
+    if rank == 0:
+        print(json.dumps({
+            "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"plain FP64 FMM {args.alg} x{levels} levels, m=n=k={n}", "m": n, "n": n, "k": n,
+                       "alg": args.alg, "levels": levels,
+                       "l2": ("L2 flushed between steps (per-step events)" if flush is not None
+                              else "inputs larger than L2; no flush"),
+                       "parallelism": f"replicas x{world}"},
+            "roofline": {"bound": "fp64_pipe", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak, "traffic": None, "kernel": "fmm_f64_kernel",
+                         "peak_kind": "nominal DFMA rate, 2 FMA/clk/SM at the max SM clock",
+                         "executed_flops_per_step": executed},
+            "cpu_baseline": None, "e2e": None, "gpu_launches": launches, "clocks": clk_sum, **extra}))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -224,6 +331,13 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
 
+    if args.form == "fp64":
+        run_fp64(args, fmm, f, dev, world, rank, barrier, max_over_ranks)
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return
+
     g = torch.Generator(device=dev).manual_seed(1234 + rank)
     A = (torch.rand((n, n), generator=g, device=dev, dtype=torch.float64) * 2 - 1).t()
     B = (torch.rand((n, n), generator=g, device=dev, dtype=torch.float64) * 2 - 1).t()
@@ -239,22 +353,18 @@ def main():
         step(C)
     torch.cuda.synchronize()
     barrier()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     n_launch0 = fmm.launch_count()
     fmm.read_kernel_timing()
     fmm.set_kernel_timing(True)
+    flush = l2_flush_buffer(torch, dev, 3 * n * n * 8)
     with Clocks(torch.cuda.current_device()) as clk:
         torch.cuda.synchronize()
         barrier()
-        e0.record(stream)
-        for _ in range(args.steps):
-            step(C)
-        e1.record(stream)
-        torch.cuda.synchronize()
+        total = timed_steps(torch, stream, args.steps, lambda: step(C), flush)
         barrier()
     fmm.set_kernel_timing(False)
     launches = fmm.launch_count() - n_launch0
-    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps)
+    ms = max_over_ranks(total / args.steps)
     gemm_ms, gemm_n, gemm_products = fmm.read_kernel_timing()
     value = world * flops / (ms / 1e3) / 1e12
 
@@ -352,7 +462,9 @@ def main():
             "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
             "config": {"workload": f"split-BF16 FMM {args.alg} x{levels} levels, m=n=k={n}, {s} slices",
                        "m": n, "n": n, "k": n, "alg": args.alg, "levels": levels, "slices": s,
-                       "l2": "inputs (3 x 2 GiB) larger than L2; no flush", "parallelism": f"replicas x{world}"},
+                       "l2": ("L2 flushed between steps (per-step events)" if flush is not None
+                              else f"inputs (3 x {n * n * 8 / 2**30:.2f} GiB) larger than L2; no flush"),
+                       "parallelism": f"replicas x{world}"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
             "clocks": clk.summary(), **extra,
         }

@@ -33,10 +33,27 @@ constexpr int kMaxEntries = 256;  /* nonzero coefficients per product column */
 
 struct Entry {
     const double* base;  /* sub-block origin in the source matrix */
+    double coef;         /* small integer coefficient, already a double */
     int rows, cols;      /* sub-block extent */
-    float coef;          /* small integer coefficient */
+    int kind;            /* 0: +1, 1: -1, 2: other (no FP64 compare per element) */
     int pad;
 };
+
+/* first term of a combination: s[t] = c * v[t], exact like the FP64
+ * product; sign flips for c = +-1 keep it off the FP64 pipe that the
+ * micro-kernel is bound by. One uniform branch for all of a thread's values. */
+template <int N>
+__device__ __forceinline__ void scale_first(const Entry& x, double (&s)[N])
+{
+    if (x.kind == 1) {
+#pragma unroll
+        for (int t = 0; t < N; ++t)
+            s[t] = __longlong_as_double(__double_as_longlong(s[t]) ^ (long long)0x8000000000000000ull);
+    } else if (x.kind == 2) {
+#pragma unroll
+        for (int t = 0; t < N; ++t) s[t] = x.coef * s[t];
+    }
+}
 
 /* Geometry of the nonzero entries [beg, end) of one product column of U
  * (or V), for a source split rt x ct, into shared memory. */
@@ -53,7 +70,8 @@ __device__ void stage_entries(const int* __restrict__ ent, int beg, int end, int
         x.base = src + ro + co * ld;
         x.rows = (int)rl;
         x.cols = (int)cl;
-        x.coef = (float)coef;
+        x.coef = (double)coef;
+        x.kind = coef == 1 ? 0 : (coef == -1 ? 1 : 2);
         x.pad = 0;
         out[e - beg] = x;
     }
@@ -108,33 +126,66 @@ fmm_f64_kernel(const int* __restrict__ tab, int64_t m, int64_t n, int64_t k,
             for (int b = 0; b < TN; ++b) acc[a][b] = 0.0;
 
         for (int64_t k0 = 0; k0 < ke; k0 += BK) {
-            /* fused pack of the A-side combination: BM x BK */
-#pragma unroll
-            for (int t = 0; t < BM * BK / NT; ++t) {
+            /* fused pack of the A-side combination: BM x BK. Each term's
+             * loads for all of this thread's elements go out together; the
+             * first term's coefficient (uniform over the CTA) is applied once
+             * after them. */
+            {
+                constexpr int NA = BM * BK / NT;
                 const int li = tid % BM;
-                const int lp = tid / BM + t * (NT / BM);
-                const int64_t gi = i0 + li, gp = k0 + lp;
-                double s = 0.0;
-                for (int e = 0; e < ue_n; ++e) {
-                    const Entry x = ue[e];
-                    const double v = (gi < x.rows && gp < x.cols) ? x.base[gi + gp * lda] : 0.0;
-                    s = e == 0 ? (double)x.coef * v : fma((double)x.coef, v, s);
+                const int64_t gi = i0 + li;
+                double s[NA];
+#pragma unroll
+                for (int t = 0; t < NA; ++t) s[t] = 0.0;
+                if (ue_n > 0) {
+                    const Entry& x0 = ue[0];
+#pragma unroll
+                    for (int t = 0; t < NA; ++t) {
+                        const int64_t gp = k0 + tid / BM + t * (NT / BM);
+                        s[t] = (gi < x0.rows && gp < x0.cols) ? x0.base[gi + gp * lda] : 0.0;
+                    }
+                    scale_first(x0, s);
                 }
-                As[lp][li] = s;
+                for (int e = 1; e < ue_n; ++e) {
+                    const Entry& x = ue[e];
+#pragma unroll
+                    for (int t = 0; t < NA; ++t) {
+                        const int64_t gp = k0 + tid / BM + t * (NT / BM);
+                        const double v = (gi < x.rows && gp < x.cols) ? x.base[gi + gp * lda] : 0.0;
+                        s[t] = fma(x.coef, v, s[t]);
+                    }
+                }
+#pragma unroll
+                for (int t = 0; t < NA; ++t) As[tid / BM + t * (NT / BM)][li] = s[t];
             }
             /* fused pack of the B-side combination: BK x BN */
-#pragma unroll
-            for (int t = 0; t < BK * BN / NT; ++t) {
+            {
+                constexpr int NB = BK * BN / NT;
                 const int lp = tid % BK;
-                const int lj = tid / BK + t * (NT / BK);
-                const int64_t gp = k0 + lp, gj = j0 + lj;
-                double s = 0.0;
-                for (int e = 0; e < ve_n; ++e) {
-                    const Entry x = ve[e];
-                    const double v = (gp < x.rows && gj < x.cols) ? x.base[gp + gj * ldb] : 0.0;
-                    s = e == 0 ? (double)x.coef * v : fma((double)x.coef, v, s);
+                const int64_t gp = k0 + lp;
+                double s[NB];
+#pragma unroll
+                for (int t = 0; t < NB; ++t) s[t] = 0.0;
+                if (ve_n > 0) {
+                    const Entry& x0 = ve[0];
+#pragma unroll
+                    for (int t = 0; t < NB; ++t) {
+                        const int64_t gj = j0 + tid / BK + t * (NT / BK);
+                        s[t] = (gp < x0.rows && gj < x0.cols) ? x0.base[gp + gj * ldb] : 0.0;
+                    }
+                    scale_first(x0, s);
                 }
-                Bs[lp][lj] = s;
+                for (int e = 1; e < ve_n; ++e) {
+                    const Entry& x = ve[e];
+#pragma unroll
+                    for (int t = 0; t < NB; ++t) {
+                        const int64_t gj = j0 + tid / BK + t * (NT / BK);
+                        const double v = (gp < x.rows && gj < x.cols) ? x.base[gp + gj * ldb] : 0.0;
+                        s[t] = fma(x.coef, v, s[t]);
+                    }
+                }
+#pragma unroll
+                for (int t = 0; t < NB; ++t) Bs[lp][tid / BK + t * (NT / BK)] = s[t];
             }
             __syncthreads();
 #pragma unroll 4
@@ -216,8 +267,13 @@ int fmm_scale_c(int64_t m, int64_t n, double beta, double* C, int64_t ldc, cudaS
 }
 
 /* Tile choice: the FP64 pipe is the bottleneck, so estimate each SM's FP64
- * work (the most tiles any SM gets, times the FMAs per tile including the
- * fused pack additions) and take the cheapest. */
+ * work for every candidate (waves of CTAs over the SMs, two resident per SM,
+ * times the FMAs per tile including the fused pack additions, over the
+ * configuration's measured efficiency) and take the cheapest. Measured on
+ * GB300 at m=n=k=16384: the 64-wide tiles with two CTAs per SM run classical
+ * FP64 at 99% of the DFMA peak, the 128 x 128 tile with one CTA per SM
+ * (248 registers) about 2% and FMM forms 5-14% slower, so it is not a
+ * candidate; 32 x 32 serves grids too small to fill the SMs. */
 int fmm_f64_launch(const AlgView& alg, int64_t m, int64_t n, int64_t k, double alpha,
                    const double* A, int64_t lda, const double* B, int64_t ldb,
                    double beta, double* C, int64_t ldc, cudaStream_t st)
@@ -231,21 +287,23 @@ int fmm_f64_launch(const AlgView& alg, int64_t m, int64_t n, int64_t k, double a
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int64_t me = (m + alg.mt - 1) / alg.mt, ne = (n + alg.nt - 1) / alg.nt;
-    const int sizes[3] = {128, 64, 32};
+    struct Cand { int id, bm, bn; double eff; };
+    const Cand cands[4] = {{3, 64, 64, 1.0}, {4, 128, 64, 0.99}, {5, 64, 128, 0.99}, {2, 32, 32, 0.8}};
     double best = 0;
-    int pick = 0;
-    for (int c = 0; c < 3; ++c) {
-        const int64_t b = sizes[c];
-        const int64_t tiles = ((me + b - 1) / b) * ((ne + b - 1) / b);
-        const double per_sm = (double)((tiles + sms - 1) / sms);
-        const double work = (double)(b * b) * (1.0 + (alg.avg_nnz_u - 1.0) / b +
-                                               (alg.avg_nnz_v - 1.0) / b + 4.0 / b);
-        const double est = per_sm * work;
-        if (c == 0 || est < best) { best = est; pick = c; }
+    int pick = 3;
+    for (int c = 0; c < 4; ++c) {
+        const int64_t bm = cands[c].bm, bn = cands[c].bn;
+        const int64_t tiles = ((me + bm - 1) / bm) * ((ne + bn - 1) / bn);
+        const double waves = (double)((tiles + 2 * (int64_t)sms - 1) / (2 * (int64_t)sms));
+        const double work = (double)(bm * bn) * (1.0 + (alg.avg_nnz_u - 1.0) / (double)bn +
+                                                 (alg.avg_nnz_v - 1.0) / (double)bm + 4.0 / (double)bm);
+        const double est = waves * work / cands[c].eff;
+        if (c == 0 || est < best) { best = est; pick = cands[c].id; }
     }
     switch (pick) {
-    case 0: return launch_cfg<128, 128, 16, 8, 8>(alg, m, n, k, alpha, A, lda, B, ldb, C, ldc, st);
-    case 1: return launch_cfg<64, 64, 16, 4, 4>(alg, m, n, k, alpha, A, lda, B, ldb, C, ldc, st);
+    case 3: return launch_cfg<64, 64, 32, 4, 4>(alg, m, n, k, alpha, A, lda, B, ldb, C, ldc, st);
+    case 4: return launch_cfg<128, 64, 16, 8, 4>(alg, m, n, k, alpha, A, lda, B, ldb, C, ldc, st);
+    case 5: return launch_cfg<64, 128, 16, 4, 8>(alg, m, n, k, alpha, A, lda, B, ldb, C, ldc, st);
     default: return launch_cfg<32, 32, 32, 2, 2>(alg, m, n, k, alpha, A, lda, B, ldb, C, ldc, st);
     }
 }

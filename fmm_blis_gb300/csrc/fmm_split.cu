@@ -316,13 +316,20 @@ __device__ __forceinline__ PEnt make_pent(const double* base, int64_t rows, int6
     return x;
 }
 
-/* first term of a packing sum: c * v, exact like the FP64 product; sign flips
- * for c = +-1 keep it off the FP64 pipe */
-__device__ __forceinline__ double first_term(const PEnt& x, double v)
+/* first term of a packing sum over a thread's values: s[t] = c * s[t],
+ * exact like the FP64 product; sign flips for c = +-1 keep it off the FP64
+ * pipe, and the branch (uniform over the CTA) is taken once for all values */
+template <int N>
+__device__ __forceinline__ void scale_first(const PEnt& x, double (&s)[N])
 {
-    if (x.kind == 0) return v;
-    if (x.kind == 1) return __longlong_as_double(__double_as_longlong(v) ^ (long long)0x8000000000000000ull);
-    return x.coef * v;
+    if (x.kind == 1) {
+#pragma unroll
+        for (int t = 0; t < N; ++t)
+            s[t] = __longlong_as_double(__double_as_longlong(s[t]) ^ (long long)0x8000000000000000ull);
+    } else if (x.kind == 2) {
+#pragma unroll
+        for (int t = 0; t < N; ++t) s[t] = x.coef * s[t];
+    }
 }
 
 /* A side, all products r0 .. r0+np-1 of a group in one launch: CTA (q, tile)
@@ -354,24 +361,37 @@ pack_a_kernel(const int* __restrict__ tab, int r0, int np, const double* __restr
         ent[e] = make_pent(A + ro + co * lda, rl, cl, t.u_ent[2 * (eb + e) + 1]);
     }
     __syncthreads();
+    /* 16 elements per thread in two halves of 8: each term's 8 loads go out
+     * together, and the first term's coefficient (uniform over the CTA) is
+     * applied once after them */
     const int li = threadIdx.x % 64;
-#pragma unroll 4
-    for (int q = 0; q < 16; ++q) {
-        const int lp = threadIdx.x / 64 + 4 * q;
-        const int64_t gi = i0 + li, gp = p0 + lp;
-        double sum = 0.0;
-        if (ne_ > 0 && gi < me && gp < ke) {
-            {
-                const PEnt& x = ent[0];
-                sum = first_term(x, (gi < x.rows && gp < x.cols) ? x.base[gi + gp * lda] : 0.0);
+    const int64_t gi = i0 + li;
+    const bool row_ok = ne_ > 0 && gi < me;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        double v8[8];
+#pragma unroll
+        for (int y = 0; y < 8; ++y) v8[y] = 0.0;
+        if (row_ok) {
+            const PEnt& x0 = ent[0];
+#pragma unroll
+            for (int y = 0; y < 8; ++y) {
+                const int64_t gp = p0 + threadIdx.x / 64 + 4 * (8 * h + y);
+                v8[y] = (gp < ke && gi < x0.rows && gp < x0.cols) ? x0.base[gi + gp * lda] : 0.0;
             }
+            scale_first(x0, v8);
             for (int e = 1; e < ne_; ++e) {
                 const PEnt& x = ent[e];
-                const double v = (gi < x.rows && gp < x.cols) ? x.base[gi + gp * lda] : 0.0;
-                sum = fma(x.coef, v, sum);
+#pragma unroll
+                for (int y = 0; y < 8; ++y) {
+                    const int64_t gp = p0 + threadIdx.x / 64 + 4 * (8 * h + y);
+                    const double v = (gp < ke && gi < x.rows && gp < x.cols) ? x.base[gi + gp * lda] : 0.0;
+                    v8[y] = fma(x.coef, v, v8[y]);
+                }
             }
         }
-        Sf[lp][li] = sum;
+#pragma unroll
+        for (int y = 0; y < 8; ++y) Sf[threadIdx.x / 64 + 4 * (8 * h + y)][li] = v8[y];
     }
     __syncthreads();
     /* thread -> (row, 8 consecutive k): 4 rows x 128 bytes per warp store */
@@ -431,8 +451,9 @@ pack_b_kernel(const int* __restrict__ tab, int r0, int np, const double* __restr
 #pragma unroll
             for (int y = 0; y < 8; ++y) {
                 const int64_t gp = p0 + y;
-                v8[y] = first_term(x, (gp < ke && gp < x.rows && gj < x.cols) ? x.base[gp + gj * ldb] : 0.0);
+                v8[y] = (gp < ke && gp < x.rows && gj < x.cols) ? x.base[gp + gj * ldb] : 0.0;
             }
+            scale_first(x, v8);
         }
         for (int e = 1; e < ne_; ++e) {
             const PEnt& x = ent[e];
@@ -630,10 +651,21 @@ split_gemm_kernel(const __grid_constant__ GemmLaunch L)
                 const int s = P.s, nkb = P.nkb;
                 const int arow = it.r * s * P.m_pad + it.tile_m * kTileM;
                 const int brow = it.r * s * P.n_pad + it.tile_n * kTileN;
-                for (int g = 2; g <= s + 1 && ok; ++g)
-                    for (int t = max(1, g - s); t <= min(s, g - 1) && ok; ++t) {
+                /* Pair order: t ascending in even levels and descending in odd
+                 * ones, so the last pair of a level and the first of the next
+                 * share a slice ((1,2)->(1,3), (3,1)->(4,1), ...), and k runs
+                 * forward and backward on alternate pairs, so a shared slice's
+                 * most recently loaded blocks are read again first, while they
+                 * are still in L2. The MMA side only counts stages; every
+                 * chunk sum is exact in any order. */
+                int pi = 0;
+                for (int g = 2; g <= s + 1 && ok; ++g) {
+                    const int tlo = max(1, g - s), thi = min(s, g - 1);
+                    for (int x = 0; x <= thi - tlo && ok; ++x, ++pi) {
+                        const int t = (g & 1) ? thi - x : tlo + x;
                         const int u = g - t;
-                        for (int kb = 0; kb < nkb; ++kb) {
+                        for (int y = 0; y < nkb; ++y) {
+                            const int kb = (pi & 1) ? nkb - 1 - y : y;
                             if (!sm103::mbar_wait(&empty[st], ph ^ 1, abort_flag, L.err, 1)) { ok = false; break; }
                             sm103::mbar_arrive_expect_tx(&full[st], kStageBytes);
                             sm103::tma_load_2d(sA + st * kATileBytes, &P.tmA, &full[st], kb * kBK,
@@ -644,6 +676,7 @@ split_gemm_kernel(const __grid_constant__ GemmLaunch L)
                             if (++st == kStages) { st = 0; ph ^= 1; armed = 0; }
                         }
                     }
+                }
             }
             if (!ok) {
                 /* let every load already issued land before the CTA exits */
@@ -708,6 +741,11 @@ split_gemm_kernel(const __grid_constant__ GemmLaunch L)
         int buf = 0;
         uint32_t aph = 0;
         bool ok = true;
+        /* Z lines stay in L2 between the level folds of an item (evict_last);
+         * the last fold marks them evict_first, as the GEMM is done with them */
+        uint64_t pol_keep, pol_drop;
+        asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol_keep));
+        asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol_drop));
         for (int b = blockIdx.x; b < L.nitems && ok; b += gridDim.x) {
             const Item it = decode_item(L, b);
             const GemmProblem& P = L.prob[it.p];
@@ -752,15 +790,16 @@ split_gemm_kernel(const __grid_constant__ GemmLaunch L)
                     const uint64_t rnd = D >= 0 ? 0 : (1ull << (rsh - 1));
                     uint64_t zp = (uint64_t)zrow;
                     const uint64_t zstep = (uint64_t)a.m_pad * 8;
+                    const uint64_t pol = g == s + 1 ? pol_drop : pol_keep;
                     if (g == 2) {
 #pragma unroll
                         for (int x = 0; x < kEpiCols; ++x)
                             asm volatile("{\n\t.reg .b64 t;\n\t"
                                          "cvt.s64.s32 t, %1;\n\t"
                                          "shl.b64 t, t, %2;\n\t"
-                                         "st.global.u64 [%0], t;\n\t"
+                                         "st.global.L2::cache_hint.u64 [%0], t, %4;\n\t"
                                          "add.u64 %0, %0, %3;\n\t}"
-                                         : "+l"(zp) : "r"(lsum[x]), "r"(lsh), "l"(zstep) : "memory");
+                                         : "+l"(zp) : "r"(lsum[x]), "r"(lsh), "l"(zstep), "l"(pol) : "memory");
                     } else {
 #pragma unroll
                         for (int x = 0; x < kEpiCols; ++x)
@@ -769,9 +808,10 @@ split_gemm_kernel(const __grid_constant__ GemmLaunch L)
                                          "shl.b64 t, t, %2;\n\t"
                                          "add.s64 t, t, %4;\n\t"
                                          "shr.s64 t, t, %3;\n\t"
-                                         "red.global.add.u64 [%0], t;\n\t"
+                                         "red.global.add.L2::cache_hint.u64 [%0], t, %6;\n\t"
                                          "add.u64 %0, %0, %5;\n\t}"
-                                         : "+l"(zp) : "r"(lsum[x]), "r"(lsh), "r"(rsh), "l"(rnd), "l"(zstep) : "memory");
+                                         : "+l"(zp) : "r"(lsum[x]), "r"(lsh), "r"(rsh), "l"(rnd), "l"(zstep), "l"(pol)
+                                         : "memory");
                     }
                 }
             }
@@ -847,6 +887,91 @@ scatter_kernel(const int* __restrict__ tab, int r0, int nprod, int64_t m, int64_
         c = fma(lam[q], i64_to_double_scaled(Z[r * zstride + zij], e_row[r * m_pad + i] + f_col[r * n_pad + j] + ebase), c);
     }
     *cp = c;
+}
+
+/* Multi-C epilogue, element-major: one thread per element (i, j) of the
+ * product grid updates that element of every C sub-block p, so each product's
+ * Z_r[i,j] is read and converted once and shared by all sub-blocks it feeds.
+ * The sub-blocks' running values live in shared memory (cs[p][thread]); for
+ * every sub-block the updates still come in increasing product order, so the
+ * result is identical to scatter_kernel's. Used when the sub-block count and
+ * the group's W entries fit the shared-memory budget. */
+constexpr int kScatterAllSmem = 32 * 1024;   /* cs[] budget: P * threads * 8 */
+
+__global__ void __launch_bounds__(256)
+scatter_all_kernel(const int* __restrict__ tab, int r0, int nprod, int64_t m, int64_t n,
+                   int m_pad, int n_pad, int zlevel, double alpha, const int64_t* __restrict__ Z,
+                   const int* __restrict__ e_row, const int* __restrict__ f_col, double* __restrict__ C,
+                   int64_t ldc)
+{
+    extern __shared__ double sm_all[];
+    const Tab t = tab_view(tab);
+    const int P = t.mt * t.nt, T = (int)blockDim.x, tid = (int)threadIdx.x;
+    const int eb = t.w_off[r0], E = t.w_off[r0 + nprod] - eb;
+    double* cs = sm_all;                 /* [P][T] */
+    double* lam = cs + (size_t)P * T;    /* [E] */
+    int* pidx = (int*)(lam + E);         /* [E] */
+    int* off = pidx + E;                 /* [nprod + 1] */
+    for (int x = tid; x < E; x += T) {
+        pidx[x] = t.w_ent[2 * (eb + x)];
+        lam[x] = alpha * (double)t.w_ent[2 * (eb + x) + 1];
+    }
+    for (int x = tid; x <= nprod; x += T) off[x] = t.w_off[r0 + x] - eb;
+    __syncthreads();
+    const int me = (int)((m + t.mt - 1) / t.mt), ne = (int)((n + t.nt - 1) / t.nt);
+    const uint64_t idx = (uint64_t)blockIdx.x * (uint64_t)T + (uint64_t)tid;
+    if (idx >= (uint64_t)me * (uint64_t)ne) return;
+    const int i = (int)(idx % (uint64_t)me), j = (int)(idx / (uint64_t)me);
+    uint64_t live = 0;
+    for (int p = 0; p < P; ++p) {
+        int ro, rl, co, cl;
+        fmm_part_geom32((int)m, t.mt, p / t.nt, &ro, &rl);
+        fmm_part_geom32((int)n, t.nt, p % t.nt, &co, &cl);
+        if (i < rl && j < cl) {
+            live |= 1ull << p;
+            cs[p * T + tid] = C[ro + i + (int64_t)(co + j) * ldc];
+        }
+    }
+    const int64_t zij = (int64_t)j * m_pad + i;
+    const int64_t zstride = (int64_t)n_pad * m_pad;
+    const int ebase = 2 - 8 * zlevel;
+    int q = 0;
+    for (; q + 4 <= nprod; q += 4) {
+        int64_t z[4];
+        int ex[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            z[u] = Z[(q + u) * zstride + zij];
+            ex[u] = e_row[(int64_t)(q + u) * m_pad + i] + f_col[(int64_t)(q + u) * n_pad + j] + ebase;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int b = off[q + u], e = off[q + u + 1];
+            if (b == e) continue;
+            const double M = i64_to_double_scaled(z[u], ex[u]);
+            for (int x = b; x < e; ++x) {
+                const int p = pidx[x];
+                if ((live >> p) & 1ull) cs[p * T + tid] = fma(lam[x], M, cs[p * T + tid]);
+            }
+        }
+    }
+    for (; q < nprod; ++q) {
+        const int b = off[q], e = off[q + 1];
+        if (b == e) continue;
+        const double M = i64_to_double_scaled(Z[q * zstride + zij],
+                                              e_row[(int64_t)q * m_pad + i] + f_col[(int64_t)q * n_pad + j] + ebase);
+        for (int x = b; x < e; ++x) {
+            const int p = pidx[x];
+            if ((live >> p) & 1ull) cs[p * T + tid] = fma(lam[x], M, cs[p * T + tid]);
+        }
+    }
+    for (int p = 0; p < P; ++p) {
+        if (!((live >> p) & 1ull)) continue;
+        int ro, rl, co, cl;
+        fmm_part_geom32((int)m, t.mt, p / t.nt, &ro, &rl);
+        fmm_part_geom32((int)n, t.nt, p % t.nt, &co, &cl);
+        C[ro + i + (int64_t)(co + j) * ldc] = cs[p * T + tid];
+    }
 }
 
 /* --------------------------------------------------------- host -------- */
@@ -1157,6 +1282,20 @@ static int64_t job_items(const SplitJob& j, int np)
 static void job_scatter(const SplitJob& j, int r0, int np, cudaStream_t st)
 {
     const int64_t elems = j.d.me * j.d.ne;   /* the largest part's extent */
+    /* element-major form when the sub-block values and the group's W entries
+     * fit: threads per block T = 32 KB / (8 P), a multiple of 32, at least 32 */
+    const Tab ht = tab_view(j.alg.htab);
+    const int P = j.alg.mt * j.alg.nt;
+    const int E = ht.w_off[r0 + np] - ht.w_off[r0];
+    int T = std::min(256, kScatterAllSmem / (8 * P)) / 32 * 32;
+    const size_t smem = (size_t)P * std::max(T, 0) * 8 + (size_t)E * 12 + (size_t)(np + 1) * 4;
+    if (P <= 64 && T >= 32 && smem <= 48 * 1024) {
+        scatter_all_kernel<<<(unsigned)((elems + T - 1) / T), (unsigned)T, smem, st>>>(
+            j.alg.tab, r0, np, j.m, j.n, (int)j.d.m_pad, (int)j.d.n_pad, job_zlevel(j), j.alpha,
+            (const int64_t*)(j.w + j.L.z), (const int*)(j.w + j.L.erow), (const int*)(j.w + j.L.fcol), j.C, j.ldc);
+        fmm_count_launch(1);
+        return;
+    }
     scatter_kernel<<<dim3((unsigned)((elems + 255) / 256), (unsigned)(j.alg.mt * j.alg.nt)), 256, 0, st>>>(
         j.alg.tab, r0, np, j.m, j.n, (int)j.d.m_pad, (int)j.d.n_pad, job_zlevel(j), j.alpha,
         (const int64_t*)(j.w + j.L.z), (const int*)(j.w + j.L.erow), (const int*)(j.w + j.L.fcol), j.C, j.ldc);
