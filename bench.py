@@ -37,6 +37,9 @@ import numpy as np
 
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
+# many differently sized request buffers (served workload): grow segments
+# instead of fragmenting fixed ones
+os.environ.setdefault("PYTORCH_ALLOC_CONF", "expandable_segments:True")
 
 METRIC = "eff. TFLOP/s (2mnk/t): split-BF16 FMM vs FP64 FMM at stated err; p99 latency"
 
@@ -56,6 +59,14 @@ def parse():
     p.add_argument("--e2e-steps", type=int, default=2)
     p.add_argument("--form", choices=["split", "fp64"], default="split",
                    help="split: split-BF16 FMM (the headline); fp64: the plain FP64 FMM drop-in")
+    p.add_argument("--workload", choices=["fmm", "batch", "serve"], default="fmm",
+                   help="fmm: one square FMM GEMM per step (the headline); batch: 512 uneven GEMMs per step; "
+                        "serve: Poisson request stream")
+    p.add_argument("--count", type=int, default=512, help="batch: GEMMs per step")
+    p.add_argument("--rate", type=float, default=200.0, help="serve: arrivals per second")
+    p.add_argument("--duration", type=float, default=60.0, help="serve: seconds of arrivals")
+    p.add_argument("--split-fraction", type=float, default=0.9, help="serve: share of split-tagged requests")
+    p.add_argument("--target", type=float, default=1e-10, help="split requests: target relative error")
     return p.parse_args()
 
 
@@ -225,6 +236,162 @@ def timed_steps(torch, stream, steps, fn, flush):
     return sum(a.elapsed_time(b) for a, b in pairs)
 
 
+def batch_shapes(count, seed, lo=256, hi=8192):
+    """count (m, n, k) triples, each dimension log-uniform in [lo, hi], seeded"""
+    rng = np.random.default_rng(seed)
+    return [tuple(int(round(float(np.exp(rng.uniform(np.log(lo), np.log(hi)))))) for _ in range(3))
+            for _ in range(count)]
+
+
+def run_batch(args, fmm, dev, world, rank, barrier, max_over_ranks):
+    """Batched uneven FMM: `count` independent GEMMs (m, n, k log-uniform in
+    [256, 8192], entries uniform [-1, 1), seeded) per step, each with the
+    plan the Tuner picks for it; one fmm_gpu_batch_dgemm call per step (one
+    persistent launch for FP64 problems, persistent waves of up to 80 split
+    problems, bounded by the workspace). The split-BF16 run at the target
+    error is the line's value; the all-FP64 run is reported beside it."""
+    import torch
+
+    from fmm_blis_gb300 import serve, tune
+
+    tuner = tune.Tuner()
+    shapes = batch_shapes(args.count, 2024 + rank)
+    algs = {}
+
+    def alg(name):
+        if name == "classical":
+            return None
+        if name not in algs:
+            algs[name] = fmm.new_fmm(tune.COEFF_DIR / f"{name}.txt")
+        return algs[name]
+
+    g = torch.Generator(device=dev).manual_seed(77 + rank)
+    ops = [(serve._colmajor_rand(torch, m, k, g, dev), serve._colmajor_rand(torch, k, n, g, dev),
+            serve._colmajor_rand(torch, m, n, g, dev)) for m, n, k in shapes]
+    flops = sum(2.0 * m * n * k for m, n, k in shapes)
+    stream = torch.cuda.current_stream()
+    results = {}
+    for form in ("split", "fp64"):
+        plans = [tuner.plan(m, n, k, form, args.target) for m, n, k in shapes]
+        probs = [{"A": A, "B": B, "C": C, "fmm": alg(p.alg), "levels": p.levels, "slices": p.slices}
+                 for (A, B, C), p in zip(ops, plans)]
+        arr = fmm.make_batch(probs)
+        need = fmm.batch_workspace_size(arr)
+        free = torch.cuda.mem_get_info(dev)[0]
+        ws_bytes = int(min(need, max(free - (8 << 30), 1 << 30)))
+        ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
+        steps, warm = (args.steps, args.warmup) if form == "split" else (1, 1)
+        for _ in range(warm):
+            fmm.batch_dgemm(arr, workspace=ws, stream=stream)
+        torch.cuda.synchronize()
+        barrier()
+        n0 = fmm.launch_count()
+        fmm.read_kernel_timing()
+        fmm.set_kernel_timing(form == "split")
+        with Clocks(torch.cuda.current_device()) as clk:
+            total = timed_steps(torch, stream, steps, lambda: fmm.batch_dgemm(arr, workspace=ws, stream=stream),
+                                None)
+            barrier()
+        fmm.set_kernel_timing(False)
+        ms = max_over_ranks(total / steps)
+        gemm_ms, gemm_n, _ = fmm.read_kernel_timing()
+        hist = {}
+        for p in plans:
+            key = f"{p.alg}x{p.levels}" + (f"/s{p.slices}" if p.slices else "")
+            hist[key] = hist.get(key, 0) + 1
+        results[form] = {"ms": ms, "tflops": world * flops / (ms / 1e3) / 1e12, "steps": steps,
+                         "launches_per_step": (fmm.launch_count() - n0) / steps, "plans": hist,
+                         "workspace_gib": ws_bytes / 2**30, "workspace_needed_gib": need / 2**30,
+                         "gemm_kernel_ms_per_step": gemm_ms / steps if gemm_n else None,
+                         "clocks": clk.summary()}
+        del ws
+        # accuracy of the split run against the FP64 classical result, on a sample
+    errs = []
+    for i in range(0, len(shapes), max(len(shapes) // 16, 1)):
+        m, n, k = shapes[i]
+        A, B, _ = ops[i]
+        p = tuner.plan(m, n, k, "split", args.target)
+        C1 = torch.zeros((n, m), dtype=torch.float64, device=dev).t()
+        C2 = torch.zeros((n, m), dtype=torch.float64, device=dev).t()
+        fmm.split_dgemm(A, B, C1, alg(p.alg), p.levels, p.slices)
+        fmm.dgemm(A, B, C2, None, 0)
+        torch.cuda.synchronize()
+        errs.append(float((C1 - C2).abs().max() / C2.abs().max()))
+    for f in algs.values():
+        fmm.free_fmm(f)
+    assert fmm.take_device_error() == 0
+    if rank == 0:
+        sp = results["split"]
+        print(json.dumps({
+            "metric": METRIC, "value": sp["tflops"], "unit": "TFLOP/s", "n_gpus": world, "steps": sp["steps"],
+            "warmup": args.warmup, "ms_per_step": sp["ms"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+            "config": {"workload": f"batched uneven FMM: {args.count} GEMMs, m,n,k log-uniform [256, 8192], "
+                                   f"split-BF16 at target relative error {args.target:g}, tuner plans",
+                       "count": args.count, "total_gflop": flops / 1e9,
+                       "l2": "operands of 512 problems (tens of GB) larger than L2; no flush",
+                       "parallelism": f"replicas x{world}"},
+            "split_batch": sp, "fp64_batch": results["fp64"],
+            "split_max_rel_err_sample": max(errs), "gpu_launches": sp["launches_per_step"] * sp["steps"],
+            "clocks": sp["clocks"]}))
+
+
+def run_serve(args, fmm, dev, world, rank, barrier, max_over_ranks):
+    """Served GEMM stream: Poisson arrivals at --rate per second for
+    --duration seconds, m, n, k log-uniform in [128, 16384] (scaled down to fit
+    HBM), each tagged split-BF16 at --target (share --split-fraction) or FP64
+    drop-in, served by the continuous-batching Server with HBM admission.
+    Latency = completion - arrival; throughput = completed 2mnk over the
+    window. Requests still running at the end of the drain are counted."""
+    import torch
+
+    from fmm_blis_gb300 import serve
+
+    free, total = torch.cuda.mem_get_info(dev)
+    srv = serve.Server(hbm_budget=int(free * 0.75), streams=4, max_batch=64, keep_results=False)
+    reqs = serve.poisson_arrivals(args.rate, args.duration, seed=31 + rank, split_fraction=args.split_fraction,
+                                  target_rel_err=args.target, cap_bytes=int(free * 0.1))
+    # warm-up: one request of each form and a small graph bucket
+    srv.run([serve.Request(1024, 1024, 1024, "split", args.target, 1, 0.0),
+             serve.Request(256, 256, 256, "split", args.target, 2, 0.0),
+             serve.Request(1024, 1024, 1024, "fp64", args.target, 3, 0.0)])
+    srv.completed.clear()
+    barrier()
+    with Clocks(torch.cuda.current_device()) as clk:
+        t0 = time.perf_counter()
+        srv.run(reqs, until_idle=True, max_s=args.duration * 2)
+        t_end = time.perf_counter()
+    done = [r for r in reqs if r.done is not None]
+    lat = sorted(r.latency * 1e3 for r in done)
+    # requests not finished by the end count with their elapsed time (a lower bound)
+    open_lat = sorted((t_end - r.arrival) * 1e3 for r in reqs if r.done is None and r.rid >= 0)
+    lat_all = sorted(lat + open_lat)
+    window = max(t_end - t0, 1e-9)
+    flops_done = sum(r.flops for r in done if r.done <= t0 + args.duration)
+    pct = lambda xs, q: xs[min(len(xs) - 1, int(q * len(xs)))] if xs else None
+    by_form = {}
+    for form in ("split", "fp64"):
+        ls = sorted(r.latency * 1e3 for r in done if r.form == form)
+        by_form[form] = {"completed": len(ls), "p50_ms": pct(ls, 0.50), "p99_ms": pct(ls, 0.99)}
+    value = world * flops_done / args.duration / 1e12
+    srv.close()
+    if rank == 0:
+        print(json.dumps({
+            "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": 1, "warmup": 1,
+            "ms_per_step": window * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16+f64", "data": "synthetic",
+            "config": {"workload": f"served GEMM stream: Poisson {args.rate:g}/s for {args.duration:g} s, "
+                                   f"m,n,k log-uniform [128, 16384], {args.split_fraction:.0%} split-BF16 at "
+                                   f"{args.target:g}, the rest FP64 drop-in",
+                       "rate_per_s": args.rate, "duration_s": args.duration, "hbm_budget_gib": srv.budget / 2**30,
+                       "l2": "operands resident per request; no flush", "parallelism": f"replicas x{world}"},
+            "submitted": sum(1 for r in reqs if r.rid >= 0), "arrivals": len(reqs), "completed": len(done),
+            "unfinished": len(open_lat), "p50_ms": pct(lat_all, 0.50), "p99_ms": pct(lat_all, 0.99),
+            "p50_ms_completed": pct(lat, 0.50), "p99_ms_completed": pct(lat, 0.99), "by_form": by_form,
+            "graph_path_requests": sum(1 for r in done if r.path == "graph"), "batches": srv.launched_batches,
+            "peak_hbm_gib": srv.peak_used / 2**30, "wall_s": window, "clocks": clk.summary()}))
+
+
 def run_fp64(args, fmm, f, dev, world, rank, barrier, max_over_ranks):
     """The plain FP64 FMM drop-in as the timed step (one kernel launch per
     step, C := C + A*B); the classical FP64 GEMM of this library at the same
@@ -331,6 +498,18 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
 
+    if args.workload == "batch":
+        run_batch(args, fmm, dev, world, rank, barrier, max_over_ranks)
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return
+    if args.workload == "serve":
+        run_serve(args, fmm, dev, world, rank, barrier, max_over_ranks)
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return
     if args.form == "fp64":
         run_fp64(args, fmm, f, dev, world, rank, barrier, max_over_ranks)
         if world > 1:

@@ -313,6 +313,22 @@ def batch_workspace_size(batch) -> int:
     return int(lib().fmm_gpu_batch_workspace_size(count, arr))
 
 
+def batch_problem_workspace_size(m: int, n: int, k: int, fmm: FmmT | None, levels: int, slices: int) -> int:
+    """Workspace one problem of this shape needs inside a batch (all of its
+    products at once), from the shape alone: the sizing call reads no operand
+    data, so placeholder addresses stand in for the operands."""
+    arr = (BatchProblem * 1)()
+    arr[0].fmm = ctypes.cast(ctypes.pointer(fmm), ctypes.c_void_p) if fmm is not None else None
+    arr[0].levels = levels if fmm is not None else 0
+    arr[0].slices = slices
+    arr[0].m, arr[0].n, arr[0].k = m, n, k
+    arr[0].alpha, arr[0].beta = 1.0, 1.0
+    arr[0].A, arr[0].lda = 256, max(m, 1)
+    arr[0].B, arr[0].ldb = 256, max(k, 1)
+    arr[0].C, arr[0].ldc = 256, max(m, 1)
+    return int(lib().fmm_gpu_batch_workspace_size(1, arr))
+
+
 def batch_dgemm(problems, workspace=None, stream=None) -> None:
     """Runs independent GEMMs as one batch (see fmm_gpu_batch_dgemm)."""
     import torch

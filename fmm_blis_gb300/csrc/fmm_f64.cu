@@ -26,6 +26,8 @@
 #include "fmm_internal.h"
 
 #include <algorithm>
+#include <cstring>
+#include <vector>
 
 namespace {
 
@@ -77,22 +79,23 @@ __device__ void stage_entries(const int* __restrict__ ent, int beg, int end, int
     }
 }
 
+/* One output tile position (ti, tj) of the ceil(m/m~) x ceil(n/n~) product
+ * grid: every product r of the algorithm over it, with the fused packs, the
+ * DFMA micro-kernel and the multi-C epilogue. Shared by the single-problem
+ * kernel (one CTA per tile position) and the batched one (a work queue of
+ * (problem, tile position) items). */
 template <int BM, int BN, int BK, int TM, int TN>
-__global__ void __launch_bounds__((BM / TM) * (BN / TN))
-fmm_f64_kernel(const int* __restrict__ tab, int64_t m, int64_t n, int64_t k,
-               double alpha, const double* __restrict__ A, int64_t lda,
-               const double* __restrict__ B, int64_t ldb,
-               double* __restrict__ C, int64_t ldc, int tiles_m)
+__device__ __forceinline__ void f64_tile(const int* __restrict__ tab, int64_t m, int64_t n, int64_t k,
+                                         double alpha, const double* __restrict__ A, int64_t lda,
+                                         const double* __restrict__ B, int64_t ldb,
+                                         double* __restrict__ C, int64_t ldc, int ti, int tj,
+                                         double (&As)[BK][BM + 1], double (&Bs)[BK][BN + 1],
+                                         Entry* ue, Entry* ve)
 {
     constexpr int NT = (BM / TM) * (BN / TN);
     constexpr int RT = BM / TM;  /* thread rows */
     constexpr int CT = BN / TN;  /* thread cols */
     static_assert(NT % BM == 0 && NT % BK == 0, "tile/thread mapping");
-
-    __shared__ double As[BK][BM + 1];
-    __shared__ double Bs[BK][BN + 1];
-    __shared__ Entry ue[kMaxEntries];
-    __shared__ Entry ve[kMaxEntries];
 
     const int mt = tab[0], kt = tab[1], nt = tab[2], R = tab[3];
     const int* u_off = tab + FMM_ALG_HDR;
@@ -104,7 +107,6 @@ fmm_f64_kernel(const int* __restrict__ tab, int64_t m, int64_t n, int64_t k,
     const int* w_ent = v_ent + 2 * v_off[R];
 
     const int64_t me = (m + mt - 1) / mt, ne = (n + nt - 1) / nt, ke = (k + kt - 1) / kt;
-    const int ti = blockIdx.x % tiles_m, tj = blockIdx.x / tiles_m;
     const int64_t i0 = (int64_t)ti * BM, j0 = (int64_t)tj * BN;
     const int tid = threadIdx.x;
     const int tr = tid % RT, tc = tid / RT;
@@ -229,6 +231,112 @@ fmm_f64_kernel(const int* __restrict__ tab, int64_t m, int64_t n, int64_t k,
     (void)me; (void)ne;
 }
 
+template <int BM, int BN, int BK, int TM, int TN>
+__global__ void __launch_bounds__((BM / TM) * (BN / TN))
+fmm_f64_kernel(const int* __restrict__ tab, int64_t m, int64_t n, int64_t k,
+               double alpha, const double* __restrict__ A, int64_t lda,
+               const double* __restrict__ B, int64_t ldb,
+               double* __restrict__ C, int64_t ldc, int tiles_m)
+{
+    __shared__ double As[BK][BM + 1];
+    __shared__ double Bs[BK][BN + 1];
+    __shared__ Entry ue[kMaxEntries];
+    __shared__ Entry ve[kMaxEntries];
+    f64_tile<BM, BN, BK, TM, TN>(tab, m, n, k, alpha, A, lda, B, ldb, C, ldc, (int)(blockIdx.x % tiles_m),
+                                 (int)(blockIdx.x / tiles_m), As, Bs, ue, ve);
+}
+
+/* ------------------------------------------------------------ batched -- */
+
+/* One problem of a batched FP64 launch; problems are laid out in the order
+ * their work items are handed out (item_begin increasing). */
+struct F64Prob {
+    const int* tab;
+    int64_t m, n, k;
+    double alpha, beta;
+    const double* A;
+    int64_t lda;
+    const double* B;
+    int64_t ldb;
+    double* C;
+    int64_t ldc;
+    int64_t item_begin;   /* first (tile position) item of this problem */
+    int tiles_m, tiles_n;
+};
+
+constexpr int kF64Bm = 64, kF64Bn = 64, kF64Bk = 32, kF64Tm = 4, kF64Tn = 4;
+constexpr int kF64TableChunk = 256;   /* problems per table-writer launch (parameter space) */
+
+struct F64TableChunk {
+    F64Prob* dst;
+    int count;
+    F64Prob p[kF64TableChunk];
+};
+
+/* copies a chunk of the problem table (passed by value, so a captured graph
+ * holds it) into device memory */
+__global__ void f64_table_write(const __grid_constant__ F64TableChunk c)
+{
+    for (int i = threadIdx.x; i < c.count; i += blockDim.x) c.dst[i] = c.p[i];
+}
+
+/* Batched FP64 FMM GEMM: one persistent launch over all (problem, tile
+ * position) items of a batch. A CTA takes the next item from an atomic
+ * counter (problems sorted by per-item work, largest first, so the long
+ * items go out first), applies beta to the C elements its threads own in
+ * every sub-block of that tile position, then runs the tile exactly as the
+ * single-problem kernel does, so each result is identical to the problem
+ * issued alone. */
+__global__ void __launch_bounds__((kF64Bm / kF64Tm) * (kF64Bn / kF64Tn))
+fmm_f64_batch_kernel(const F64Prob* __restrict__ probs, int nprob, int64_t nitems,
+                     unsigned long long* __restrict__ counter)
+{
+    constexpr int RT = kF64Bm / kF64Tm, CT = kF64Bn / kF64Tn;
+    __shared__ double As[kF64Bk][kF64Bm + 1];
+    __shared__ double Bs[kF64Bk][kF64Bn + 1];
+    __shared__ Entry ue[kMaxEntries];
+    __shared__ Entry ve[kMaxEntries];
+    __shared__ long long next;
+    const int tid = threadIdx.x, tr = tid % RT, tc = tid / RT;
+    for (;;) {
+        __syncthreads();   /* the previous item is done with next, ue and ve */
+        if (tid == 0) next = (long long)atomicAdd(counter, 1ull);
+        __syncthreads();
+        const int64_t b = next;
+        if (b >= nitems) break;
+        int lo = 0, hi = nprob - 1;        /* last problem with item_begin <= b */
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) / 2;
+            if (probs[mid].item_begin <= b) lo = mid; else hi = mid - 1;
+        }
+        const F64Prob P = probs[lo];
+        const int64_t local = b - P.item_begin;
+        const int ti = (int)(local % P.tiles_m), tj = (int)(local / P.tiles_m);
+        const int mt = P.tab[0], nt = P.tab[2];
+        if (P.beta != 1.0) {
+            for (int part = 0; part < mt * nt; ++part) {
+                int64_t ro, rl, co, cl;
+                fmm_part_geom(P.m, mt, part / nt, &ro, &rl);
+                fmm_part_geom(P.n, nt, part % nt, &co, &cl);
+                for (int y = 0; y < kF64Tn; ++y) {
+                    const int64_t gj = (int64_t)tj * kF64Bn + tc + y * CT;
+                    if (gj >= cl) continue;
+                    for (int x = 0; x < kF64Tm; ++x) {
+                        const int64_t gi = (int64_t)ti * kF64Bm + tr + x * RT;
+                        if (gi < rl) {
+                            double* q = P.C + ro + gi + (co + gj) * P.ldc;
+                            *q = P.beta == 0.0 ? 0.0 : P.beta * *q;
+                        }
+                    }
+                }
+            }
+        }
+        if (P.k == 0 || P.alpha == 0.0) continue;
+        f64_tile<kF64Bm, kF64Bn, kF64Bk, kF64Tm, kF64Tn>(P.tab, P.m, P.n, P.k, P.alpha, P.A, P.lda, P.B, P.ldb,
+                                                        P.C, P.ldc, ti, tj, As, Bs, ue, ve);
+    }
+}
+
 __global__ void scale_c_kernel(int64_t m, int64_t n, double beta, double* C, int64_t ldc)
 {
     const int64_t total = m * n;
@@ -306,4 +414,69 @@ int fmm_f64_launch(const AlgView& alg, int64_t m, int64_t n, int64_t k, double a
     case 5: return launch_cfg<64, 128, 16, 4, 8>(alg, m, n, k, alpha, A, lda, B, ldb, C, ldc, st);
     default: return launch_cfg<32, 32, 32, 2, 2>(alg, m, n, k, alpha, A, lda, B, ldb, C, ldc, st);
     }
+}
+
+/* Workspace of a batched FP64 launch: the work counter and the problem table. */
+size_t fmm_f64_batch_ws_bytes(int count)
+{
+    return 256 + ((size_t)std::max(count, 0) * sizeof(F64Prob) + 255) / 256 * 256;
+}
+
+/* All problems of a batch in one persistent launch (plus the table-writer
+ * launches and a counter reset). Problems are ordered by the FP64 work of one
+ * of their items, largest first. Each result is identical to the problem
+ * issued alone through fmm_f64_launch: every tile shape accumulates the
+ * packed sums, the k loop and the products in the same order. */
+int fmm_f64_batch_launch(int count, const F64BatchItem* items, void* ws, size_t ws_bytes, cudaStream_t st)
+{
+    if (count <= 0) return FMM_OK;
+    if (ws == nullptr || ws_bytes < fmm_f64_batch_ws_bytes(count)) return FMM_ERR_WORKSPACE;
+    if (((uintptr_t)ws & 255) != 0) return FMM_ERR_ARG;
+    std::vector<int> order;
+    std::vector<double> cost(count, 0.0);
+    for (int i = 0; i < count; ++i) {
+        const F64BatchItem& it = items[i];
+        if (it.alg.max_nnz_u > kMaxEntries || it.alg.max_nnz_v > kMaxEntries) return FMM_ERR_UNSUPPORTED;
+        if (it.m == 0 || it.n == 0) continue;   /* nothing to do at all */
+        const int64_t ke = (it.k + it.alg.kt - 1) / it.alg.kt;
+        cost[i] = (it.k == 0 || it.alpha == 0.0) ? 1.0 : (double)it.alg.R * (double)(ke + 1);
+        order.push_back(i);
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+    std::vector<F64Prob> tab(order.size());
+    int64_t items_total = 0;
+    for (size_t q = 0; q < order.size(); ++q) {
+        const F64BatchItem& it = items[order[q]];
+        F64Prob& P = tab[q];
+        P.tab = it.alg.tab;
+        P.m = it.m; P.n = it.n; P.k = it.k;
+        P.alpha = it.alpha; P.beta = it.beta;
+        P.A = it.A; P.lda = it.lda; P.B = it.B; P.ldb = it.ldb; P.C = it.C; P.ldc = it.ldc;
+        const int64_t me = (it.m + it.alg.mt - 1) / it.alg.mt, ne = (it.n + it.alg.nt - 1) / it.alg.nt;
+        const int64_t tm = (me + kF64Bm - 1) / kF64Bm, tn = (ne + kF64Bn - 1) / kF64Bn;
+        if (tm > 0x7fffffffLL || tn > 0x7fffffffLL) return FMM_ERR_UNSUPPORTED;
+        P.tiles_m = (int)tm; P.tiles_n = (int)tn;
+        P.item_begin = items_total;
+        items_total += tm * tn;
+    }
+    if (tab.empty()) return FMM_OK;
+    unsigned long long* counter = (unsigned long long*)ws;
+    F64Prob* dtab = (F64Prob*)((uint8_t*)ws + 256);
+    if (cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st) != cudaSuccess) return FMM_ERR_CUDA;
+    for (size_t c0 = 0; c0 < tab.size(); c0 += kF64TableChunk) {
+        F64TableChunk ch;
+        ch.dst = dtab + c0;
+        ch.count = (int)std::min<size_t>(kF64TableChunk, tab.size() - c0);
+        memcpy(ch.p, tab.data() + c0, sizeof(F64Prob) * (size_t)ch.count);
+        f64_table_write<<<1, 128, 0, st>>>(ch);
+        fmm_count_launch(1);
+    }
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t grid = std::min<int64_t>(items_total, 2 * (int64_t)sms);
+    fmm_f64_batch_kernel<<<(unsigned)grid, (kF64Bm / kF64Tm) * (kF64Bn / kF64Tn), 0, st>>>(
+        dtab, (int)tab.size(), items_total, counter);
+    fmm_count_launch(1);
+    return cudaGetLastError() == cudaSuccess ? FMM_OK : FMM_ERR_CUDA;
 }

@@ -69,6 +69,22 @@ int fmm_f64_launch(const AlgView& alg, int64_t m, int64_t n, int64_t k,
                    const double* B, int64_t ldb, double beta, double* C, int64_t ldc,
                    cudaStream_t st);
 
+/* batched FP64 form (fmm_f64.cu): one persistent launch over every
+ * (problem, tile position) item */
+struct F64BatchItem {
+    AlgView alg;
+    int64_t m, n, k;
+    double alpha, beta;
+    const double* A;
+    int64_t lda;
+    const double* B;
+    int64_t ldb;
+    double* C;
+    int64_t ldc;
+};
+size_t fmm_f64_batch_ws_bytes(int count);
+int fmm_f64_batch_launch(int count, const F64BatchItem* items, void* ws, size_t ws_bytes, cudaStream_t st);
+
 /* split form (fmm_split.cu) */
 size_t fmm_split_ws_bytes(const AlgView& alg, int64_t m, int64_t n, int64_t k, int slices);
 int fmm_split_launch(const AlgView& alg, int64_t m, int64_t n, int64_t k,

@@ -52,6 +52,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <deque>
 #include <mutex>
 #include <utility>
 #include <vector>
@@ -557,7 +558,10 @@ struct GemmProblem {
     int item_begin;       /* first work item of this problem in the launch */
 };
 
-constexpr int kMaxLaunchProblems = 32;
+/* problems per GEMM launch: the table travels as a kernel parameter, whose
+ * space is 32764 bytes (a GemmProblem is 384 bytes with its two 128-byte
+ * aligned tensor maps) */
+constexpr int kMaxLaunchProblems = 80;
 
 /* Everything a launch needs, passed by value (tensor maps included), so a
  * launch copies nothing to the device and can be captured in a graph. */
@@ -567,6 +571,7 @@ struct GemmLaunch {
     int* err;
     GemmProblem prob[kMaxLaunchProblems];
 };
+static_assert(sizeof(GemmLaunch) <= 32764, "GemmLaunch must fit the kernel parameter space");
 
 __device__ __forceinline__ int level_pairs(int g, int s) { return min(s, g - 1) - max(1, g - s) + 1; }
 
@@ -579,8 +584,11 @@ struct Item {
 
 __device__ __forceinline__ Item decode_item(const GemmLaunch& L, int b)
 {
-    int p = 0;
-    while (p + 1 < L.nprob && L.prob[p + 1].item_begin <= b) ++p;
+    int p = 0, hi = L.nprob - 1;        /* last problem with item_begin <= b */
+    while (p < hi) {
+        const int mid = (p + hi + 1) / 2;
+        if (L.prob[mid].item_begin <= b) p = mid; else hi = mid - 1;
+    }
     const GemmProblem& P = L.prob[p];
     const int local = b - P.item_begin;
     const int per_prod = P.tiles_m * P.tiles_n;
@@ -1407,7 +1415,17 @@ int fmm_split_batch(int count, const SplitJob* jobs_in, void* ws, size_t ws_byte
             off += (full[q] + 255) / 256 * 256;
             if ((rc = job_prologue(j, st)) != FMM_OK) return rc;
             if ((rc = job_pack(j, 0, j.alg.R, st)) != FMM_OK) return rc;
-            if ((rc = job_fill(j, gl.prob[q - i], j.alg.R, (int)items)) != FMM_OK) return rc;
+        }
+        /* work items of the costliest problems (slice pairs x k blocks per
+         * item) first, so the CTAs' round-robin shares end evenly */
+        std::vector<int> ord;
+        for (int q = i; q < e; ++q) ord.push_back(q);
+        auto item_cost = [&](int q) { return (int64_t)jobs[q].s * (jobs[q].s + 1) / 2 * (jobs[q].d.k_pad / kBK); };
+        std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return item_cost(a) > item_cost(b); });
+        for (size_t x = 0; x < ord.size(); ++x) {
+            SplitJob& j = jobs[ord[x]];
+            int rc = job_fill(j, gl.prob[x], j.alg.R, (int)items);
+            if (rc != FMM_OK) return rc;
             items += job_items(j, j.alg.R);
             prods += j.alg.R;
         }
@@ -1531,8 +1549,12 @@ extern "C" int fmm_gpu_split_dgemm_noalloc(const fmm_t* fmm, int levels, int64_t
  * ------------------------------------------------------------------------- */
 namespace {
 
+/* Validates a batch and describes its problems. With `host_tables` (sizing
+ * only) the algorithm tables are built on the host and kept in it, so sizing
+ * needs no device; otherwise they are the cached device tables. */
 int batch_jobs(int count, const fmm_batch_problem* probs, std::vector<SplitJob>& jobs,
-               std::vector<int>& f64_idx, std::vector<AlgView>& f64_alg)
+               std::vector<int>& f64_idx, std::vector<AlgView>& f64_alg,
+               std::deque<std::vector<int>>* host_tables = nullptr)
 {
     if (count < 0 || (count > 0 && probs == nullptr)) return FMM_ERR_ARG;
     for (int i = 0; i < count; ++i) {
@@ -1548,7 +1570,12 @@ int batch_jobs(int count, const fmm_batch_problem* probs, std::vector<SplitJob>&
         int rc = fmm_flatten(p.fmm, p.fmm ? p.levels : 0, &flat, &owned);
         if (rc != FMM_OK) return rc;
         AlgView alg;
-        rc = fmm_alg_get(&flat, &alg);
+        if (host_tables) {
+            host_tables->emplace_back();
+            rc = fmm_alg_describe(&flat, &host_tables->back(), &alg);
+        } else {
+            rc = fmm_alg_get(&flat, &alg);
+        }
         if (owned) free_fmm(flat);
         if (rc != FMM_OK) return rc;
         if (p.slices == 0) {
@@ -1566,14 +1593,18 @@ int batch_jobs(int count, const fmm_batch_problem* probs, std::vector<SplitJob>&
 
 }  // namespace
 
+/* Batch workspace: the FP64 problems' table, then the split problems' region. */
+static size_t batch_f64_bytes(size_t nf64) { return nf64 ? fmm_f64_batch_ws_bytes((int)nf64) : 0; }
+
 extern "C" size_t fmm_gpu_batch_workspace_size(int count, const fmm_batch_problem* probs)
 {
     std::vector<SplitJob> jobs;
     std::vector<int> fi;
     std::vector<AlgView> fa;
-    if (batch_jobs(count, probs, jobs, fi, fa) != FMM_OK) return 0;
-    if (jobs.empty()) return 256;
-    return fmm_split_batch_ws((int)jobs.size(), jobs.data());
+    std::deque<std::vector<int>> tables;
+    if (batch_jobs(count, probs, jobs, fi, fa, &tables) != FMM_OK) return 0;
+    const size_t split = jobs.empty() ? 0 : fmm_split_batch_ws((int)jobs.size(), jobs.data());
+    return std::max<size_t>(256, batch_f64_bytes(fi.size()) + split);
 }
 
 extern "C" int fmm_gpu_batch_dgemm(int count, const fmm_batch_problem* probs, void* workspace,
@@ -1586,10 +1617,21 @@ extern "C" int fmm_gpu_batch_dgemm(int count, const fmm_batch_problem* probs, vo
     if (rc != FMM_OK) return rc;
     if (fmm_device_error_word() == nullptr) return FMM_ERR_CUDA;
     cudaStream_t st = (cudaStream_t)stream;
-    for (size_t q = 0; q < fi.size(); ++q) {
-        const fmm_batch_problem& p = probs[fi[q]];
-        rc = fmm_f64_launch(fa[q], p.m, p.n, p.k, p.alpha, p.A, p.lda, p.B, p.ldb, p.beta, p.C, p.ldc, st);
+    const size_t f64_bytes = batch_f64_bytes(fi.size());
+    if (!fi.empty()) {
+        /* all FP64 problems in one persistent launch */
+        std::vector<F64BatchItem> items(fi.size());
+        for (size_t q = 0; q < fi.size(); ++q) {
+            const fmm_batch_problem& p = probs[fi[q]];
+            items[q] = F64BatchItem{fa[q], p.m, p.n, p.k, p.alpha, p.beta, p.A, p.lda, p.B, p.ldb, p.C, p.ldc};
+        }
+        rc = fmm_f64_batch_launch((int)items.size(), items.data(), workspace, workspace_bytes, st);
         if (rc != FMM_OK) return rc;
+    }
+    if (!jobs.empty()) {
+        if (workspace_bytes < f64_bytes) return FMM_ERR_WORKSPACE;
+        workspace = workspace ? (void*)((uint8_t*)workspace + f64_bytes) : nullptr;
+        workspace_bytes -= f64_bytes;
     }
     if (jobs.empty()) return FMM_OK;
     return fmm_split_batch((int)jobs.size(), jobs.data(), workspace, workspace_bytes, st);

@@ -1,0 +1,324 @@
+"""Serving loop for GEMM requests on one GPU: continuous batching with
+admission by HBM footprint, batched launches that overlap on a pool of
+streams, and per-size-bucket CUDA graphs for small requests.
+
+The reference has no serving layer (its only caller is one synchronous
+bli_strassen_ab_ex call, test/test_strassen_oapi.c:166); this is the served
+form of the same FMM GEMM built on the library's batched C-ABI call
+(fmm_gpu_batch_dgemm) and the per-problem Tuner.
+
+Loop (Server.tick):
+  1. completions: a batch whose event has fired releases its requests'
+     device memory (operands stay on the device until the request is done)
+     and their footprint;
+  2. admission: waiting requests, first come first served, are admitted while
+     their footprint -- A, B, C and the FMM workspace of their plan -- fits the
+     HBM budget; a request that does not fit blocks the ones behind it (no
+     overtaking, so large requests are not starved);
+  3. launch: the requests admitted in this tick run as one batch (one
+     persistent launch for the FP64 problems, waves of persistent launches for
+     the split ones) on the next stream of the pool, so the batches of
+     successive ticks overlap on the device while earlier ones run.
+
+A request's result depends only on the request: its plan comes from the
+deterministic Tuner and the batched call gives every problem exactly its
+single-call result, so a request served in a mix returns the bits it returns
+alone.
+
+Small split requests whose plan is classical (levels 0) and whose dimensions
+fit a size bucket (powers of two from 128 to graph_max_dim) run through CUDA
+graphs captured once per bucket: the operands are written into a zero-padded
+slot of the bucket's size and one graph launch replaces the prologue, pack,
+GEMM and scatter launches. Zero padding leaves a levels-0 split result
+unchanged (row and column maxima, digits and the exact integer slice products
+of the real rows and columns are the same), so the graph path returns the
+same bits as the batched path.
+"""
+from __future__ import annotations
+
+import collections
+import itertools
+import time
+from dataclasses import dataclass, field
+
+from . import tune as _tune
+
+
+@dataclass
+class Request:
+    m: int
+    n: int
+    k: int
+    form: str = "split"               # "split" (target_rel_err) or "fp64" (drop-in)
+    target_rel_err: float = 1e-10
+    seed: int = 0
+    arrival: float = 0.0              # perf_counter seconds
+    rid: int = -1
+    plan: object = None
+    admitted: float | None = None
+    done: float | None = None
+    path: str = ""                    # "batch" or "graph"
+    C: object = None                  # result (device tensor, column-major), kept after completion
+    footprint: int = 0
+    _A: object = field(default=None, repr=False)
+    _B: object = field(default=None, repr=False)
+
+    @property
+    def latency(self) -> float | None:
+        return None if self.done is None else self.done - self.arrival
+
+    @property
+    def flops(self) -> float:
+        return 2.0 * self.m * self.n * self.k
+
+
+def _colmajor_rand(torch, rows, cols, gen, dev):
+    """uniform [-1, 1) column-major (rows x cols) tensor from a seeded
+    generator (2u - 1 in place: no full-size temporaries)"""
+    return torch.rand((cols, rows), generator=gen, device=dev, dtype=torch.float64).mul_(2).sub_(1).t()
+
+
+def _bucket(x: int, lo: int = 128) -> int:
+    b = lo
+    while b < x:
+        b *= 2
+    return b
+
+
+class _GraphSlot:
+    """A zero-padded operand set of one bucket shape and the graph of one
+    levels-0 split call over it."""
+
+    def __init__(self, torch, fmm, dev, bm, bn, bk, slices, stream):
+        self.bm, self.bn, self.bk = bm, bn, bk
+        self.stream = stream
+        self.A = torch.zeros((bk, bm), dtype=torch.float64, device=dev).t()
+        self.B = torch.zeros((bn, bk), dtype=torch.float64, device=dev).t()
+        self.C = torch.zeros((bn, bm), dtype=torch.float64, device=dev).t()
+        self.ws = torch.empty(max(fmm.split_workspace_size(bm, bn, bk, None, 0, slices), 256),
+                              dtype=torch.uint8, device=dev)
+        self.busy_event = None
+        with torch.cuda.stream(stream):
+            # warm-up outside capture: tables, attributes, device error word
+            fmm.split_dgemm(self.A, self.B, self.C, None, 0, slices, workspace=self.ws, stream=stream)
+        torch.cuda.synchronize()
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph, stream=stream):
+            fmm.split_dgemm(self.A, self.B, self.C, None, 0, slices, workspace=self.ws,
+                            stream=torch.cuda.current_stream())
+        torch.cuda.synchronize()
+
+
+class Server:
+    def __init__(self, hbm_budget: int | None = None, streams: int = 4, tuner: _tune.Tuner | None = None,
+                 max_batch: int = 64, graph_max_dim: int = 1024, graph_slots: int = 2, use_graphs: bool = True,
+                 keep_results: bool = True, device: int = 0):
+        import torch
+
+        import fmm_blis_gb300 as fmm
+        self.torch, self.fmm = torch, fmm
+        self.dev = torch.device("cuda", device)
+        if hbm_budget is None:
+            free, _total = torch.cuda.mem_get_info(self.dev)
+            hbm_budget = int(free * 0.8)
+        self.budget = hbm_budget
+        self.used = 0
+        self.peak_used = 0
+        self.tuner = tuner or _tune.Tuner()
+        self.streams = [torch.cuda.Stream(device=self.dev) for _ in range(streams)]
+        self._next_stream = itertools.cycle(range(streams))
+        self.max_batch = max_batch
+        self.keep_results = keep_results
+        self.graph_max_dim = graph_max_dim if use_graphs else 0
+        self.graph_slots = graph_slots
+        self.pending: collections.deque[Request] = collections.deque()
+        self.inflight: list[tuple[object, list[Request], object]] = []   # (event, requests, workspace)
+        self.completed: list[Request] = []
+        self._algs: dict = {}
+        self._slots: dict = {}
+        self._rid = itertools.count()
+        self.launched_batches = 0
+
+    # ------------------------------------------------------------ helpers
+    def _alg(self, name: str):
+        if name == "classical":
+            return None
+        if name not in self._algs:
+            self._algs[name] = self.fmm.new_fmm(_tune.COEFF_DIR / f"{name}.txt")
+        return self._algs[name]
+
+    def _workspace_bytes(self, r: Request) -> int:
+        """FMM temporaries of the request's plan when it runs inside a batch:
+        all products' digit slices and level accumulators at once (split), or
+        its share of the FP64 problem table."""
+        p = r.plan
+        if p.form == "fp64":
+            return 4096
+        return self.fmm.batch_problem_workspace_size(r.m, r.n, r.k, self._alg(p.alg), p.levels, p.slices)
+
+    def _graph_bucket(self, r: Request):
+        p = r.plan
+        if p.form != "split" or p.levels != 0 or max(r.m, r.n, r.k) > self.graph_max_dim:
+            return None
+        return (_bucket(r.m), _bucket(r.n), _bucket(r.k), p.slices)
+
+    # -------------------------------------------------------------- API
+    def submit(self, r: Request) -> Request:
+        r.rid = next(self._rid)
+        if not r.arrival:
+            r.arrival = time.perf_counter()
+        r.plan = self.tuner.plan(r.m, r.n, r.k, r.form, r.target_rel_err)
+        r.footprint = 8 * (r.m * r.k + r.k * r.n + r.m * r.n) + self._workspace_bytes(r)
+        if r.footprint > self.budget:
+            raise ValueError(f"request {r.rid} needs {r.footprint} bytes, more than the HBM budget {self.budget}")
+        self.pending.append(r)
+        return r
+
+    def idle(self) -> bool:
+        return not self.pending and not self.inflight
+
+    def tick(self) -> int:
+        """One scheduling round; returns the number of requests launched."""
+        torch = self.torch
+        # 1. completions
+        still = []
+        now = time.perf_counter()
+        for ev, reqs, ws in self.inflight:
+            if ev.query():
+                for r in reqs:
+                    r.done = now
+                    r._A = r._B = None
+                    if not self.keep_results:
+                        r.C = None
+                    self.used -= r.footprint
+                    self.completed.append(r)
+            else:
+                still.append((ev, reqs, ws))
+        self.inflight = still
+        # 2. admission, first come first served
+        batch: list[Request] = []
+        while self.pending and len(batch) < self.max_batch:
+            r = self.pending[0]
+            if self.used + r.footprint > self.budget:
+                break
+            self.pending.popleft()
+            self.used += r.footprint
+            self.peak_used = max(self.peak_used, self.used)
+            r.admitted = time.perf_counter()
+            batch.append(r)
+        if not batch:
+            return 0
+        # 3. launch on the next stream of the pool
+        st = self.streams[next(self._next_stream)]
+        with torch.cuda.stream(st):
+            direct = []
+            for r in batch:
+                g = torch.Generator(device=self.dev).manual_seed(r.seed)
+                bucket = self._graph_bucket(r)
+                if bucket is not None:
+                    self._run_graph(r, bucket, g, st)
+                    continue
+                r._A = _colmajor_rand(torch, r.m, r.k, g, self.dev)
+                r._B = _colmajor_rand(torch, r.k, r.n, g, self.dev)
+                r.C = _colmajor_rand(torch, r.m, r.n, g, self.dev)
+                r.path = "batch"
+                direct.append(r)
+            ws = None
+            if direct:
+                probs = [{"A": r._A, "B": r._B, "C": r.C, "fmm": self._alg(r.plan.alg), "levels": r.plan.levels,
+                          "slices": r.plan.slices} for r in direct]
+                arr = self.fmm.make_batch(probs)
+                need = self.fmm.batch_workspace_size(arr)
+                ws = torch.empty(max(need, 256), dtype=torch.uint8, device=self.dev)
+                self.fmm.batch_dgemm(arr, workspace=ws, stream=st)
+            ev = torch.cuda.Event()
+            ev.record(st)
+        self.inflight.append((ev, batch, ws))
+        self.launched_batches += 1
+        return len(batch)
+
+    def _run_graph(self, r: Request, bucket, gen, st):
+        """operands into a zero-padded slot of the bucket, one graph launch,
+        the result copied out (all on stream st)"""
+        torch = self.torch
+        slots = self._slots.get(bucket)
+        if slots is None:
+            bm, bn, bk, s = bucket
+            slots = [_GraphSlot(torch, self.fmm, self.dev, bm, bn, bk, s, torch.cuda.Stream(device=self.dev))
+                     for _ in range(self.graph_slots)]
+            self._slots[bucket] = slots
+        slot = None
+        while slot is None:
+            for sl in slots:
+                if sl.busy_event is None or sl.busy_event.query():
+                    slot = sl
+                    break
+            if slot is None:
+                slots[0].busy_event.synchronize()
+        slot.stream.wait_stream(st)
+        with torch.cuda.stream(slot.stream):
+            slot.A.zero_()
+            slot.B.zero_()
+            slot.C.zero_()
+            slot.A[:r.m, :r.k].copy_(_colmajor_rand(torch, r.m, r.k, gen, self.dev))
+            slot.B[:r.k, :r.n].copy_(_colmajor_rand(torch, r.k, r.n, gen, self.dev))
+            C = _colmajor_rand(torch, r.m, r.n, gen, self.dev)
+            slot.C[:r.m, :r.n].copy_(C)
+            slot.graph.replay()
+            C.copy_(slot.C[:r.m, :r.n])
+            ev = torch.cuda.Event()
+            ev.record(slot.stream)
+        slot.busy_event = ev
+        st.wait_stream(slot.stream)
+        r.C = C
+        r.path = "graph"
+
+    def run(self, arrivals, until_idle: bool = True, poll_s: float = 50e-6, max_s: float | None = None):
+        """Serves `arrivals` (Requests with arrival offsets in seconds from
+        now, sorted): each is submitted when its time comes. Returns the
+        completed requests."""
+        t0 = time.perf_counter()
+        queue = collections.deque(sorted(arrivals, key=lambda r: r.arrival))
+        while queue or (until_idle and not self.idle()):
+            now = time.perf_counter()
+            if max_s is not None and now - t0 > max_s:
+                break
+            while queue and t0 + queue[0].arrival <= now:
+                r = queue.popleft()
+                r.arrival = t0 + r.arrival
+                self.submit(r)
+            launched = self.tick()
+            if not launched and (not queue or t0 + queue[0].arrival > time.perf_counter()):
+                time.sleep(poll_s)
+        return self.completed
+
+    def close(self):
+        self.torch.cuda.synchronize()
+        for f in self._algs.values():
+            self.fmm.free_fmm(f)
+        self._algs.clear()
+
+
+def poisson_arrivals(rate: float, duration: float, seed: int, dims=(128, 16384), split_fraction: float = 0.5,
+                     target_rel_err: float = 1e-10, cap_bytes: int | None = None):
+    """Seeded request stream: exponential inter-arrival times at `rate` per
+    second over `duration` seconds; m, n, k log-uniform in dims; each request
+    tagged split (target relative error) or FP64 drop-in. With cap_bytes, the
+    dimensions are scaled down until A, B and C fit in it."""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    out, t = [], 0.0
+    lo, hi = np.log(dims[0]), np.log(dims[1])
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t > duration:
+            break
+        m, n, k = (int(round(float(np.exp(rng.uniform(lo, hi))))) for _ in range(3))
+        if cap_bytes is not None:
+            while 8 * (m * k + k * n + m * n) > cap_bytes:
+                m, n, k = max(m // 2, 1), max(n // 2, 1), max(k // 2, 1)
+        form = "split" if rng.uniform() < split_fraction else "fp64"
+        out.append(Request(m, n, k, form=form, target_rel_err=target_rel_err,
+                           seed=int(rng.integers(0, 2**31 - 1)), arrival=t))
+    return out

@@ -1,0 +1,179 @@
+"""Per-problem plan choice for the FMM GEMM: form, algorithm, recursion depth,
+slice count.
+
+The reference fixes the algorithm (the coefficient file handed to
+bli_strassen_ab_ex, frame/base/bli_strassen_ab.c:123) and runs one recursion
+level; it has no tuner. For batched and served mixes of uneven shapes this
+module picks, per problem, among classical (levels 0) and the coefficient
+files at one or two levels, by a cost model of the GB300 kernels of this
+library, and, for the split form, the fewest BF16 slices whose predicted error
+meets the requested relative error.
+
+Cost model (calibrated on GB300 at m = n = k = 16384, SM clock 1.8-2.07 GHz):
+  FP64 form: a CTA per 64 x 64 tile position of the product grid runs all
+    R products over it, the CTAs of an SM share its FP64 pipe (2 FMA/clk):
+    time = ceil(tiles / SMs) * 2048 * k_e * R / clock / 0.98, times
+    1 + 1.5 ((nnz(U)-1) + (nnz(V)-1)) / 64 for the fused pack sums.
+    (16384^3: classical 7.03 s measured, 7.14 s modelled; 222 one level
+    6.40 / 6.45 s; 222 two levels 6.14 / 5.97 s.)
+  Split form: the persistent tcgen05 GEMM runs (problem, product, 128 x 256
+    tile) items on 152 CTAs, each item s(s+1)/2 slice pairs x k_pad/64 blocks
+    of 512 MMA clocks at about 61% of 2.07 GHz under the power cap
+    (222 two levels, 6 slices: 90-95 ms measured); the digit packs cost 1.16 ps
+    per element-slice and side, the multi-C scatter 2.44 ps per W entry and
+    element, the row/column maxima one read of A and B.
+
+Error model (split form, uniform-like inputs): the max-norm error relative to
+max|C| of s slices is about 0.4 * 2^-8s * sqrt(k) * 1.5^levels (222 two
+levels, 6 slices, k = 16384: 1.7e-13 measured). The tuner keeps a safety
+factor of 4 on it.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+from pathlib import Path
+
+COEFF_DIR = Path(__file__).resolve().parent.parent / "tests" / "golden" / "coeffs"
+
+SMS = 152
+CLOCK_HZ = 2.07e9
+FP64_EFF = 0.98
+SPLIT_EFF = 0.61
+PACK_S_PER_ELEM_SLICE = 1.16e-12
+SCATTER_S_PER_ENTRY_ELEM = 2.44e-12
+HBM_BPS = 6.0e12
+LAUNCH_S = 4e-6
+ERR_C0 = 0.4
+ERR_LEVEL_GROWTH = 1.5
+ERR_SAFETY = 4.0
+
+
+def _cdiv(a: int, b: int) -> int:
+    return -(-a // b)
+
+
+def _round_up(a: int, b: int) -> int:
+    return _cdiv(a, b) * b
+
+
+@dataclass(frozen=True)
+class AlgShape:
+    """What the cost model needs of a (flattened) algorithm."""
+
+    name: str            # coefficient file stem, "classical" for the plain GEMM
+    levels: int
+    mt: int
+    kt: int
+    nt: int
+    R: int
+    nnz_u: float         # average nonzeros per product column of U
+    nnz_v: float
+    nnz_w: int           # total nonzeros of W
+
+
+def alg_shapes(names=("222", "232", "322", "333", "444"), levels=(1, 2)) -> list[AlgShape]:
+    """Classical plus every coefficient file at the given recursion levels,
+    read with the library's own reader (new_fmm, the format of
+    frame/base/bli_read_fmm.c:24-86)."""
+    from . import free_fmm, new_fmm
+
+    out = [AlgShape("classical", 0, 1, 1, 1, 1, 1.0, 1.0, 1)]
+    for nm in names:
+        f = new_fmm(COEFF_DIR / f"{nm}.txt")
+        try:
+            U, V, W = f.coeffs()
+            mt, kt, nt, R = f.m_tilde, f.k_tilde, f.n_tilde, f.R
+        finally:
+            free_fmm(f)
+        nu = [sum(1 for row in U if row[r] != 0) for r in range(R)]
+        nv = [sum(1 for row in V if row[r] != 0) for r in range(R)]
+        nw = sum(1 for row in W for x in row if x != 0)
+        for L in levels:
+            out.append(AlgShape(nm, L, mt ** L, kt ** L, nt ** L, R ** L,
+                                (sum(nu) / R) ** L, (sum(nv) / R) ** L, nw ** L))
+    return out
+
+
+@dataclass
+class Plan:
+    form: str                  # "fp64" or "split"
+    alg: str                   # coefficient file stem or "classical"
+    levels: int
+    slices: int                # 0 for the FP64 form
+    est_s: float               # modelled device time
+    est_rel_err: float | None  # modelled max-norm error / max|C| (split form)
+    candidates: list = field(default_factory=list, repr=False)
+
+
+def fp64_time(a: AlgShape, m: int, n: int, k: int) -> float:
+    me, ne, ke = _cdiv(m, a.mt), _cdiv(n, a.nt), _cdiv(k, a.kt)
+    tiles = _cdiv(me, 64) * _cdiv(ne, 64)
+    per_sm = _cdiv(tiles, SMS)
+    pack = 1.0 + 1.5 * ((a.nnz_u - 1.0) + (a.nnz_v - 1.0)) / 64
+    return per_sm * 2048.0 * ke * a.R / CLOCK_HZ / FP64_EFF * pack + 2 * LAUNCH_S
+
+
+def split_time(a: AlgShape, m: int, n: int, k: int, s: int) -> float:
+    me, ne, ke = _cdiv(m, a.mt), _cdiv(n, a.nt), _cdiv(k, a.kt)
+    m_pad, n_pad, k_pad = _round_up(max(me, 1), 128), _round_up(max(ne, 1), 256), _round_up(max(ke, 1), 64)
+    items = a.R * (m_pad // 128) * (n_pad // 256)
+    waves = _cdiv(items, SMS)
+    pairs = s * (s + 1) // 2
+    gemm = waves * pairs * (k_pad // 64) * 512.0 / (CLOCK_HZ * SPLIT_EFF)
+    pack = a.R * (m_pad + n_pad) * k_pad * s * PACK_S_PER_ELEM_SLICE
+    scatter = a.nnz_w * me * ne * SCATTER_S_PER_ENTRY_ELEM
+    maxima = 8.0 * (m * k + k * n) / HBM_BPS
+    return gemm + pack + scatter + maxima + 7 * LAUNCH_S
+
+
+def split_rel_err(a: AlgShape, k: int, s: int) -> float:
+    return ERR_C0 * 2.0 ** (-8 * s) * math.sqrt(max(k, 1)) * ERR_LEVEL_GROWTH ** a.levels
+
+
+def _fits(a: AlgShape, m: int, n: int, k: int, min_block: int) -> bool:
+    """FMM levels only where every sub-block keeps a useful size."""
+    if a.levels == 0:
+        return True
+    return min(_cdiv(m, a.mt), _cdiv(n, a.nt), _cdiv(k, a.kt)) >= min_block
+
+
+class Tuner:
+    """Chooses a Plan per (m, n, k, form, target error). Deterministic: the
+    same request always gets the same plan, so a result served in a mix is the
+    one served alone."""
+
+    def __init__(self, algs: list[AlgShape] | None = None, min_block_fp64: int = 256,
+                 min_block_split: int = 1024, slice_range=(3, 8)):
+        self.algs = algs if algs is not None else alg_shapes()
+        self.min_block_fp64 = min_block_fp64
+        self.min_block_split = min_block_split
+        self.slice_range = slice_range
+        self.cache: dict = {}
+
+    def plan(self, m: int, n: int, k: int, form: str = "split", target_rel_err: float = 1e-10) -> Plan:
+        key = (m, n, k, form, target_rel_err)
+        if key in self.cache:
+            return self.cache[key]
+        cands = []
+        for a in self.algs:
+            if form == "fp64":
+                if not _fits(a, m, n, k, self.min_block_fp64):
+                    continue
+                cands.append(Plan("fp64", a.name, a.levels, 0, fp64_time(a, m, n, k), None))
+            else:
+                if not _fits(a, m, n, k, self.min_block_split):
+                    continue
+                for s in range(self.slice_range[0], self.slice_range[1] + 1):
+                    err = split_rel_err(a, k, s)
+                    if err * ERR_SAFETY <= target_rel_err:
+                        cands.append(Plan("split", a.name, a.levels, s, split_time(a, m, n, k, s), err))
+                        break
+        if not cands:
+            raise ValueError(f"no plan meets the target for m={m} n={n} k={k} form={form} "
+                             f"target={target_rel_err}")
+        cands.sort(key=lambda p: p.est_s)
+        best = cands[0]
+        best.candidates = cands
+        self.cache[key] = best
+        return best

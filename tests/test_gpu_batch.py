@@ -73,3 +73,58 @@ def test_batch_empty_and_degenerate(fmm, torch_cuda):
     fmm.batch_dgemm([p])
     torch.cuda.synchronize()
     assert np.array_equal(to_host(p["C"]), 3.0 * C0)
+
+
+def test_batch_all_fp64_one_launch(fmm, torch_cuda):
+    """Plain FP64 problems of a batch run in one persistent launch (a work
+    queue over (problem, tile position) items) and match their single calls
+    bit for bit, including the degenerate ones (k = 0, alpha = 0, beta = 0)."""
+    import torch
+    rng = np.random.default_rng(11)
+    algs = {a: fmm.new_fmm(COEFFS / f"{a}.txt") for a in ("222", "322", "444")}
+    cases = [(None, 0), (algs["222"], 1), (algs["222"], 2), (algs["322"], 1), (algs["444"], 1), (algs["444"], 2)]
+    probs = []
+    try:
+        for i in range(48):
+            m, n, k = (int(x) for x in np.exp(rng.uniform(np.log(4), np.log(600), 3)))
+            if i == 5:
+                k = 0
+            f, levels = cases[i % len(cases)]
+            C0 = rand(m, n, 500 + i)
+            probs.append({"A": to_dev(rand(m, k, 600 + i)), "B": to_dev(rand(k, n, 700 + i)), "C0": C0,
+                          "C": to_dev(C0), "fmm": f, "levels": levels, "slices": 0,
+                          "alpha": 0.0 if i == 7 else float(rng.choice([1.0, 0.75])),
+                          "beta": float(rng.choice([1.0, 0.0, -1.5]))})
+        n0 = fmm.launch_count()
+        fmm.batch_dgemm(probs)
+        torch.cuda.synchronize()
+        launches = fmm.launch_count() - n0
+        assert launches <= 2, launches          # table writer + the batch kernel
+        for i, p in enumerate(probs):
+            assert np.array_equal(to_host(p["C"]), single(fmm, p)), f"problem {i}"
+        assert fmm.take_device_error() == 0
+    finally:
+        for f in algs.values():
+            fmm.free_fmm(f)
+
+
+def test_batch_more_problems_than_one_launch(fmm, torch_cuda):
+    """More split problems than one GEMM launch's table holds: consecutive
+    waves, each result still equal to its single call."""
+    import torch
+    f = fmm.strassen_fmm()
+    probs = []
+    for i in range(100):
+        m, n, k = 40 + (i * 7) % 90, 30 + (i * 11) % 100, 50 + (i * 13) % 120
+        C0 = rand(m, n, 900 + i)
+        probs.append({"A": to_dev(rand(m, k, 1900 + i)), "B": to_dev(rand(k, n, 2900 + i)), "C0": C0,
+                      "C": to_dev(C0), "fmm": f, "levels": 1 if i % 3 else 0, "slices": 3 + i % 5,
+                      "alpha": 1.0, "beta": 1.0})
+    for p in probs:
+        if p["levels"] == 0:
+            p["fmm"] = None
+    fmm.batch_dgemm(probs)
+    torch.cuda.synchronize()
+    for i, p in enumerate(probs):
+        assert np.array_equal(to_host(p["C"]), single(fmm, p)), f"problem {i}"
+    assert fmm.take_device_error() == 0

@@ -1,0 +1,75 @@
+"""Tuner (per-problem plan choice) and the served request generator: host
+logic only, no GPU."""
+import pytest
+
+from fmm_blis_gb300 import serve, tune
+
+
+@pytest.fixture(scope="module")
+def tuner():
+    return tune.Tuner()
+
+
+def test_alg_shapes_from_coefficient_files():
+    shapes = {(a.name, a.levels): a for a in tune.alg_shapes()}
+    s222 = shapes[("222", 1)]
+    assert (s222.mt, s222.kt, s222.nt, s222.R, s222.nnz_w) == (2, 2, 2, 7, 12)
+    assert shapes[("222", 2)].R == 49 and shapes[("222", 2)].nnz_w == 144
+    assert (shapes[("232", 1)].mt, shapes[("232", 1)].kt, shapes[("232", 1)].nt) == (2, 3, 2)
+    assert shapes[("444", 2)].R == 2401
+
+
+def test_model_matches_calibration_points():
+    """The cost model reproduces the GB300 measurements it was fitted to
+    (m = n = k = 16384) within 10%."""
+    a = {(x.name, x.levels): x for x in tune.alg_shapes()}
+    n = 16384
+    assert tune.fp64_time(a[("classical", 0)], n, n, n) == pytest.approx(7.03, rel=0.1)
+    assert tune.fp64_time(a[("222", 1)], n, n, n) == pytest.approx(6.40, rel=0.1)
+    assert tune.fp64_time(a[("222", 2)], n, n, n) == pytest.approx(6.14, rel=0.1)
+    assert tune.split_time(a[("222", 2)], n, n, n, 6) == pytest.approx(0.114, rel=0.1)
+
+
+def test_plans(tuner):
+    p = tuner.plan(16384, 16384, 16384, "fp64")
+    assert (p.form, p.alg, p.levels, p.slices) == ("fp64", "222", 2, 0)
+    p = tuner.plan(16384, 16384, 16384, "split", 1e-10)
+    assert p.form == "split" and p.levels >= 1 and 5 <= p.slices <= 7
+    # small or skinny shapes stay classical
+    for shp in [(256, 256, 256), (128, 16384, 128), (300, 200, 100)]:
+        assert tuner.plan(*shp, "fp64").levels == 0
+        assert tuner.plan(*shp, "split", 1e-10).levels == 0
+    # deterministic and cached
+    assert tuner.plan(5000, 3000, 7000, "split", 1e-10) is tuner.plan(5000, 3000, 7000, "split", 1e-10)
+
+
+def test_slices_follow_target(tuner):
+    prev = None
+    for tol in (1e-6, 1e-8, 1e-10, 1e-12, 1e-14):
+        p = tuner.plan(4096, 4096, 4096, "split", tol)
+        assert p.est_rel_err * tune.ERR_SAFETY <= tol
+        if prev is not None:
+            assert p.slices >= prev
+        prev = p.slices
+    with pytest.raises(ValueError):
+        tuner.plan(4096, 4096, 4096, "split", 1e-30)
+
+
+def test_poisson_arrivals_seeded():
+    a = serve.poisson_arrivals(1000.0, 2.0, seed=3, cap_bytes=8 * 3 * 4096 ** 2)
+    b = serve.poisson_arrivals(1000.0, 2.0, seed=3, cap_bytes=8 * 3 * 4096 ** 2)
+    assert [(r.m, r.n, r.k, r.form, r.seed, r.arrival) for r in a] == \
+           [(r.m, r.n, r.k, r.form, r.seed, r.arrival) for r in b]
+    assert 1700 < len(a) < 2300                      # rate x duration
+    assert all(8 * (r.m * r.k + r.k * r.n + r.m * r.n) <= 8 * 3 * 4096 ** 2 for r in a)
+    assert all(0 < r.arrival <= 2.0 for r in a)
+    assert {r.form for r in a} == {"split", "fp64"}
+
+
+def test_batch_sizing_needs_no_gpu():
+    """Workspace sizing of a batch problem reads shapes only (host tables)."""
+    import fmm_blis_gb300 as fmm
+    f = fmm.strassen_fmm()
+    sizes = [fmm.batch_problem_workspace_size(1000, 900, 800, f, 1, s) for s in (3, 5, 7)]
+    assert 0 < sizes[0] < sizes[1] < sizes[2]
+    assert fmm.batch_problem_workspace_size(100, 90, 80, None, 0, 5) > 0
