@@ -59,9 +59,10 @@ def parse():
     p.add_argument("--e2e-steps", type=int, default=2)
     p.add_argument("--form", choices=["split", "fp64"], default="split",
                    help="split: split-BF16 FMM (the headline); fp64: the plain FP64 FMM drop-in")
-    p.add_argument("--workload", choices=["fmm", "batch", "serve"], default="fmm",
+    p.add_argument("--workload", choices=["fmm", "batch", "serve", "sweep", "accuracy"], default="fmm",
                    help="fmm: one square FMM GEMM per step (the headline); batch: 512 uneven GEMMs per step; "
-                        "serve: Poisson request stream")
+                        "serve: Poisson request stream; sweep: plain FP64 FMM over algorithms, levels and "
+                        "sizes; accuracy: split error per slice count")
     p.add_argument("--count", type=int, default=512, help="batch: GEMMs per step")
     p.add_argument("--rate", type=float, default=200.0, help="serve: arrivals per second")
     p.add_argument("--duration", type=float, default=60.0, help="serve: seconds of arrivals")
@@ -241,6 +242,124 @@ def batch_shapes(count, seed, lo=256, hi=8192):
     rng = np.random.default_rng(seed)
     return [tuple(int(round(float(np.exp(rng.uniform(np.log(lo), np.log(hi)))))) for _ in range(3))
             for _ in range(count)]
+
+
+def _dev_operand(torch, rows, cols, seed, dev, phi=None):
+    """column-major operand on the device: uniform [-1, 1) or, with phi, the
+    wide-range case (u - 0.5) * exp(phi * g), u ~ U[0, 1), g ~ N(0, 1)"""
+    g = torch.Generator(device=dev).manual_seed(seed)
+    u = torch.rand((cols, rows), generator=g, device=dev, dtype=torch.float64)
+    if phi is None:
+        return u.mul_(2).sub_(1).t()
+    z = torch.randn((cols, rows), generator=g, device=dev, dtype=torch.float64)
+    return u.sub_(0.5).mul_(z.mul_(phi).exp_()).t()
+
+
+def _time_once(torch, fn):
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def run_sweep(args, fmm, dev, rank):
+    """Plain FP64 FMM sweep: 232, 322, 333, 444 at one and two levels, square
+    m = n = k in {4096, 8192, 12288, 16384} and (m, k, n) = (16384, 4096, 16384),
+    (8192, 16384, 8192); each beside the classical FP64 GEMM of this library
+    (time, and the max-norm difference against it in units of
+    eps64 * k * max|A| * max|B|). One warm call, one timed call per case."""
+    import torch
+
+    shapes = [(n, n, n) for n in (4096, 8192, 12288, 16384)] + [(16384, 16384, 4096), (8192, 8192, 16384)]
+    rows = []
+    algs = {a: fmm.new_fmm(ROOT / "tests" / "golden" / "coeffs" / f"{a}.txt") for a in ("232", "322", "333", "444")}
+    for (m, n, k) in shapes:
+        A = _dev_operand(torch, m, k, 11, dev)
+        B = _dev_operand(torch, k, n, 12, dev)
+        C0 = _dev_operand(torch, m, n, 13, dev)
+        Cc = C0.clone()
+        fmm.dgemm(A, B, Cc.clone(), None, 0)
+        ms_c = _time_once(torch, lambda: fmm.dgemm(A, B, Cc, None, 0))
+        unit = 2.0 ** -52 * k * float(A.abs().max()) * float(B.abs().max())
+        flops = 2.0 * m * n * k
+        for name, f in algs.items():
+            for L in (1, 2):
+                Cf = C0.clone()
+                fmm.dgemm(A, B, Cf.clone(), f, L)
+                ms = _time_once(torch, lambda: fmm.dgemm(A, B, Cf, f, L))
+                rows.append({"alg": name, "levels": L, "m": m, "n": n, "k": k, "ms": ms,
+                             "tflops": flops / ms / 1e9, "vs_classical": ms_c / ms,
+                             "err_units": float((Cf - Cc).abs().max()) / unit})
+                del Cf
+        rows.append({"alg": "classical", "levels": 0, "m": m, "n": n, "k": k, "ms": ms_c,
+                     "tflops": flops / ms_c / 1e9, "vs_classical": 1.0, "err_units": 0.0})
+        del A, B, C0, Cc
+        torch.cuda.empty_cache()
+    for f in algs.values():
+        fmm.free_fmm(f)
+    assert fmm.take_device_error() == 0
+    if rank == 0:
+        best = max((r for r in rows if r["m"] == r["n"] == r["k"] == 16384 and r["levels"] > 0),
+                   key=lambda r: r["tflops"])
+        print(json.dumps({"metric": METRIC, "value": best["tflops"], "unit": "TFLOP/s", "n_gpus": 1, "steps": 1,
+                          "warmup": 1, "ms_per_step": best["ms"], "higher_is_better": True, "scaling": "weak",
+                          "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                          "config": {"workload": "plain FP64 FMM sweep (232, 322, 333, 444 x levels 1, 2; "
+                                                 "square 4096..16384 and two rectangular shapes)"},
+                          "rows": rows}))
+
+
+def run_accuracy(args, fmm, dev, rank):
+    """Split-form accuracy per slice count: 222 two levels and 333 one level
+    at m = n = k in {8192, 16384}, inputs uniform [-1, 1) and the wide-range
+    case with phi = 1 and 4; 3..7 BF16 slices. Errors against the classical
+    FP64 GEMM of this library: max-norm, max-norm relative to max|C|,
+    relative Frobenius; the plain FP64 FMM's error beside them."""
+    import torch
+
+    algs = {"222": (fmm.new_fmm(ROOT / "tests" / "golden" / "coeffs" / "222.txt"), 2),
+            "333": (fmm.new_fmm(ROOT / "tests" / "golden" / "coeffs" / "333.txt"), 1)}
+    rows = []
+    for n in (8192, 16384):
+        for dist, phi in (("uniform", None), ("hard_phi1", 1.0), ("hard_phi4", 4.0)):
+            A = _dev_operand(torch, n, n, 21, dev, phi)
+            B = _dev_operand(torch, n, n, 22, dev, phi)
+            ref = torch.zeros((n, n), dtype=torch.float64, device=dev).t()
+            fmm.dgemm(A, B, ref, None, 0)
+            torch.cuda.synchronize()
+            rmax, rfro = float(ref.abs().max()), float(torch.linalg.norm(ref))
+            for name, (f, L) in algs.items():
+                Cf = torch.zeros_like(ref)
+                fmm.dgemm(A, B, Cf, f, L)
+                torch.cuda.synchronize()
+                e64 = float((Cf - ref).abs().max())
+                del Cf
+                errs = {}
+                for s in range(3, 8):
+                    Cs = torch.zeros_like(ref)
+                    fmm.split_dgemm(A, B, Cs, f, L, s)
+                    torch.cuda.synchronize()
+                    d = Cs - ref
+                    errs[s] = {"max": float(d.abs().max()), "max_rel": float(d.abs().max()) / rmax,
+                               "fro_rel": float(torch.linalg.norm(d)) / rfro,
+                               "ratio_to_fp64_fmm": float(d.abs().max()) / e64 if e64 > 0 else None}
+                    del Cs, d
+                rows.append({"n": n, "inputs": dist, "alg": name, "levels": L, "fp64_fmm_max_err": e64,
+                             "fp64_fmm_max_rel": e64 / rmax, "split": errs})
+            del A, B, ref
+            torch.cuda.empty_cache()
+    for f, _ in algs.values():
+        fmm.free_fmm(f)
+    assert fmm.take_device_error() == 0
+    if rank == 0:
+        print(json.dumps({"metric": METRIC, "value": None, "unit": "TFLOP/s", "n_gpus": 1, "steps": 1,
+                          "warmup": 0, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+                          "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+                          "config": {"workload": "split-BF16 accuracy per slice count (222 x2, 333 x1; "
+                                                 "n = 8192, 16384; uniform and wide-range inputs)"},
+                          "rows": rows}))
 
 
 def run_batch(args, fmm, dev, world, rank, barrier, max_over_ranks):
@@ -503,6 +622,9 @@ def main():
         if world > 1:
             import torch.distributed as dist
             dist.destroy_process_group()
+        return
+    if args.workload in ("sweep", "accuracy"):
+        (run_sweep if args.workload == "sweep" else run_accuracy)(args, fmm, dev, rank)
         return
     if args.workload == "serve":
         run_serve(args, fmm, dev, world, rank, barrier, max_over_ranks)
