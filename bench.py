@@ -54,6 +54,8 @@ def parse():
     p.add_argument("--alg", default="222")
     p.add_argument("--levels", type=int, default=2)
     p.add_argument("--slices", type=int, default=6)
+    p.add_argument("--fmt", choices=["bf16", "fp8"], default="bf16",
+                   help="slice format of the split form: BF16 (base-256 digits) or FP8-E4M3 (base-32 digits)")
     p.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison runs")
     p.add_argument("--no-cpu", action="store_true", help="skip the host-core baseline")
     p.add_argument("--e2e-steps", type=int, default=2)
@@ -314,7 +316,7 @@ def run_sweep(args, fmm, dev, rank):
 def run_accuracy(args, fmm, dev, rank):
     """Split-form accuracy per slice count: 222 two levels and 333 one level
     at m = n = k in {8192, 16384}, inputs uniform [-1, 1) and the wide-range
-    case with phi = 1 and 4; 3..7 BF16 slices. Errors against the classical
+    case with phi = 1 and 4; 3..7 BF16 slices and 7..12 FP8-E4M3 slices. Errors against the classical
     FP64 GEMM of this library: max-norm, max-norm relative to max|C|,
     relative Frobenius; the plain FP64 FMM's error beside them."""
     import torch
@@ -337,15 +339,16 @@ def run_accuracy(args, fmm, dev, rank):
                 e64 = float((Cf - ref).abs().max())
                 del Cf
                 errs = {}
-                for s in range(3, 8):
-                    Cs = torch.zeros_like(ref)
-                    fmm.split_dgemm(A, B, Cs, f, L, s)
-                    torch.cuda.synchronize()
-                    d = Cs - ref
-                    errs[s] = {"max": float(d.abs().max()), "max_rel": float(d.abs().max()) / rmax,
-                               "fro_rel": float(torch.linalg.norm(d)) / rfro,
-                               "ratio_to_fp64_fmm": float(d.abs().max()) / e64 if e64 > 0 else None}
-                    del Cs, d
+                for fmt, slices in (("bf16", range(3, 8)), ("fp8", range(7, 13))):
+                    for s in slices:
+                        Cs = torch.zeros_like(ref)
+                        fmm.split_dgemm(A, B, Cs, f, L, s, fmt=fmt)
+                        torch.cuda.synchronize()
+                        d = Cs - ref
+                        errs[f"{fmt}/{s}"] = {"max": float(d.abs().max()), "max_rel": float(d.abs().max()) / rmax,
+                                              "fro_rel": float(torch.linalg.norm(d)) / rfro,
+                                              "ratio_to_fp64_fmm": float(d.abs().max()) / e64 if e64 > 0 else None}
+                        del Cs, d
                 rows.append({"n": n, "inputs": dist, "alg": name, "levels": L, "fp64_fmm_max_err": e64,
                              "fp64_fmm_max_rel": e64 / rmax, "split": errs})
             del A, B, ref
@@ -357,8 +360,8 @@ def run_accuracy(args, fmm, dev, rank):
         print(json.dumps({"metric": METRIC, "value": None, "unit": "TFLOP/s", "n_gpus": 1, "steps": 1,
                           "warmup": 0, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
                           "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
-                          "config": {"workload": "split-BF16 accuracy per slice count (222 x2, 333 x1; "
-                                                 "n = 8192, 16384; uniform and wide-range inputs)"},
+                          "config": {"workload": "split accuracy per slice count, BF16 and FP8-E4M3 slices "
+                                                 "(222 x2, 333 x1; n = 8192, 16384; uniform and wide-range inputs)"},
                           "rows": rows}))
 
 
@@ -644,11 +647,12 @@ def main():
     B = (torch.rand((n, n), generator=g, device=dev, dtype=torch.float64) * 2 - 1).t()
     C0 = (torch.rand((n, n), generator=g, device=dev, dtype=torch.float64) * 2 - 1).t()
     C = C0.clone()
-    ws = torch.empty(fmm.split_workspace_size(n, n, n, f, levels, s), dtype=torch.uint8, device=dev)
+    fmt = args.fmt
+    ws = torch.empty(fmm.split_workspace_size(n, n, n, f, levels, s, fmt), dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream()
 
     def step(Cx):
-        fmm.split_dgemm(A, B, Cx, f, levels, s, workspace=ws, stream=stream)
+        fmm.split_dgemm(A, B, Cx, f, levels, s, workspace=ws, stream=stream, fmt=fmt)
 
     for _ in range(args.warmup):
         step(C)
@@ -669,25 +673,30 @@ def main():
     gemm_ms, gemm_n, gemm_products = fmm.read_kernel_timing()
     value = world * flops / (ms / 1e3) / 1e12
 
-    # dominant kernel roofline: executed BF16 MMA flops per GEMM launch (a
-    # launch covers a group of products, each pairs * 2 * me^3)
+    # dominant kernel roofline: executed MMA flops per GEMM launch (a launch
+    # covers a group of products, each pairs * 2 * me^3); FP8 against twice
+    # the measured BF16 peak (the nominal FP8:BF16 rate ratio)
     mt = f.m_tilde ** levels
     me = -(-n // mt)
     pairs = s * (s + 1) // 2
     kernel_flops = pairs * 2.0 * me * me * me * gemm_products / max(gemm_n, 1)
     avg_launch_s = (gemm_ms / max(gemm_n, 1)) / 1e3
     peak_sus, peak_burst, hbm, peak_kind = peaks()
+    peak_kind = f"{peak_kind} bf16 sustained"
+    if fmt == "fp8":
+        peak_sus, peak_kind = 2 * peak_sus, f"2x {peak_kind} (FP8 nominal ratio)"
     achieved = kernel_flops / avg_launch_s / 1e12
     traffic = None
     tf = ROOT / "profiles" / "split_gemm_traffic.json"
-    if tf.exists():
+    # the committed capture is of the default workload only
+    if tf.exists() and (n, args.alg, levels, s, fmt) == (16384, "222", 2, 6, "bf16"):
         try:
             traffic = json.loads(tf.read_text()).get("bytes_per_launch_16384_x2")
         except ValueError:
             traffic = None
     roofline = {"bound": "tensor", "achieved": achieved, "peak": peak_sus, "unit": "TFLOP/s",
                 "frac": achieved / peak_sus, "traffic": traffic,
-                "kernel": "split_gemm_kernel", "peak_kind": f"{peak_kind} bf16 sustained",
+                "kernel": "split_gemm_kernel", "peak_kind": peak_kind,
                 "flops_per_launch": kernel_flops, "avg_launch_ms": avg_launch_s * 1e3, "launches_timed": gemm_n,
                 "products_per_launch": gemm_products / max(gemm_n, 1)}
 
@@ -739,7 +748,7 @@ def main():
             dA.copy_(hA, non_blocking=True)
             dB.copy_(hB, non_blocking=True)
             dC.copy_(hC, non_blocking=True)
-            fmm.split_dgemm(dA, dB, dC, f, levels, s, workspace=ws, stream=stream)
+            fmm.split_dgemm(dA, dB, dC, f, levels, s, workspace=ws, stream=stream, fmt=fmt)
             hC.copy_(dC, non_blocking=True)
         t1.record(stream)
         torch.cuda.synchronize()
@@ -760,9 +769,9 @@ def main():
         out = {
             "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
-            "config": {"workload": f"split-BF16 FMM {args.alg} x{levels} levels, m=n=k={n}, {s} slices",
-                       "m": n, "n": n, "k": n, "alg": args.alg, "levels": levels, "slices": s,
+            "vs_baseline": None, "dtype": "fp8_e4m3" if fmt == "fp8" else "bf16", "data": "synthetic",
+            "config": {"workload": f"split-{fmt.upper()} FMM {args.alg} x{levels} levels, m=n=k={n}, {s} slices",
+                       "m": n, "n": n, "k": n, "alg": args.alg, "levels": levels, "slices": s, "fmt": fmt,
                        "l2": ("L2 flushed between steps (per-step events)" if flush is not None
                               else f"inputs (3 x {n * n * 8 / 2**30:.2f} GiB) larger than L2; no flush"),
                        "parallelism": f"replicas x{world}"},

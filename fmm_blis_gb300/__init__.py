@@ -46,6 +46,7 @@ class BatchProblem(ctypes.Structure):
         ("alpha", ctypes.c_double), ("A", ctypes.c_void_p), ("lda", ctypes.c_int64),
         ("B", ctypes.c_void_p), ("ldb", ctypes.c_int64),
         ("beta", ctypes.c_double), ("C", ctypes.c_void_p), ("ldc", ctypes.c_int64),
+        ("format", ctypes.c_int),
     ]
 
 
@@ -111,6 +112,11 @@ def lib() -> ctypes.CDLL:
     L.fmm_gpu_strassen_ab.argtypes = [dbl, vp, i64, vp, i64, dbl, vp, i64, i64, i64, i64]
     L.fmm_gpu_split_workspace_size.restype = ctypes.c_size_t
     L.fmm_gpu_split_workspace_size.argtypes = [pf, ci, i64, i64, i64, ci]
+    L.fmm_gpu_split_workspace_size_fmt.restype = ctypes.c_size_t
+    L.fmm_gpu_split_workspace_size_fmt.argtypes = [pf, ci, i64, i64, i64, ci, ci]
+    L.fmm_gpu_split_dgemm_fmt.restype = ci
+    L.fmm_gpu_split_dgemm_fmt.argtypes = [pf, ci, i64, i64, i64, dbl, vp, i64, vp, i64, dbl, vp, i64, ci, ci, vp,
+                                          ctypes.c_size_t, vp]
     L.fmm_gpu_split_dgemm.restype = ci
     L.fmm_gpu_split_dgemm.argtypes = [pf, ci, i64, i64, i64, dbl, vp, i64, vp, i64, dbl, vp, i64, ci, vp,
                                       ctypes.c_size_t, vp]
@@ -243,29 +249,42 @@ def dgemm(A, B, C, fmm: FmmT | None = None, levels: int = 1, alpha: float = 1.0,
     _check(st, "fmm_gpu_dgemm")
 
 
-def split_workspace_size(m: int, n: int, k: int, fmm: FmmT | None, levels: int, slices: int) -> int:
+SPLIT_FORMATS = {"bf16": 0, "fp8": 1}   # FMM_SPLIT_BF16, FMM_SPLIT_FP8_E4M3
+
+
+def _fmt(fmt) -> int:
+    if isinstance(fmt, str):
+        if fmt not in SPLIT_FORMATS:
+            raise ValueError(f"unknown slice format {fmt!r}")
+        return SPLIT_FORMATS[fmt]
+    return int(fmt)
+
+
+def split_workspace_size(m: int, n: int, k: int, fmm: FmmT | None, levels: int, slices: int, fmt="bf16") -> int:
     pf = ctypes.byref(fmm) if fmm is not None else None
-    return int(lib().fmm_gpu_split_workspace_size(pf, levels if fmm is not None else 0, m, n, k, slices))
+    return int(lib().fmm_gpu_split_workspace_size_fmt(pf, levels if fmm is not None else 0, m, n, k, slices,
+                                                      _fmt(fmt)))
 
 
 def split_dgemm(A, B, C, fmm: FmmT | None = None, levels: int = 1, slices: int = 6, alpha: float = 1.0,
-                beta: float = 1.0, workspace=None, stream=None) -> None:
-    """C := beta*C + alpha*A*B from BF16 digit slices on the tensor cores.
-    `workspace` is a CUDA uint8 tensor of at least split_workspace_size bytes
-    (allocated here when None)."""
+                beta: float = 1.0, workspace=None, stream=None, fmt="bf16") -> None:
+    """C := beta*C + alpha*A*B from digit slices on the tensor cores: fmt
+    "bf16" (8-bit digits, slices 2..8) or "fp8" (5-bit digits as FP8-E4M3,
+    slices 2..12). `workspace` is a CUDA uint8 tensor of at least
+    split_workspace_size bytes (allocated here when None)."""
     import torch
     m, k = A.shape
     k2, n = B.shape
     if k2 != k or tuple(C.shape) != (m, n):
         raise ValueError("shape mismatch")
     lda, ldb, ldc = _colmajor_ld(A, m, "A"), _colmajor_ld(B, k, "B"), _colmajor_ld(C, m, "C")
-    need = split_workspace_size(m, n, k, fmm, levels, slices)
+    need = split_workspace_size(m, n, k, fmm, levels, slices, fmt)
     if workspace is None:
         workspace = torch.empty(max(need, 256), dtype=torch.uint8, device=C.device)
     pf = ctypes.byref(fmm) if fmm is not None else None
-    st = lib().fmm_gpu_split_dgemm(pf, levels if fmm is not None else 0, m, n, k, alpha, A.data_ptr(), lda,
-                                   B.data_ptr(), ldb, beta, C.data_ptr(), ldc, slices,
-                                   workspace.data_ptr(), workspace.numel(), _stream_ptr(stream))
+    st = lib().fmm_gpu_split_dgemm_fmt(pf, levels if fmm is not None else 0, m, n, k, alpha, A.data_ptr(), lda,
+                                       B.data_ptr(), ldb, beta, C.data_ptr(), ldc, slices, _fmt(fmt),
+                                       workspace.data_ptr(), workspace.numel(), _stream_ptr(stream))
     _check(st, "fmm_gpu_split_dgemm")
 
 
@@ -289,7 +308,8 @@ def split_dgemm_noalloc(A, B, C, fmm: FmmT | None = None, levels: int = 1, slice
 def make_batch(problems):
     """problems: iterable of dicts with keys A, B, C (column-major CUDA
     tensors), and optional fmm (FmmT or None), levels, slices (0: plain FP64
-    form), alpha, beta. Returns a ctypes array of fmm_batch_problem."""
+    form), fmt ("bf16" or "fp8" slices), alpha, beta. Returns a ctypes array
+    of fmm_batch_problem."""
     probs = list(problems)
     arr = (BatchProblem * max(len(probs), 1))()
     for i, p in enumerate(probs):
@@ -305,6 +325,7 @@ def make_batch(problems):
         arr[i].A, arr[i].lda = A.data_ptr(), _colmajor_ld(A, m, "A")
         arr[i].B, arr[i].ldb = B.data_ptr(), _colmajor_ld(B, k, "B")
         arr[i].C, arr[i].ldc = C.data_ptr(), _colmajor_ld(C, m, "C")
+        arr[i].format = _fmt(p.get("fmt", "bf16"))
     return arr, len(probs)
 
 
@@ -313,7 +334,8 @@ def batch_workspace_size(batch) -> int:
     return int(lib().fmm_gpu_batch_workspace_size(count, arr))
 
 
-def batch_problem_workspace_size(m: int, n: int, k: int, fmm: FmmT | None, levels: int, slices: int) -> int:
+def batch_problem_workspace_size(m: int, n: int, k: int, fmm: FmmT | None, levels: int, slices: int,
+                                 fmt="bf16") -> int:
     """Workspace one problem of this shape needs inside a batch (all of its
     products at once), from the shape alone: the sizing call reads no operand
     data, so placeholder addresses stand in for the operands."""
@@ -326,6 +348,7 @@ def batch_problem_workspace_size(m: int, n: int, k: int, fmm: FmmT | None, level
     arr[0].A, arr[0].lda = 256, max(m, 1)
     arr[0].B, arr[0].ldb = 256, max(k, 1)
     arr[0].C, arr[0].ldc = 256, max(m, 1)
+    arr[0].format = _fmt(fmt)
     return int(lib().fmm_gpu_batch_workspace_size(1, arr))
 
 

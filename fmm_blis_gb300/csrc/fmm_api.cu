@@ -268,13 +268,20 @@ extern "C" int fmm_gpu_strassen_ab(double alpha, const double* A, int64_t lda, c
 extern "C" size_t fmm_gpu_split_workspace_size(const fmm_t* fmm, int levels, int64_t m, int64_t n, int64_t k,
                                                int slices)
 {
-    if (m < 0 || n < 0 || k < 0 || slices < 2 || slices > 8) return 0;
+    return fmm_gpu_split_workspace_size_fmt(fmm, levels, m, n, k, slices, FMM_SPLIT_BF16);
+}
+
+extern "C" size_t fmm_gpu_split_workspace_size_fmt(const fmm_t* fmm, int levels, int64_t m, int64_t n, int64_t k,
+                                                   int slices, int format)
+{
+    if (format != FMM_SPLIT_BF16 && format != FMM_SPLIT_FP8_E4M3) return 0;
+    if (m < 0 || n < 0 || k < 0 || slices < 2 || slices > (format ? 12 : 8)) return 0;
     fmm_t flat;
     int owned = 0;
     if (fmm_flatten(fmm, levels, &flat, &owned) != FMM_OK) return 0;
     AlgView v;
     v.mt = flat.m_tilde; v.kt = flat.k_tilde; v.nt = flat.n_tilde; v.R = flat.R;
-    size_t b = fmm_split_ws_bytes(v, m, n, k, slices);
+    size_t b = fmm_split_ws_bytes(v, m, n, k, slices, format);
     if (owned) free_fmm(flat);
     return b;
 }
@@ -284,9 +291,19 @@ extern "C" int fmm_gpu_split_dgemm(const fmm_t* fmm, int levels, int64_t m, int6
                                    double beta, double* C, int64_t ldc, int slices, void* workspace,
                                    size_t workspace_bytes, void* stream)
 {
+    return fmm_gpu_split_dgemm_fmt(fmm, levels, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, slices,
+                                   FMM_SPLIT_BF16, workspace, workspace_bytes, stream);
+}
+
+extern "C" int fmm_gpu_split_dgemm_fmt(const fmm_t* fmm, int levels, int64_t m, int64_t n, int64_t k,
+                                       double alpha, const double* A, int64_t lda, const double* B, int64_t ldb,
+                                       double beta, double* C, int64_t ldc, int slices, int format,
+                                       void* workspace, size_t workspace_bytes, void* stream)
+{
     int rc = check_gemm_args(m, n, k, A, lda, B, ldb, C, ldc);
     if (rc != FMM_OK) return rc;
-    if (slices < 2 || slices > 8) return FMM_ERR_ARG;
+    if (format != FMM_SPLIT_BF16 && format != FMM_SPLIT_FP8_E4M3) return FMM_ERR_ARG;
+    if (slices < 2 || slices > (format ? 12 : 8)) return FMM_ERR_ARG;
     fmm_t flat;
     int owned = 0;
     rc = fmm_flatten(fmm, levels, &flat, &owned);
@@ -296,6 +313,6 @@ extern "C" int fmm_gpu_split_dgemm(const fmm_t* fmm, int levels, int64_t m, int6
     if (owned) free_fmm(flat);
     if (rc != FMM_OK) return rc;
     if (fmm_device_error_word() == nullptr) return FMM_ERR_CUDA;
-    return fmm_split_launch(alg, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, slices, workspace,
+    return fmm_split_launch(alg, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, slices, format, workspace,
                             workspace_bytes, (cudaStream_t)stream);
 }

@@ -86,11 +86,12 @@ size_t fmm_f64_batch_ws_bytes(int count);
 int fmm_f64_batch_launch(int count, const F64BatchItem* items, void* ws, size_t ws_bytes, cudaStream_t st);
 
 /* split form (fmm_split.cu) */
-size_t fmm_split_ws_bytes(const AlgView& alg, int64_t m, int64_t n, int64_t k, int slices);
+/* fmt: 0 = BF16 slices, 1 = FP8-E4M3 slices */
+size_t fmm_split_ws_bytes(const AlgView& alg, int64_t m, int64_t n, int64_t k, int slices, int fmt);
 int fmm_split_launch(const AlgView& alg, int64_t m, int64_t n, int64_t k,
                      double alpha, const double* A, int64_t lda,
                      const double* B, int64_t ldb, double beta, double* C, int64_t ldc,
-                     int slices, void* ws, size_t ws_bytes, cudaStream_t st);
+                     int slices, int fmt, void* ws, size_t ws_bytes, cudaStream_t st);
 
 /* C := beta*C (fmm_f64.cu) */
 int fmm_scale_c(int64_t m, int64_t n, double beta, double* C, int64_t ldc, cudaStream_t st);

@@ -1,6 +1,7 @@
 /*
  * Split-precision (Ozaki-style) form of the FMM GEMM on the sm_103a tensor
- * cores.
+ * cores, with BF16 slices (base-256 digits, tcgen05 kind::f16) or FP8-E4M3
+ * slices (base-32 digits, kind::f8f6f4). db below is the digit width: 8 or 5.
  *
  * Per product r of the (flattened) FMM algorithm:
  *
@@ -9,31 +10,36 @@
  *              |S_r[i,:]| <= sum_q |U[q,r]| * max|A_q[i,:]|, evaluated in FP64
  *              in the same order as the sums themselves (so the bound holds
  *              for the rounded sums too). The per-sub-block row/column maxima
- *              are computed once per call (amax/bmax kernels).
+ *              are computed once per call (amax/bmax kernels). These
+ *              power-of-two scales are per row of S_r and per column of T_r
+ *              for both formats: a scale that varied along k would give each
+ *              k block's products a different weight and end the exact
+ *              integer accumulation over k.
  *   2. pack:   the fused multi-operand pack (plugin/ref_kernels/
  *              bli_packm_fmm_ref.c:89-147): S_r (T_r) is formed in FP64 in
  *              sub-block order with zero fill, then split there into `s`
- *              balanced base-256 digits d_1..d_s in [-128, 128]:
- *                  S[i,p] ~= 2^(E_i + 1 - 8s) * sum_t d_t[i,p] 256^(s-t)
- *              using integer arithmetic on the FP64 bit pattern. Each digit is
- *              an integer of at most 8 significant bits, so it is exact in
- *              BF16. Digits are written K-major ("slices" [t][row][k]).
- *   3. gemm:   tcgen05.mma (kind::f16, BF16 x BF16 -> FP32 in TMEM) over the
- *              slice pairs (t,u) with t+u = g for the levels g = 2..s+1. Every
- *              product of two digits is an integer of magnitude <= 2^14, so a
- *              1024-term chunk sums to an integer of magnitude <= 2^24 that
- *              FP32 holds exactly; the epilogue warps drain each chunk from
- *              TMEM (double-buffered, so the tensor core keeps running),
- *              convert it exactly to int32 and add it to the level sum L_g.
- *              At the end of a level, L_g is folded into a 64-bit fixed-point
- *              accumulator Z (held in TMEM) in units of level G (G = 6, or 7
- *              when k_pad <= 128: the finest unit for which k_pad * 2^14 *
- *              2^(8(G-2)) stays below 2^62):
- *                  Z = sum_{g<=G} L_g * 2^(8(G-g)) + sum_{g>G} round(L_g / 2^(8(g-G)))
- *              and at the end of the tile M_r[i,j] ~= 2^(E_i + F_j + 2 - 8G) * Z
- *              is formed in FP64 and added with alpha*W[p,r] into every C
- *              sub-block p (the multi-C epilogue,
- *              plugin/ref_kernels/bli_gemm_fmm_ref.c:99-120), coalesced.
+ *              balanced base-2^db digits d_1..d_s:
+ *                  S[i,p] ~= 2^(E_i + 1 - db*s) * sum_t d_t[i,p] 2^(db(s-t))
+ *              using integer arithmetic on the FP64 bit pattern. BF16 digits
+ *              are integers in [-128, 128] (at most 8 significant bits), FP8
+ *              digits integers in [-16, 16] (at most 4): exact either way.
+ *              Digits are written K-major ("slices" [t][row][k]).
+ *   3. gemm:   tcgen05.mma (FP32 accumulation in TMEM) over the slice pairs
+ *              (t,u) with t+u = g for the levels g = 2..s+1. A digit product
+ *              is an integer of magnitude <= 2^14 (BF16) or 2^8 (FP8), so a
+ *              chunk of 16 stage rows (1024 BF16 or 2048 FP8 terms) sums to an
+ *              integer of magnitude <= 2^24 that FP32 holds exactly; the
+ *              epilogue warps drain each chunk from TMEM (double-buffered, so
+ *              the tensor core keeps running), convert it exactly to int32 and
+ *              add it to the level sum L_g. At the end of a level, L_g is
+ *              folded into a 64-bit fixed-point accumulator Z in global
+ *              memory in units of level G (BF16: G = 6, or 7 when
+ *              k_pad <= 128; FP8: G = min(s + 1, 10); the finest units that
+ *              keep Z inside int64):
+ *                  Z = sum_{g<=G} L_g * 2^(db(G-g)) + sum_{g>G} round(L_g / 2^(db(g-G)))
+ *              and M_r[i,j] ~= 2^(E_i + F_j + 2 - db*G) * Z is formed in FP64
+ *              and added with alpha*W[p,r] into every C sub-block p (the
+ *              multi-C epilogue, plugin/ref_kernels/bli_gemm_fmm_ref.c:99-120).
  *
  * FP64 is only used for the packing sums, the bounds, the int64 -> FP64
  * conversion and the C updates; the digit split, the level sums and Z are
@@ -41,7 +47,7 @@
  * bit for bit by a CPU restatement.
  *
  * Limits: k_e = ceil(k/k~) <= 16384 per call (level sums stay inside int32
- * and Z inside int64); slices 2..8; finite inputs.
+ * and Z inside int64); slices 2..8 (BF16) or 2..12 (FP8); finite inputs.
  */
 #include "fmm_internal.h"
 #include "sm103_ptx.cuh"
@@ -89,22 +95,33 @@ __device__ __forceinline__ int exp_above(double b)
     return -1010 - __clzll((long long)bits);
 }
 
-/* Balanced base-256 digits of x relative to 2^E (|x| < 2^E): X =
- * round(x * 2^(8s-E-1)) (ties away from zero), |X| <= 2^(8s-1), split as
- * d[s-1], ..., d[1] in [-128, 127] from the bottom and d[0] in [-128, 128];
- * every digit has at most 8 significant bits, so it is exact in BF16. */
-/* The same digits in one step: Y = X + sum_{j < S-1} 128 * 256^j. Adding 128
- * at every lower byte position turns the balanced digits into plain bytes, so
- * the low S-1 bytes of Y are d[S-1] + 128, ..., d[1] + 128 and floor(Y /
- * 256^(S-1)) is d[0]: the balanced digits above, without a digit loop. Y is
- * kept modulo 2^64 (its low bytes are exact); d[0] is (X >> 8(S-1)) plus the
- * carry out of the low bytes, which stays exact for the 64-bit X of S = 8. */
+/* Balanced base-2^DB digits of x relative to 2^E (|x| < 2^E): X =
+ * round(x * 2^(DB*s-E-1)) (ties away from zero), |X| <= 2^(DB*s-1), split as
+ * d[s-1], ..., d[1] in [-2^(DB-1), 2^(DB-1)) from the bottom and d[0] in
+ * [-2^(DB-1), 2^(DB-1)]. DB = 8 (BF16 slices): every digit has at most 8
+ * significant bits; DB = 5 (FP8-E4M3 slices): every digit is an integer of
+ * magnitude at most 16, at most 4 significant bits. Both are exact.
+ * The same digits in one step: Y = X + sum_{j < S-1} 2^(DB-1) * 2^(DB*j).
+ * Adding 2^(DB-1) at every lower digit position turns the balanced digits
+ * into plain DB-bit fields, so the low S-1 fields of Y are d[S-1] + 2^(DB-1),
+ * ..., d[1] + 2^(DB-1) and floor(Y / 2^(DB(S-1))) is d[0]: the balanced
+ * digits above, without a digit loop. Y is kept modulo 2^64 (its low fields
+ * are exact); d[0] is (X >> DB(S-1)) plus the carry out of the low fields,
+ * which stays exact for the 64-bit X of the largest S. */
 struct Digits {
     int64_t X;
     uint64_t Y;
 };
 
-template <int S>
+template <int S, int DB>
+__host__ __device__ constexpr uint64_t digit_offset()
+{
+    uint64_t off = 0;
+    for (int j = 0; j < S - 1; ++j) off |= (uint64_t)1 << (DB * j + DB - 1);
+    return off;
+}
+
+template <int S, int DB>
 __device__ __forceinline__ Digits split_offset(double x, int E)
 {
     const uint64_t bits = (uint64_t)__double_as_longlong(x);
@@ -113,34 +130,47 @@ __device__ __forceinline__ Digits split_offset(double x, int E)
     uint64_t mant = bits & 0x000fffffffffffffull;
     int ex;
     if (bexp == 0) ex = -1074; else { mant |= 0x0010000000000000ull; ex = bexp - 1075; }
-    const int sh = ex + 8 * S - E - 1;
+    const int sh = ex + DB * S - E - 1;
     int64_t X;
     if (mant == 0 || sh < -62) X = 0;
     else if (sh >= 0) X = (int64_t)(mant << sh);
     else X = (int64_t)((mant + (1ull << (-sh - 1))) >> (-sh));
     if (neg) X = -X;
-    constexpr uint64_t kOff = S > 1 ? (0x8080808080808080ull >> (8 * (9 - S))) : 0ull;
-    return Digits{X, (uint64_t)X + kOff};
+    return Digits{X, (uint64_t)X + digit_offset<S, DB>()};
 }
 
-/* digit t (0 = most significant) as an exact float. A lower digit is byte
- * S-1-t of Y minus 128: the byte is placed in the mantissa of 2^23 (one byte
- * permute) and 2^23 + 128 is subtracted, both exact. The top digit goes
- * through the same 2^23-offset conversion from its integer value. With t a
- * compile-time constant after unrolling, the byte choice folds away. */
-template <int S>
+/* digit t (0 = most significant) as an exact float. A lower digit is field
+ * S-1-t of Y minus 2^(DB-1): the field is placed in the mantissa of 2^23 (one
+ * byte permute for DB = 8, a shift and mask for DB = 5) and 2^23 + 2^(DB-1)
+ * is subtracted, both exact. The top digit goes through the same 2^23-offset
+ * conversion from its integer value. With t a compile-time constant after
+ * unrolling, the field choice folds away. */
+template <int S, int DB>
 __device__ __forceinline__ float digit_f(const Digits& g, int t)
 {
-    constexpr int sh = 8 * (S - 1);
-    constexpr uint64_t kOff = S > 1 ? (0x8080808080808080ull >> (8 * (9 - S))) : 0ull;
+    constexpr int sh = DB * (S - 1);
+    constexpr uint64_t kOff = digit_offset<S, DB>();
     constexpr uint64_t kMask = (1ull << sh) - 1;
     if (t == 0) {
         const int d = (int)(g.X >> sh) + (int)((((uint64_t)g.X & kMask) + kOff) >> sh);
         return __int_as_float(0x4B400000 + d) - 12582912.0f;   /* exact for |d| < 2^22 */
     }
-    const int bi = S - 1 - t;
-    const uint32_t w = bi < 4 ? (uint32_t)g.Y : (uint32_t)(g.Y >> 32);
-    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u + (unsigned)(bi & 3))) - 8388736.0f;
+    const int fi = S - 1 - t;
+    if (DB == 8) {
+        const uint32_t w = fi < 4 ? (uint32_t)g.Y : (uint32_t)(g.Y >> 32);
+        return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u + (unsigned)(fi & 3))) - 8388736.0f;
+    }
+    const uint32_t field = (uint32_t)(g.Y >> (DB * fi)) & ((1u << DB) - 1);
+    return __uint_as_float(0x4B000000u | field) - (8388608.0f + (float)(1 << (DB - 1)));
+}
+
+/* two floats that are exact in FP8-E4M3 (integers of magnitude <= 16) as a
+ * packed e4m3x2 half-word, first value in the low byte */
+__device__ __forceinline__ uint32_t pack_e4m3x2_exact(float lo, float hi)
+{
+    unsigned short h;
+    asm("cvt.rn.satfinite.e4m3x2.f32 %0, %1, %2;" : "=h"(h) : "f"(hi), "f"(lo));
+    return (uint32_t)h;
 }
 
 /* two floats that are exact in BF16 (at most 8 significant bits) as a packed
@@ -148,6 +178,33 @@ __device__ __forceinline__ float digit_f(const Digits& g, int t)
 __device__ __forceinline__ uint32_t pack_bf16x2_exact(float lo, float hi)
 {
     return __byte_perm(__float_as_uint(lo), __float_as_uint(hi), 0x7632u);
+}
+
+/* Writes the S digit slices of 8 consecutive k elements: slice tt of the
+ * element at (slice-0) element offset off lands at off + tt * slice_stride
+ * of a BF16 (DB = 8, 16 bytes per slice) or FP8-E4M3 (DB = 5, 8 bytes per
+ * slice) array. */
+template <int S, int DB>
+__device__ __forceinline__ void store_digits8(uint8_t* __restrict__ base, int64_t off, int64_t slice_stride,
+                                              const Digits (&Y)[8])
+{
+#pragma unroll
+    for (int tt = 0; tt < S; ++tt) {
+        const int64_t e = off + (int64_t)tt * slice_stride;
+        if (DB == 8) {
+            uint32_t w[4];
+#pragma unroll
+            for (int h = 0; h < 4; ++h)
+                w[h] = pack_bf16x2_exact(digit_f<S, DB>(Y[2 * h], tt), digit_f<S, DB>(Y[2 * h + 1], tt));
+            *(uint4*)(base + 2 * e) = make_uint4(w[0], w[1], w[2], w[3]);
+        } else {
+            uint32_t h[4];
+#pragma unroll
+            for (int x = 0; x < 4; ++x)
+                h[x] = pack_e4m3x2_exact(digit_f<S, DB>(Y[2 * x], tt), digit_f<S, DB>(Y[2 * x + 1], tt));
+            *(uint2*)(base + e) = make_uint2(h[0] | (h[1] << 16), h[2] | (h[3] << 16));
+        }
+    }
 }
 
 /* v * 2^e, in at most two exact power-of-two multiplications. */
@@ -338,11 +395,11 @@ __device__ __forceinline__ void scale_first(const PEnt& x, double (&s)[N])
  * row-major (K-major) into slices sa[q][t][m_pad][k_pad]. The product index
  * runs fastest in the block order, so the products at one tile position run
  * together and read their shared A sub-block tiles through L2 once. */
-template <int S>
+template <int S, int DB>
 __global__ void __launch_bounds__(256)
 pack_a_kernel(const int* __restrict__ tab, int r0, int np, const double* __restrict__ A, int64_t lda,
               int64_t m, int64_t k, int64_t m_pad, int64_t k_pad,
-              const int* __restrict__ e_row, uint16_t* __restrict__ sa)
+              const int* __restrict__ e_row, uint8_t* __restrict__ sa)
 {
     __shared__ double Sf[64][65];
     __shared__ PEnt ent[kPackMaxEnt];
@@ -352,7 +409,7 @@ pack_a_kernel(const int* __restrict__ tab, int r0, int np, const double* __restr
     const int r = r0 + q;
     const int64_t i0 = (int64_t)(blockIdx.x / (unsigned)np) * 64, p0 = (int64_t)blockIdx.y * 64;
     e_row += (int64_t)q * m_pad;
-    sa += (int64_t)q * S * m_pad * k_pad;
+    const int64_t slice0 = (int64_t)q * S * m_pad * k_pad;   /* element offset of this product */
     const int eb = t.u_off[r], ne_ = t.u_off[r + 1] - eb;
     for (int e = threadIdx.x; e < ne_; e += blockDim.x) {
         const int part = t.u_ent[2 * (eb + e)];
@@ -402,15 +459,8 @@ pack_a_kernel(const int* __restrict__ tab, int r0, int np, const double* __restr
         const int E = e_row[gi];
         Digits Y[8];
 #pragma unroll
-        for (int x = 0; x < 8; ++x) Y[x] = split_offset<S>(Sf[kg * 8 + x][rr], E);
-#pragma unroll
-        for (int tt = 0; tt < S; ++tt) {
-            uint32_t w[4];
-#pragma unroll
-            for (int h = 0; h < 4; ++h) w[h] = pack_bf16x2_exact(digit_f<S>(Y[2 * h], tt), digit_f<S>(Y[2 * h + 1], tt));
-            uint4* dst = (uint4*)(sa + ((int64_t)tt * m_pad + gi) * k_pad + p0 + kg * 8);
-            *dst = make_uint4(w[0], w[1], w[2], w[3]);
-        }
+        for (int x = 0; x < 8; ++x) Y[x] = split_offset<S, DB>(Sf[kg * 8 + x][rr], E);
+        store_digits8<S, DB>(sa, slice0 + gi * k_pad + p0 + kg * 8, m_pad * k_pad, Y);
     }
 }
 
@@ -418,11 +468,11 @@ pack_a_kernel(const int* __restrict__ tab, int r0, int np, const double* __restr
  * columns x 64 k of T_r, r = r0 + q (column j of T_r is contiguous in k
  * already), and writes its digits into slices sb[q][t][n_pad][k_pad];
  * product index fastest, as on the A side. */
-template <int S>
+template <int S, int DB>
 __global__ void __launch_bounds__(256)
 pack_b_kernel(const int* __restrict__ tab, int r0, int np, const double* __restrict__ B, int64_t ldb,
               int64_t k, int64_t n, int64_t n_pad, int64_t k_pad,
-              const int* __restrict__ f_col, uint16_t* __restrict__ sb)
+              const int* __restrict__ f_col, uint8_t* __restrict__ sb)
 {
     __shared__ PEnt ent[kPackMaxEnt];
     const Tab t = tab_view(tab);
@@ -430,7 +480,7 @@ pack_b_kernel(const int* __restrict__ tab, int r0, int np, const double* __restr
     const int q = (int)(blockIdx.x % (unsigned)np);
     const int r = r0 + q;
     f_col += (int64_t)q * n_pad;
-    sb += (int64_t)q * S * n_pad * k_pad;
+    const int64_t slice0 = (int64_t)q * S * n_pad * k_pad;
     const int eb = t.v_off[r], ne_ = t.v_off[r + 1] - eb;
     for (int e = threadIdx.x; e < ne_; e += blockDim.x) {
         const int part = t.v_ent[2 * (eb + e)];
@@ -469,43 +519,56 @@ pack_b_kernel(const int* __restrict__ tab, int r0, int np, const double* __restr
     const int F = f_col[gj];
     Digits Y[8];
 #pragma unroll
-    for (int x = 0; x < 8; ++x) Y[x] = split_offset<S>(v8[x], F);
-#pragma unroll
-    for (int tt = 0; tt < S; ++tt) {
-        uint32_t w[4];
-#pragma unroll
-        for (int h = 0; h < 4; ++h) w[h] = pack_bf16x2_exact(digit_f<S>(Y[2 * h], tt), digit_f<S>(Y[2 * h + 1], tt));
-        uint4* dst = (uint4*)(sb + ((int64_t)tt * n_pad + gj) * k_pad + p0);
-        *dst = make_uint4(w[0], w[1], w[2], w[3]);
-    }
+    for (int x = 0; x < 8; ++x) Y[x] = split_offset<S, DB>(v8[x], F);
+    store_digits8<S, DB>(sb, slice0 + gj * k_pad + p0, n_pad * k_pad, Y);
 }
 
-template <int S>
+template <int S, int DB>
 void launch_packs_t(const int* tab, int r, int np, const double* A, int64_t lda, const double* B, int64_t ldb,
                     int64_t m, int64_t n, int64_t k, int64_t m_pad, int64_t n_pad, int64_t k_pad,
-                    const int* e_row, const int* f_col, uint16_t* sa, uint16_t* sb, cudaStream_t st)
+                    const int* e_row, const int* f_col, uint8_t* sa, uint8_t* sb, cudaStream_t st)
 {
-    pack_a_kernel<S><<<dim3((unsigned)(np * (m_pad / 64)), (unsigned)(k_pad / 64)), 256, 0, st>>>(
+    pack_a_kernel<S, DB><<<dim3((unsigned)(np * (m_pad / 64)), (unsigned)(k_pad / 64)), 256, 0, st>>>(
         tab, r, np, A, lda, m, k, m_pad, k_pad, e_row, sa);
-    pack_b_kernel<S><<<dim3((unsigned)(np * (n_pad / 32)), (unsigned)(k_pad / 64)), 256, 0, st>>>(
+    pack_b_kernel<S, DB><<<dim3((unsigned)(np * (n_pad / 32)), (unsigned)(k_pad / 64)), 256, 0, st>>>(
         tab, r, np, B, ldb, k, n, n_pad, k_pad, f_col, sb);
 }
 
-/* digit slices of the products r .. r+np-1 (exponents already in place) */
-void launch_packs(int s, const int* tab, int r, int np, const double* A, int64_t lda, const double* B,
+/* digit slices of the products r .. r+np-1 (exponents already in place);
+ * fmt 0: BF16 (s = 2..8), fmt 1: FP8-E4M3 (s = 2..12) */
+void launch_packs(int fmt, int s, const int* tab, int r, int np, const double* A, int64_t lda, const double* B,
                   int64_t ldb, int64_t m, int64_t n, int64_t k, int64_t m_pad, int64_t n_pad,
-                  int64_t k_pad, const int* e_row, const int* f_col, uint16_t* sa, uint16_t* sb,
+                  int64_t k_pad, const int* e_row, const int* f_col, uint8_t* sa, uint8_t* sb,
                   cudaStream_t st)
 {
-    switch (s) {
-    case 2: launch_packs_t<2>(tab, r, np, A, lda, B, ldb, m, n, k, m_pad, n_pad, k_pad, e_row, f_col, sa, sb, st); break;
-    case 3: launch_packs_t<3>(tab, r, np, A, lda, B, ldb, m, n, k, m_pad, n_pad, k_pad, e_row, f_col, sa, sb, st); break;
-    case 4: launch_packs_t<4>(tab, r, np, A, lda, B, ldb, m, n, k, m_pad, n_pad, k_pad, e_row, f_col, sa, sb, st); break;
-    case 5: launch_packs_t<5>(tab, r, np, A, lda, B, ldb, m, n, k, m_pad, n_pad, k_pad, e_row, f_col, sa, sb, st); break;
-    case 6: launch_packs_t<6>(tab, r, np, A, lda, B, ldb, m, n, k, m_pad, n_pad, k_pad, e_row, f_col, sa, sb, st); break;
-    case 7: launch_packs_t<7>(tab, r, np, A, lda, B, ldb, m, n, k, m_pad, n_pad, k_pad, e_row, f_col, sa, sb, st); break;
-    default: launch_packs_t<8>(tab, r, np, A, lda, B, ldb, m, n, k, m_pad, n_pad, k_pad, e_row, f_col, sa, sb, st); break;
+#define FMM_PACKS(S_, DB_) \
+    launch_packs_t<S_, DB_>(tab, r, np, A, lda, B, ldb, m, n, k, m_pad, n_pad, k_pad, e_row, f_col, sa, sb, st)
+    if (fmt == 0) {
+        switch (s) {
+        case 2: FMM_PACKS(2, 8); break;
+        case 3: FMM_PACKS(3, 8); break;
+        case 4: FMM_PACKS(4, 8); break;
+        case 5: FMM_PACKS(5, 8); break;
+        case 6: FMM_PACKS(6, 8); break;
+        case 7: FMM_PACKS(7, 8); break;
+        default: FMM_PACKS(8, 8); break;
+        }
+    } else {
+        switch (s) {
+        case 2: FMM_PACKS(2, 5); break;
+        case 3: FMM_PACKS(3, 5); break;
+        case 4: FMM_PACKS(4, 5); break;
+        case 5: FMM_PACKS(5, 5); break;
+        case 6: FMM_PACKS(6, 5); break;
+        case 7: FMM_PACKS(7, 5); break;
+        case 8: FMM_PACKS(8, 5); break;
+        case 9: FMM_PACKS(9, 5); break;
+        case 10: FMM_PACKS(10, 5); break;
+        case 11: FMM_PACKS(11, 5); break;
+        default: FMM_PACKS(12, 5); break;
+        }
     }
+#undef FMM_PACKS
 }
 
 /* ------------------------------------------------------ GEMM kernel ---- */
@@ -552,7 +615,10 @@ struct GemmProblem {
     int64_t* Z;           /* [product][n_pad][m_pad] int64 level accumulators */
     int s;                /* slices */
     int zlevel;           /* G: the level whose unit Z counts in */
-    int nkb;              /* k_pad / 64 */
+    int nkb;              /* k_pad / kbe */
+    int kbe;              /* k elements per 128-byte stage row: 64 (BF16) or 128 (FP8) */
+    int db;               /* digit bits: 8 (BF16) or 5 (FP8-E4M3) */
+    int fmt;              /* 0: BF16 slices, kind::f16; 1: FP8-E4M3 slices, kind::f8f6f4 */
     int m_pad, n_pad;     /* rows per slice in the A / B slice arrays */
     int tiles_m, tiles_n; /* per product */
     int item_begin;       /* first work item of this problem in the launch */
@@ -676,9 +742,9 @@ split_gemm_kernel(const __grid_constant__ GemmLaunch L)
                             const int kb = (pi & 1) ? nkb - 1 - y : y;
                             if (!sm103::mbar_wait(&empty[st], ph ^ 1, abort_flag, L.err, 1)) { ok = false; break; }
                             sm103::mbar_arrive_expect_tx(&full[st], kStageBytes);
-                            sm103::tma_load_2d(sA + st * kATileBytes, &P.tmA, &full[st], kb * kBK,
+                            sm103::tma_load_2d(sA + st * kATileBytes, &P.tmA, &full[st], kb * P.kbe,
                                                arow + (t - 1) * P.m_pad);
-                            sm103::tma_load_2d(sB + st * kBTileBytes, &P.tmB, &full[st], kb * kBK,
+                            sm103::tma_load_2d(sB + st * kBTileBytes, &P.tmB, &full[st], kb * P.kbe,
                                                brow + (u - 1) * P.n_pad);
                             armed |= 1u << st;
                             if (++st == kStages) { st = 0; ph ^= 1; armed = 0; }
@@ -699,13 +765,14 @@ split_gemm_kernel(const __grid_constant__ GemmLaunch L)
     } else if (warp == 1) {
         /* ---------------- MMA issuer ---------------- */
         if (lane == 0) {
-            constexpr uint32_t idesc = sm103::idesc_bf16_f32(kTileM, kTileN);
+            constexpr uint32_t idesc16 = sm103::idesc_bf16_f32(kTileM, kTileN);
+            constexpr uint32_t idesc8 = sm103::idesc_e4m3_f32(kTileM, kTileN);
             int st = 0, buf = 0;
             uint32_t ph = 0, aph = 0;
             bool ok = true;
             for (int b = blockIdx.x; b < L.nitems && ok; b += gridDim.x) {
                 const Item it = decode_item(L, b);
-                const int s = L.prob[it.p].s, nkb = L.prob[it.p].nkb;
+                const int s = L.prob[it.p].s, nkb = L.prob[it.p].nkb, fmt = L.prob[it.p].fmt;
                 for (int g = 2; g <= s + 1 && ok; ++g) {
                     const int level_kb = level_pairs(g, s) * nkb;
                     int jl = 0;
@@ -719,11 +786,21 @@ split_gemm_kernel(const __grid_constant__ GemmLaunch L)
                             sm103::tc_fence_after();
                             const uint32_t a0 = sm103::smem_u32(sA + st * kATileBytes);
                             const uint32_t b0 = sm103::smem_u32(sB + st * kBTileBytes);
+                            /* four MMAs per 128-byte stage row: K = 16 BF16 or 32 FP8
+                             * elements each, 32 bytes apart */
+                            if (fmt) {
 #pragma unroll
-                            for (int kk = 0; kk < kBK / 16; ++kk)
-                                sm103::mma_bf16(tmem + buf * kTileN, sm103::smem_desc_sw128(a0 + kk * 32),
-                                                sm103::smem_desc_sw128(b0 + kk * 32), idesc,
-                                                (jl % kChunkKB != 0 || kk != 0) ? 1u : 0u);
+                                for (int kk = 0; kk < 4; ++kk)
+                                    sm103::mma_f8(tmem + buf * kTileN, sm103::smem_desc_sw128(a0 + kk * 32),
+                                                  sm103::smem_desc_sw128(b0 + kk * 32), idesc8,
+                                                  (jl % kChunkKB != 0 || kk != 0) ? 1u : 0u);
+                            } else {
+#pragma unroll
+                                for (int kk = 0; kk < 4; ++kk)
+                                    sm103::mma_bf16(tmem + buf * kTileN, sm103::smem_desc_sw128(a0 + kk * 32),
+                                                    sm103::smem_desc_sw128(b0 + kk * 32), idesc16,
+                                                    (jl % kChunkKB != 0 || kk != 0) ? 1u : 0u);
+                            }
                             sm103::mma_commit(&empty[st]);
                             if (++st == kStages) { st = 0; ph ^= 1; }
                             ++jl;
@@ -760,7 +837,7 @@ split_gemm_kernel(const __grid_constant__ GemmLaunch L)
             const int s = P.s, nkb = P.nkb;
             int64_t* zrow = P.Z + (int64_t)it.r * P.n_pad * P.m_pad +
                             (int64_t)(it.tile_n * kTileN + colbase) * P.m_pad + it.tile_m * kTileM + row;
-            const struct { int zlevel, m_pad; } a = {P.zlevel, P.m_pad};
+            const struct { int zlevel, m_pad, db; } a = {P.zlevel, P.m_pad, P.db};
             for (int g = 2; g <= s + 1 && ok; ++g) {
                 int lsum[kEpiCols];
 #pragma unroll
@@ -786,15 +863,15 @@ split_gemm_kernel(const __grid_constant__ GemmLaunch L)
                 }
                 if (!ok) break;
                 /* fold L_g into the Z tile (units of level G): D = G - g, exact
-                 * left shift by 8D for D >= 0, rounded right shift by -8D (ties
-                 * up) for D < 0. The first level stores; later levels add with
+                 * left shift by db*D for D >= 0, rounded right shift by -db*D
+                 * (ties up) for D < 0. The first level stores; later levels add with
                  * fire-and-forget 64-bit reductions (two's-complement addition
                  * is exact and order-free), so the warps go straight back to
                  * draining the accumulator. */
                 {
                     const int D = a.zlevel - g;
-                    const uint32_t lsh = D >= 0 ? 8 * D : 0;
-                    const uint32_t rsh = D >= 0 ? 0 : -8 * D;
+                    const uint32_t lsh = D >= 0 ? a.db * D : 0;
+                    const uint32_t rsh = D >= 0 ? 0 : -a.db * D;
                     const uint64_t rnd = D >= 0 ? 0 : (1ull << (rsh - 1));
                     uint64_t zp = (uint64_t)zrow;
                     const uint64_t zstep = (uint64_t)a.m_pad * 8;
@@ -834,14 +911,15 @@ split_gemm_kernel(const __grid_constant__ GemmLaunch L)
 /* Multi-C epilogue for a group of products [r0, r0 + nprod): one thread per
  * (C sub-block p = blockIdx.y, element (i, j) of p) adds alpha*W[p,r] *
  * M_r[i,j] for the group's products in increasing order, with M_r[i,j] =
- * 2^(E_i + F_j + 2 - 8G) * Z_r[i,j] converted in integer arithmetic
+ * 2^(E_i + F_j + 2 - db*G) * Z_r[i,j] = 2^(ebase + E_i + F_j) * Z_r[i,j]
+ * converted in integer arithmetic
  * (plugin/ref_kernels/bli_gemm_fmm_ref.c:99-120, once per group instead of
  * once per product). */
 constexpr int kScatterMaxEnt = 1024;
 
 __global__ void __launch_bounds__(256)
 scatter_kernel(const int* __restrict__ tab, int r0, int nprod, int64_t m, int64_t n,
-               int m_pad, int n_pad, int zlevel, double alpha, const int64_t* __restrict__ Z,
+               int m_pad, int n_pad, int ebase, double alpha, const int64_t* __restrict__ Z,
                const int* __restrict__ e_row, const int* __restrict__ f_col, double* __restrict__ C,
                int64_t ldc)
 {
@@ -876,7 +954,6 @@ scatter_kernel(const int* __restrict__ tab, int r0, int nprod, int64_t m, int64_
     double c = *cp;
     const int64_t zij = (int64_t)j * m_pad + i;
     const int64_t zstride = (int64_t)n_pad * m_pad;
-    const int ebase = 2 - 8 * zlevel;
     int q = 0;
     for (; q + 4 <= ne; q += 4) {
         int64_t z[4];
@@ -908,7 +985,7 @@ constexpr int kScatterAllSmem = 32 * 1024;   /* cs[] budget: P * threads * 8 */
 
 __global__ void __launch_bounds__(256)
 scatter_all_kernel(const int* __restrict__ tab, int r0, int nprod, int64_t m, int64_t n,
-                   int m_pad, int n_pad, int zlevel, double alpha, const int64_t* __restrict__ Z,
+                   int m_pad, int n_pad, int ebase, double alpha, const int64_t* __restrict__ Z,
                    const int* __restrict__ e_row, const int* __restrict__ f_col, double* __restrict__ C,
                    int64_t ldc)
 {
@@ -942,7 +1019,6 @@ scatter_all_kernel(const int* __restrict__ tab, int r0, int nprod, int64_t m, in
     }
     const int64_t zij = (int64_t)j * m_pad + i;
     const int64_t zstride = (int64_t)n_pad * m_pad;
-    const int ebase = 2 - 8 * zlevel;
     int q = 0;
     for (; q + 4 <= nprod; q += 4) {
         int64_t z[4];
@@ -1002,15 +1078,17 @@ PFN_cuTensorMapEncodeTiled_v12000 get_encode_fn()
  * 128-byte swizzle. */
 /* 2-D map over slices[rows_total][k_pad] BF16, box 64 (k) x box_rows, 128-byte
  * swizzle. */
-int make_slice_map(CUtensorMap* map, const void* base, int64_t k_pad, int64_t rows_total, int box_rows)
+int make_slice_map(CUtensorMap* map, const void* base, int64_t k_pad, int64_t rows_total, int box_rows, int fmt)
 {
     PFN_cuTensorMapEncodeTiled_v12000 enc = get_encode_fn();
     if (!enc) return FMM_ERR_CUDA;
+    const int esz = fmt ? 1 : 2;                         /* FP8-E4M3 bytes or BF16 */
     cuuint64_t dims[2] = {(cuuint64_t)k_pad, (cuuint64_t)rows_total};
-    cuuint64_t strides[1] = {(cuuint64_t)(k_pad * 2)};
-    cuuint32_t box[2] = {(cuuint32_t)kBK, (cuuint32_t)box_rows};
+    cuuint64_t strides[1] = {(cuuint64_t)(k_pad * esz)};
+    cuuint32_t box[2] = {(cuuint32_t)(128 / esz), (cuuint32_t)box_rows};   /* 128-byte rows */
     cuuint32_t estr[2] = {1, 1};
-    CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box,
+    CUresult r = enc(map, fmt ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
+                     const_cast<void*>(base), dims, strides, box,
                      estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     return r == CUDA_SUCCESS ? FMM_OK : FMM_ERR_CUDA;
@@ -1026,7 +1104,10 @@ struct Dims {
     int64_t me, ne, ke, m_pad, n_pad, k_pad;
 };
 
-Dims dims_of(const AlgView& alg, int64_t m, int64_t n, int64_t k)
+/* k elements per 128-byte stage row of a slice format */
+inline int kbe_of(int fmt) { return fmt ? 128 : kBK; }
+
+Dims dims_of(const AlgView& alg, int64_t m, int64_t n, int64_t k, int fmt = 0)
 {
     Dims d;
     d.me = (m + alg.mt - 1) / alg.mt;
@@ -1034,19 +1115,19 @@ Dims dims_of(const AlgView& alg, int64_t m, int64_t n, int64_t k)
     d.ke = (k + alg.kt - 1) / alg.kt;
     d.m_pad = round_up(std::max<int64_t>(d.me, 1), kTileM);
     d.n_pad = round_up(std::max<int64_t>(d.ne, 1), kTileN);
-    d.k_pad = round_up(std::max<int64_t>(d.ke, 1), kBK);
+    d.k_pad = round_up(std::max<int64_t>(d.ke, 1), kbe_of(fmt));
     return d;
 }
 
-size_t per_product_bytes(const Dims& d, int s)
+size_t per_product_bytes(const Dims& d, int s, int fmt)
 {
-    return 2 * (size_t)s * (size_t)(d.m_pad + d.n_pad) * (size_t)d.k_pad +
+    return (fmt ? 1 : 2) * (size_t)s * (size_t)(d.m_pad + d.n_pad) * (size_t)d.k_pad +
            8 * (size_t)d.m_pad * (size_t)d.n_pad + 4 * (size_t)(d.m_pad + d.n_pad) + 1024;
 }
 
-int group_size(const AlgView& alg, const Dims& d, int s, size_t budget)
+int group_size(const AlgView& alg, const Dims& d, int s, size_t budget, int fmt)
 {
-    const size_t per = per_product_bytes(d, s);
+    const size_t per = per_product_bytes(d, s, fmt);
     size_t g = budget / per;
     if (g < 1) g = 1;
     if (g > (size_t)alg.R) g = (size_t)alg.R;
@@ -1060,8 +1141,9 @@ struct WsLayout {
     int group;
 };
 
-WsLayout ws_layout_g(const AlgView& alg, const Dims& d, int64_t m, int64_t n, int s, int G)
+WsLayout ws_layout_g(const AlgView& alg, const Dims& d, int64_t m, int64_t n, int s, int G, int fmt)
 {
+    const size_t esz = fmt ? 1 : 2;
     WsLayout L;
     size_t off = 0;
     auto take = [&](size_t bytes) { size_t o = off; off += (bytes + 255) / 256 * 256; return o; };
@@ -1070,8 +1152,8 @@ WsLayout ws_layout_g(const AlgView& alg, const Dims& d, int64_t m, int64_t n, in
     L.bmax = take(sizeof(unsigned long long) * (size_t)alg.kt * (size_t)n);
     L.erow = take(sizeof(int) * (size_t)G * (size_t)d.m_pad);
     L.fcol = take(sizeof(int) * (size_t)G * (size_t)d.n_pad);
-    L.sa = take(2 * (size_t)G * s * (size_t)d.m_pad * (size_t)d.k_pad);
-    L.sb = take(2 * (size_t)G * s * (size_t)d.n_pad * (size_t)d.k_pad);
+    L.sa = take(esz * (size_t)G * s * (size_t)d.m_pad * (size_t)d.k_pad);
+    L.sb = take(esz * (size_t)G * s * (size_t)d.n_pad * (size_t)d.k_pad);
     L.z = take(8 * (size_t)G * (size_t)d.m_pad * (size_t)d.n_pad);
     L.total = off;
     return L;
@@ -1079,12 +1161,13 @@ WsLayout ws_layout_g(const AlgView& alg, const Dims& d, int64_t m, int64_t n, in
 
 /* Layout for the largest product group whose whole workspace fits in
  * `budget` bytes (at least one product). */
-WsLayout ws_layout(const AlgView& alg, int64_t m, int64_t n, int64_t k, int s, size_t budget = kGroupBudget)
+WsLayout ws_layout(const AlgView& alg, int64_t m, int64_t n, int64_t k, int s, size_t budget = kGroupBudget,
+                   int fmt = 0)
 {
-    const Dims d = dims_of(alg, m, n, k);
-    int G = group_size(alg, d, s, budget);
-    WsLayout L = ws_layout_g(alg, d, m, n, s, G);
-    while (G > 1 && L.total > budget) L = ws_layout_g(alg, d, m, n, s, --G);
+    const Dims d = dims_of(alg, m, n, k, fmt);
+    int G = group_size(alg, d, s, budget, fmt);
+    WsLayout L = ws_layout_g(alg, d, m, n, s, G, fmt);
+    while (G > 1 && L.total > budget) L = ws_layout_g(alg, d, m, n, s, --G, fmt);
     return L;
 }
 
@@ -1143,9 +1226,9 @@ extern "C" int fmm_gpu_read_kernel_timing(double* total_ms, uint64_t* launches, 
     return rc;
 }
 
-size_t fmm_split_ws_bytes(const AlgView& alg, int64_t m, int64_t n, int64_t k, int slices)
+size_t fmm_split_ws_bytes(const AlgView& alg, int64_t m, int64_t n, int64_t k, int slices, int fmt)
 {
-    return ws_layout(alg, m, n, k, slices).total;
+    return ws_layout(alg, m, n, k, slices, kGroupBudget, fmt).total;
 }
 
 /* One split-form GEMM problem being executed: its algorithm, geometry,
@@ -1162,6 +1245,7 @@ struct SplitJob {
     double* C;
     int64_t ldc;
     int s;
+    int fmt;       /* 0: BF16 slices, 1: FP8-E4M3 slices */
     bool trivial;  /* nothing beyond C := beta*C */
     WsLayout L;
     uint8_t* w;
@@ -1169,9 +1253,11 @@ struct SplitJob {
 
 static int job_init(SplitJob& j, const AlgView& alg, int64_t m, int64_t n, int64_t k, double alpha,
                     const double* A, int64_t lda, const double* B, int64_t ldb, double beta, double* C,
-                    int64_t ldc, int s)
+                    int64_t ldc, int s, int fmt = 0)
 {
-    if (s < 2 || s > 8) return FMM_ERR_ARG;
+    if (fmt != 0 && fmt != 1) return FMM_ERR_ARG;
+    if (s < 2 || s > (fmt ? 12 : 8)) return FMM_ERR_ARG;
+    j.fmt = fmt;
     j.alg = alg;
     j.m = m; j.n = n; j.k = k;
     j.alpha = alpha; j.beta = beta;
@@ -1182,7 +1268,7 @@ static int job_init(SplitJob& j, const AlgView& alg, int64_t m, int64_t n, int64
     if (j.trivial) return FMM_OK;
     if (alg.max_nnz_u > kPackMaxEnt || alg.max_nnz_v > kPackMaxEnt) return FMM_ERR_UNSUPPORTED;
     if (m > 0x7fffffffLL || n > 0x7fffffffLL) return FMM_ERR_UNSUPPORTED;
-    j.d = dims_of(alg, m, n, k);
+    j.d = dims_of(alg, m, n, k, fmt);
     if (j.d.ke > kMaxKe) return FMM_ERR_UNSUPPORTED;
     if (j.d.me * j.d.ne > 0xffffffffLL) return FMM_ERR_UNSUPPORTED;
     /* the scatter keeps one C part's W entries of a group in shared memory */
@@ -1196,7 +1282,7 @@ static int job_init(SplitJob& j, const AlgView& alg, int64_t m, int64_t n, int64
 static int job_bind(SplitJob& j, void* ws, size_t ws_bytes, size_t budget)
 {
     if (j.trivial) return FMM_OK;
-    j.L = ws_layout(j.alg, j.m, j.n, j.k, j.s, budget);
+    j.L = ws_layout(j.alg, j.m, j.n, j.k, j.s, budget, j.fmt);
     if ((int64_t)j.L.group * j.s * std::max(j.d.m_pad, j.d.n_pad) > 0x7fffffffLL) return FMM_ERR_UNSUPPORTED;
     if (ws == nullptr || ws_bytes < j.L.total) return FMM_ERR_WORKSPACE;
     if (((uintptr_t)ws & 255) != 0) return FMM_ERR_ARG;
@@ -1208,7 +1294,7 @@ static int job_bind(SplitJob& j, void* ws, size_t ws_bytes, size_t budget)
 static int job_bind_group(SplitJob& j, void* ws, size_t ws_bytes, int G)
 {
     if (j.trivial) return FMM_OK;
-    j.L = ws_layout_g(j.alg, j.d, j.m, j.n, j.s, G);
+    j.L = ws_layout_g(j.alg, j.d, j.m, j.n, j.s, G, j.fmt);
     if ((int64_t)j.L.group * j.s * std::max(j.d.m_pad, j.d.n_pad) > 0x7fffffffLL) return FMM_ERR_UNSUPPORTED;
     if (ws == nullptr || ws_bytes < j.L.total) return FMM_ERR_WORKSPACE;
     if (((uintptr_t)ws & 255) != 0) return FMM_ERR_ARG;
@@ -1244,35 +1330,47 @@ static int job_pack(SplitJob& j, int r0, int np, cudaStream_t st)
     unsigned long long* bmax = (unsigned long long*)(j.w + j.L.bmax);
     int* e_row = (int*)(j.w + j.L.erow);
     int* f_col = (int*)(j.w + j.L.fcol);
-    uint16_t* sa = (uint16_t*)(j.w + j.L.sa);
-    uint16_t* sb = (uint16_t*)(j.w + j.L.sb);
+    uint8_t* sa = j.w + j.L.sa;
+    uint8_t* sb = j.w + j.L.sb;
     if (np <= 0) return FMM_OK;
     /* one launch per kernel for the whole group (grid y holds the product of
      * the exponent pass; the pack grids' x extent np * tiles stays far below
      * 2^31 since np * s * max(m_pad, n_pad) < 2^31) */
     exps_kernel<<<dim3((unsigned)((d.m_pad + d.n_pad + 255) / 256), (unsigned)np), 256, 0, st>>>(
         j.alg.tab, r0, j.m, j.n, j.k, d.m_pad, d.n_pad, amax, bmax, e_row, f_col);
-    launch_packs(j.s, j.alg.tab, r0, np, j.A, j.lda, j.B, j.ldb, j.m, j.n, j.k, d.m_pad, d.n_pad, d.k_pad, e_row,
+    launch_packs(j.fmt, j.s, j.alg.tab, r0, np, j.A, j.lda, j.B, j.ldb, j.m, j.n, j.k, d.m_pad, d.n_pad, d.k_pad, e_row,
                  f_col, sa, sb, st);
     fmm_count_launch(3);
     return FMM_OK;
 }
 
-static int job_zlevel(const SplitJob& j) { return j.d.k_pad <= 128 ? 7 : 6; }
+/* G, the level whose unit Z counts in: BF16 6, or 7 when k_pad <= 128 (the
+ * finest unit keeping Z inside int64); FP8 s + 1 up to 10 (exact for s <= 9) */
+static int job_zlevel(const SplitJob& j)
+{
+    if (j.fmt) return std::min(j.s + 1, 10);
+    return j.d.k_pad <= 128 ? 7 : 6;
+}
+static int job_db(const SplitJob& j) { return j.fmt ? 5 : 8; }
+/* exponent of Z's unit relative to 2^(E_i + F_j) */
+static int job_ebase(const SplitJob& j) { return 2 - job_db(j) * job_zlevel(j); }
 
 /* the job's product group as one problem of a GEMM launch */
 static int job_fill(const SplitJob& j, GemmProblem& gp, int np, int item_begin)
 {
     const Dims& d = j.d;
     const int G = j.L.group;
-    if (make_slice_map(&gp.tmA, j.w + j.L.sa, d.k_pad, (int64_t)G * j.s * d.m_pad, kTileM) != FMM_OK)
+    if (make_slice_map(&gp.tmA, j.w + j.L.sa, d.k_pad, (int64_t)G * j.s * d.m_pad, kTileM, j.fmt) != FMM_OK)
         return FMM_ERR_CUDA;
-    if (make_slice_map(&gp.tmB, j.w + j.L.sb, d.k_pad, (int64_t)G * j.s * d.n_pad, kTileN) != FMM_OK)
+    if (make_slice_map(&gp.tmB, j.w + j.L.sb, d.k_pad, (int64_t)G * j.s * d.n_pad, kTileN, j.fmt) != FMM_OK)
         return FMM_ERR_CUDA;
     gp.Z = (int64_t*)(j.w + j.L.z);
     gp.s = j.s;
     gp.zlevel = job_zlevel(j);
-    gp.nkb = (int)(d.k_pad / kBK);
+    gp.kbe = kbe_of(j.fmt);
+    gp.nkb = (int)(d.k_pad / gp.kbe);
+    gp.db = job_db(j);
+    gp.fmt = j.fmt;
     gp.m_pad = (int)d.m_pad;
     gp.n_pad = (int)d.n_pad;
     gp.tiles_m = (int)(d.m_pad / kTileM);
@@ -1299,13 +1397,13 @@ static void job_scatter(const SplitJob& j, int r0, int np, cudaStream_t st)
     const size_t smem = (size_t)P * std::max(T, 0) * 8 + (size_t)E * 12 + (size_t)(np + 1) * 4;
     if (P <= 64 && T >= 32 && smem <= 48 * 1024) {
         scatter_all_kernel<<<(unsigned)((elems + T - 1) / T), (unsigned)T, smem, st>>>(
-            j.alg.tab, r0, np, j.m, j.n, (int)j.d.m_pad, (int)j.d.n_pad, job_zlevel(j), j.alpha,
+            j.alg.tab, r0, np, j.m, j.n, (int)j.d.m_pad, (int)j.d.n_pad, job_ebase(j), j.alpha,
             (const int64_t*)(j.w + j.L.z), (const int*)(j.w + j.L.erow), (const int*)(j.w + j.L.fcol), j.C, j.ldc);
         fmm_count_launch(1);
         return;
     }
     scatter_kernel<<<dim3((unsigned)((elems + 255) / 256), (unsigned)(j.alg.mt * j.alg.nt)), 256, 0, st>>>(
-        j.alg.tab, r0, np, j.m, j.n, (int)j.d.m_pad, (int)j.d.n_pad, job_zlevel(j), j.alpha,
+        j.alg.tab, r0, np, j.m, j.n, (int)j.d.m_pad, (int)j.d.n_pad, job_ebase(j), j.alpha,
         (const int64_t*)(j.w + j.L.z), (const int*)(j.w + j.L.erow), (const int*)(j.w + j.L.fcol), j.C, j.ldc);
     fmm_count_launch(1);
 }
@@ -1340,11 +1438,11 @@ static int launch_gemm(GemmLaunch& gl, int64_t nitems, int nprod_timed, cudaStre
 
 static int split_launch_budget(const AlgView& alg, int64_t m, int64_t n, int64_t k, double alpha,
                                const double* A, int64_t lda, const double* B, int64_t ldb, double beta,
-                               double* C, int64_t ldc, int s, void* ws, size_t ws_bytes, size_t budget,
+                               double* C, int64_t ldc, int s, int fmt, void* ws, size_t ws_bytes, size_t budget,
                                cudaStream_t st)
 {
     SplitJob j;
-    int rc = job_init(j, alg, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, s);
+    int rc = job_init(j, alg, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, s, fmt);
     if (rc != FMM_OK) return rc;
     if (!j.trivial && (rc = job_bind(j, ws, ws_bytes, budget)) != FMM_OK) return rc;
     if ((rc = job_prologue(j, st)) != FMM_OK || j.trivial) return rc;
@@ -1374,7 +1472,8 @@ int fmm_split_batch(int count, const SplitJob* jobs_in, void* ws, size_t ws_byte
     std::vector<size_t> full(count, 0);
     for (int i = 0; i < count; ++i)
         if (!jobs[i].trivial) {
-            const WsLayout Lf = ws_layout_g(jobs[i].alg, jobs[i].d, jobs[i].m, jobs[i].n, jobs[i].s, jobs[i].alg.R);
+            const WsLayout Lf = ws_layout_g(jobs[i].alg, jobs[i].d, jobs[i].m, jobs[i].n, jobs[i].s, jobs[i].alg.R,
+                                            jobs[i].fmt);
             full[i] = Lf.total;
         }
     int i = 0;
@@ -1388,7 +1487,7 @@ int fmm_split_batch(int count, const SplitJob* jobs_in, void* ws, size_t ws_byte
         if (full[i] > ws_bytes) {
             SplitJob& j = jobs[i];
             int rc = split_launch_budget(j.alg, j.m, j.n, j.k, j.alpha, j.A, j.lda, j.B, j.ldb, j.beta, j.C, j.ldc,
-                                         j.s, ws, ws_bytes, ws_bytes, st);
+                                         j.s, j.fmt, ws, ws_bytes, ws_bytes, st);
             if (rc != FMM_OK) return rc;
             ++i;
             continue;
@@ -1420,7 +1519,10 @@ int fmm_split_batch(int count, const SplitJob* jobs_in, void* ws, size_t ws_byte
          * item) first, so the CTAs' round-robin shares end evenly */
         std::vector<int> ord;
         for (int q = i; q < e; ++q) ord.push_back(q);
-        auto item_cost = [&](int q) { return (int64_t)jobs[q].s * (jobs[q].s + 1) / 2 * (jobs[q].d.k_pad / kBK); };
+        auto item_cost = [&](int q) {
+            return (int64_t)jobs[q].s * (jobs[q].s + 1) / 2 * (jobs[q].d.k_pad / kbe_of(jobs[q].fmt)) /
+                   (jobs[q].fmt ? 2 : 1);   /* FP8 MMAs run at twice the BF16 rate */
+        };
         std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return item_cost(a) > item_cost(b); });
         for (size_t x = 0; x < ord.size(); ++x) {
             SplitJob& j = jobs[ord[x]];
@@ -1443,9 +1545,10 @@ size_t fmm_split_batch_ws(int count, const SplitJob* jobs)
     size_t sum = 0, mx = 0;
     for (int i = 0; i < count; ++i) {
         if (jobs[i].trivial) continue;
-        const size_t f = ws_layout_g(jobs[i].alg, jobs[i].d, jobs[i].m, jobs[i].n, jobs[i].s, jobs[i].alg.R).total;
+        const size_t f =
+            ws_layout_g(jobs[i].alg, jobs[i].d, jobs[i].m, jobs[i].n, jobs[i].s, jobs[i].alg.R, jobs[i].fmt).total;
         sum += (f + 255) / 256 * 256;
-        const size_t one = ws_layout(jobs[i].alg, jobs[i].m, jobs[i].n, jobs[i].k, jobs[i].s, 1).total;
+        const size_t one = ws_layout(jobs[i].alg, jobs[i].m, jobs[i].n, jobs[i].k, jobs[i].s, 1, jobs[i].fmt).total;
         mx = std::max(mx, one);
     }
     return std::max(std::min(sum, kGroupBudget), mx);
@@ -1466,10 +1569,10 @@ void fmm_split_job_free(SplitJob* j) { delete j; }
 
 int fmm_split_launch(const AlgView& alg, int64_t m, int64_t n, int64_t k, double alpha,
                      const double* A, int64_t lda, const double* B, int64_t ldb, double beta,
-                     double* C, int64_t ldc, int s, void* ws, size_t ws_bytes, cudaStream_t st)
+                     double* C, int64_t ldc, int s, int fmt, void* ws, size_t ws_bytes, cudaStream_t st)
 {
     /* the group size follows the workspace the caller provides */
-    return split_launch_budget(alg, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, s, ws, ws_bytes,
+    return split_launch_budget(alg, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, s, fmt, ws, ws_bytes,
                                ws_bytes, st);
 }
 
@@ -1540,7 +1643,7 @@ extern "C" int fmm_gpu_split_dgemm_noalloc(const fmm_t* fmm, int levels, int64_t
         return FMM_ERR_CUDA;
     alg.tab = (const int*)scratch;
     alg.htab = table.data();
-    return split_launch_budget(alg, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, slices, scratch + tab_bytes,
+    return split_launch_budget(alg, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, slices, 0, scratch + tab_bytes,
                                ws_bytes, ws_bytes, st);
 }
 
@@ -1564,7 +1667,8 @@ int batch_jobs(int count, const fmm_batch_problem* probs, std::vector<SplitJob>&
             return FMM_ERR_ARG;
         if (p.m > 0 && p.n > 0 && p.C == nullptr) return FMM_ERR_ARG;
         if (p.m > 0 && p.n > 0 && p.k > 0 && (p.A == nullptr || p.B == nullptr)) return FMM_ERR_ARG;
-        if (p.slices != 0 && (p.slices < 2 || p.slices > 8)) return FMM_ERR_ARG;
+        if (p.format != 0 && p.format != 1) return FMM_ERR_ARG;
+        if (p.slices != 0 && (p.slices < 2 || p.slices > (p.format ? 12 : 8))) return FMM_ERR_ARG;
         fmm_t flat;
         int owned = 0;
         int rc = fmm_flatten(p.fmm, p.fmm ? p.levels : 0, &flat, &owned);
@@ -1584,7 +1688,8 @@ int batch_jobs(int count, const fmm_batch_problem* probs, std::vector<SplitJob>&
             continue;
         }
         SplitJob j;
-        rc = job_init(j, alg, p.m, p.n, p.k, p.alpha, p.A, p.lda, p.B, p.ldb, p.beta, p.C, p.ldc, p.slices);
+        rc = job_init(j, alg, p.m, p.n, p.k, p.alpha, p.A, p.lda, p.B, p.ldb, p.beta, p.C, p.ldc, p.slices,
+                      p.format);
         if (rc != FMM_OK) return rc;
         jobs.push_back(j);
     }

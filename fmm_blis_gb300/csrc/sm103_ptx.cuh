@@ -137,6 +137,17 @@ __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a_desc, uint6
                  : "memory");
 }
 
+/* D[tmem] (+)= A[smem desc] * B[smem desc], kind::f8f6f4 (FP8 in, FP32 accumulate). */
+__device__ __forceinline__ void mma_f8(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc,
+                                       uint32_t idesc, uint32_t accumulate)
+{
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "setp.ne.u32 p, %4, 0;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}"
+                 ::"r"(d_tmem), "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+                 : "memory");
+}
+
 /* Arrive on an mbarrier once all previously issued tcgen05.mma of this
  * thread have completed. */
 __device__ __forceinline__ void mma_commit(uint64_t* bar)
@@ -164,6 +175,15 @@ __host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N)
     return (1u << 4)                       /* D format: F32 */
          | (1u << 7)                       /* A format: BF16 */
          | (1u << 10)                      /* B format: BF16 */
+         | ((uint32_t)(N >> 3) << 17)      /* N / 8 */
+         | ((uint32_t)(M >> 4) << 24);     /* M / 16 */
+}
+
+/* Instruction descriptor for kind::f8f6f4: E4M3 A and B (format 0, both
+ * K-major), FP32 D. */
+__host__ __device__ constexpr uint32_t idesc_e4m3_f32(int M, int N)
+{
+    return (1u << 4)                       /* D format: F32 */
          | ((uint32_t)(N >> 3) << 17)      /* N / 8 */
          | ((uint32_t)(M >> 4) << 24);     /* M / 16 */
 }

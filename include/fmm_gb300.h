@@ -181,11 +181,34 @@ int fmm_gpu_split_dgemm(const fmm_t* fmm, int levels,
                         int slices, void* workspace, size_t workspace_bytes,
                         void* stream);
 
+/* Slice formats of the split form. No counterpart in the reference. */
+#define FMM_SPLIT_BF16 0      /* base-256 digits as BF16, tcgen05 kind::f16, slices 2..8 */
+#define FMM_SPLIT_FP8_E4M3 1  /* base-32 digits as FP8-E4M3, tcgen05 kind::f8f6f4, slices 2..12 */
+
+/* fmm_gpu_split_workspace_size for a slice format (FMM_SPLIT_*). */
+size_t fmm_gpu_split_workspace_size_fmt(const fmm_t* fmm, int levels,
+                                        int64_t m, int64_t n, int64_t k,
+                                        int slices, int format);
+
+/* fmm_gpu_split_dgemm with a slice format: FMM_SPLIT_BF16 (identical to
+ * fmm_gpu_split_dgemm) or FMM_SPLIT_FP8_E4M3: 5-bit digits in [-16, 16]
+ * stored as FP8-E4M3, multiplied at the FP8 tensor rate with the same
+ * per-row/per-column power-of-two scales and exact integer accumulation, so
+ * each slice carries 5 bits instead of 8. No counterpart in the reference. */
+int fmm_gpu_split_dgemm_fmt(const fmm_t* fmm, int levels,
+                            int64_t m, int64_t n, int64_t k,
+                            double alpha, const double* A, int64_t lda,
+                            const double* B, int64_t ldb,
+                            double beta, double* C, int64_t ldc,
+                            int slices, int format, void* workspace, size_t workspace_bytes,
+                            void* stream);
+
 /* ------------------------------------------------------- GPU, batched -- */
 
 /* One GEMM of a batch: C := beta*C + alpha*A*B with `levels` levels of `fmm`
- * (NULL: classical), in the split form with `slices` digit slices, or in the
- * plain FP64 form when slices == 0. Device pointers, column-major. */
+ * (NULL: classical), in the split form with `slices` digit slices of
+ * `format` (FMM_SPLIT_*), or in the plain FP64 form when slices == 0. Device
+ * pointers, column-major. */
 typedef struct fmm_batch_problem_s {
     const fmm_t* fmm;
     int levels;
@@ -199,18 +222,20 @@ typedef struct fmm_batch_problem_s {
     double beta;
     double* C;
     int64_t ldc;
+    int format;
 } fmm_batch_problem;
 
 /* Recommended workspace for fmm_gpu_batch_dgemm (capped at 32 GiB; any size
  * that holds the largest problem's one-product workspace works). */
 size_t fmm_gpu_batch_workspace_size(int count, const fmm_batch_problem* problems);
 
-/* Runs `count` independent GEMMs (their C regions must not overlap). Split-
- * form problems go in waves: every problem of a wave is packed, one
- * persistent tensor-core launch covers all their (problem, product, tile)
- * work items, then each C is updated; each problem's result is bit-identical
- * to its fmm_gpu_split_dgemm result. Plain FP64 problems run in order through
- * the FP64 kernel. No counterpart in the reference (which runs one GEMM per
+/* Runs `count` independent GEMMs (their C regions must not overlap). Plain
+ * FP64 problems run in one persistent launch over all their (problem, tile
+ * position) work items. Split-form problems go in waves of up to 80 whose
+ * workspaces fit together: every problem of a wave is packed, one persistent
+ * tensor-core launch covers all their (problem, product, tile) work items,
+ * then each C is updated. Each result is bit-identical to the problem's own
+ * single call. No counterpart in the reference (which runs one GEMM per
  * call). Asynchronous on `stream`. */
 int fmm_gpu_batch_dgemm(int count, const fmm_batch_problem* problems,
                         void* workspace, size_t workspace_bytes, void* stream);

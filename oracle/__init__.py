@@ -45,6 +45,8 @@ def lib() -> ctypes.CDLL:
         L.oracle_split_fmm_dgemm.restype = ci
         L.oracle_split_fmm_dgemm.argtypes = [ci, ci, ci, ci, ip, ip, ip, i64, i64, i64, dbl, vp, i64, vp,
                                              i64, dbl, vp, i64, ci]
+        L.oracle_split_fmm_dgemm_fmt.restype = ci
+        L.oracle_split_fmm_dgemm_fmt.argtypes = L.oracle_split_fmm_dgemm.argtypes + [ci]
         L.oracle_dgemm.restype = None
         L.oracle_dgemm.argtypes = [i64, i64, i64, dbl, vp, i64, vp, i64, dbl, vp, i64]
         L.oracle_naive_dgemm.restype = None
@@ -86,14 +88,16 @@ def fmm_dgemm(alg, A, B, C, alpha=1.0, beta=1.0, r_begin=0, r_end=None):
     return C
 
 
-def split_fmm_dgemm(alg, A, B, C, slices, alpha=1.0, beta=1.0):
-    """The split-precision form's exact arithmetic (in place)."""
+def split_fmm_dgemm(alg, A, B, C, slices, alpha=1.0, beta=1.0, fmt="bf16"):
+    """The split-precision form's exact arithmetic (in place); fmt "bf16"
+    (base-256 digits) or "fp8" (base-32 digits, FP8-E4M3 slices)."""
     A, B, C = _f64(A), _f64(B), _f64(C)
     m, k = A.shape
     n = B.shape[1]
     args, keep = _alg(alg)
-    rc = lib().oracle_split_fmm_dgemm(*args, m, n, k, alpha, A.ctypes.data, max(m, 1), B.ctypes.data,
-                                      max(k, 1), beta, C.ctypes.data, max(m, 1), slices)
+    rc = lib().oracle_split_fmm_dgemm_fmt(*args, m, n, k, alpha, A.ctypes.data, max(m, 1), B.ctypes.data,
+                                          max(k, 1), beta, C.ctypes.data, max(m, 1), slices,
+                                          {"bf16": 0, "fp8": 1}[fmt])
     if rc != 0:
         raise ValueError("oracle_split_fmm_dgemm: unsupported size or allocation failure")
     return C

@@ -211,7 +211,10 @@ static int o_exp_above(double b)
     return -1010 - __builtin_clzll(bits);
 }
 
-static void o_split_digits(double x, int E, int s, int* d)
+/* Balanced base-2^db digits of x relative to 2^E: X = round(x * 2^(db*s-E-1))
+ * (ties away from zero), then digits d[s-1..1] in [-2^(db-1), 2^(db-1)) from
+ * the bottom and the rest in d[0]. db = 8: BF16 slices; db = 5: FP8-E4M3. */
+static void o_split_digits(double x, int E, int s, int db, int* d)
 {
     uint64_t bits;
     memcpy(&bits, &x, 8);
@@ -220,16 +223,17 @@ static void o_split_digits(double x, int E, int s, int* d)
     uint64_t mant = bits & 0x000fffffffffffffull;
     int ex;
     if (bexp == 0) ex = -1074; else { mant |= 0x0010000000000000ull; ex = bexp - 1075; }
-    int sh = ex + 8 * s - E - 1;
+    int sh = ex + db * s - E - 1;
     int64_t X;
     if (mant == 0 || sh < -62) X = 0;
     else if (sh >= 0) X = (int64_t)(mant << sh);
     else X = (int64_t)((mant + (1ull << (-sh - 1))) >> (-sh));
     if (neg) X = -X;
+    const int64_t half = (int64_t)1 << (db - 1), mask = ((int64_t)1 << db) - 1;
     for (int t = s - 1; t >= 1; --t) {
-        int dd = (int)((X + 128) & 255) - 128;
+        int dd = (int)(((X + half) & mask) - half);
         d[t] = dd;
-        X = (X - dd) >> 8;
+        X = (X - dd) >> db;
     }
     d[0] = (int)X;
 }
@@ -249,20 +253,23 @@ static double o_scale2(double v, int e)
     return v * o_pow2(e);
 }
 
-/* C := beta*C + alpha*A*B through the split form with `s` slices (2..8).
- * Returns 0, or -1 on allocation failure / unsupported size. */
-int oracle_split_fmm_dgemm(int mt, int kt, int nt, int R,
-                           const int* U, const int* V, const int* W,
-                           int64_t m, int64_t n, int64_t k, double alpha,
-                           const double* A, int64_t lda, const double* B, int64_t ldb,
-                           double beta, double* C, int64_t ldc, int s)
+/* C := beta*C + alpha*A*B through the split form with `s` slices: fmt 0 =
+ * BF16 digits (base 256, s = 2..8), fmt 1 = FP8-E4M3 digits (base 32,
+ * s = 2..12). Returns 0, or -1 on allocation failure / unsupported size. */
+int oracle_split_fmm_dgemm_fmt(int mt, int kt, int nt, int R,
+                               const int* U, const int* V, const int* W,
+                               int64_t m, int64_t n, int64_t k, double alpha,
+                               const double* A, int64_t lda, const double* B, int64_t ldb,
+                               double beta, double* C, int64_t ldc, int s, int fmt)
 {
     if (beta != 1.0)
         for (int64_t j = 0; j < n; ++j)
             for (int64_t i = 0; i < m; ++i)
                 C[i + j * ldc] = beta == 0.0 ? 0.0 : beta * C[i + j * ldc];
     if (m == 0 || n == 0 || k == 0 || alpha == 0.0) return 0;
-    if (s < 2 || s > 8) return -1;
+    if (fmt != 0 && fmt != 1) return -1;
+    const int db = fmt ? 5 : 8;               /* digit bits */
+    if (s < 2 || s > (fmt ? 12 : 8)) return -1;
     const int64_t me = (m + mt - 1) / mt, ke = (k + kt - 1) / kt, ne = (n + nt - 1) / nt;
     if (ke > 16384) return -1;
     double* amax = (double*)calloc((size_t)(kt * m), sizeof(double));
@@ -274,9 +281,10 @@ int oracle_split_fmm_dgemm(int mt, int kt, int nt, int R,
     int16_t* DA = (int16_t*)malloc(sizeof(int16_t) * (size_t)(s * me * ke)); /* [t][p][i] */
     int16_t* DB = (int16_t*)malloc(sizeof(int16_t) * (size_t)(s * ke * ne)); /* [u][j][p] */
     int64_t* Z = (int64_t*)malloc(sizeof(int64_t) * (size_t)(me * ne));
-    /* Z counts in units of level G: 6, or 7 when the padded k is <= 128 */
+    /* Z counts in units of level G: BF16 6, or 7 when the padded k is <= 128;
+     * FP8 s + 1 up to 10 (exact for s <= 9) */
     const int64_t k_pad = (ke + 63) / 64 * 64;
-    const int G = k_pad <= 128 ? 7 : 6;
+    const int G = fmt ? (s + 1 < 10 ? s + 1 : 10) : (k_pad <= 128 ? 7 : 6);
     if (!amax || !bmax || !Er || !Fc || !S || !T || !DA || !DB || !Z) {
         free(amax); free(bmax); free(Er); free(Fc); free(S); free(T); free(DA); free(DB); free(Z);
         return -1;
@@ -366,14 +374,14 @@ int oracle_split_fmm_dgemm(int mt, int kt, int nt, int R,
         /* digits */
         for (int64_t p = 0; p < ke; ++p)
             for (int64_t i = 0; i < me; ++i) {
-                int d[8];
-                o_split_digits(S[i + p * me], Er[i], s, d);
+                int d[12];
+                o_split_digits(S[i + p * me], Er[i], s, db, d);
                 for (int t = 0; t < s; ++t) DA[((size_t)t * ke + p) * me + i] = (int16_t)d[t];
             }
         for (int64_t j = 0; j < ne; ++j)
             for (int64_t p = 0; p < ke; ++p) {
-                int d[8];
-                o_split_digits(T[p + j * ke], Fc[j], s, d);
+                int d[12];
+                o_split_digits(T[p + j * ke], Fc[j], s, db, d);
                 for (int t = 0; t < s; ++t) DB[((size_t)t * ne + j) * ke + p] = (int16_t)d[t];
             }
         /* level sums folded into Z (units of level G) */
@@ -395,9 +403,9 @@ int oracle_split_fmm_dgemm(int mt, int kt, int nt, int R,
                     }
                 }
                 for (int64_t i = 0; i < me; ++i) {
-                    if (g <= G) Z[i + j * me] += lv[i] * ((int64_t)1 << (8 * (G - g)));
+                    if (g <= G) Z[i + j * me] += lv[i] * ((int64_t)1 << (db * (G - g)));
                     else {
-                        int sh = 8 * (g - G);
+                        int sh = db * (g - G);
                         Z[i + j * me] += (lv[i] + ((int64_t)1 << (sh - 1))) >> sh;
                     }
                 }
@@ -414,7 +422,7 @@ int oracle_split_fmm_dgemm(int mt, int kt, int nt, int R,
             double lam = alpha * (double)w;
             for (int64_t j = 0; j < cl; ++j)
                 for (int64_t i = 0; i < rl; ++i) {
-                    double v = o_scale2((double)Z[i + j * me], Er[i] + Fc[j] + 2 - 8 * G);
+                    double v = o_scale2((double)Z[i + j * me], Er[i] + Fc[j] + 2 - db * G);
                     double* c = C + ro + i + (co + j) * ldc;
                     *c = fma(lam, v, *c);
                 }
@@ -422,4 +430,14 @@ int oracle_split_fmm_dgemm(int mt, int kt, int nt, int R,
     }
     free(amax); free(bmax); free(Er); free(Fc); free(S); free(T); free(DA); free(DB); free(Z);
     return 0;
+}
+
+/* BF16 split form (fmt 0) */
+int oracle_split_fmm_dgemm(int mt, int kt, int nt, int R,
+                           const int* U, const int* V, const int* W,
+                           int64_t m, int64_t n, int64_t k, double alpha,
+                           const double* A, int64_t lda, const double* B, int64_t ldb,
+                           double beta, double* C, int64_t ldc, int s)
+{
+    return oracle_split_fmm_dgemm_fmt(mt, kt, nt, R, U, V, W, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, s, 0);
 }

@@ -98,3 +98,25 @@ def test_split_oracle_zero_and_tiny(orc, algs):
     A = rand(9, 7, 5) * 1e-300
     out = orc.split_fmm_dgemm(algs["222"], A, B, np.zeros((9, 5), order="F"), 7)
     assert np.max(np.abs(out - A @ B)) <= 1e-13 * np.max(np.abs(A @ B)) + 1e-320
+
+
+def test_split_oracle_fp8_digits(orc, algs):
+    """FP8-E4M3 slices (base-32 digits): about 5 bits per slice, the error
+    falls with every slice and reaches the FP64 FMM's level at 11-12 slices."""
+    rng = np.random.default_rng(41)
+    m, n, k = 60, 70, 90
+    A = np.asfortranarray(rng.uniform(-1, 1, (m, k)))
+    B = np.asfortranarray(rng.uniform(-1, 1, (k, n)))
+    ref = A @ B
+    errs = []
+    for s in range(3, 13):
+        C = np.zeros((m, n), order="F")
+        orc.split_fmm_dgemm(algs["222"], A, B, C, s, fmt="fp8")
+        errs.append(float(np.abs(C - ref).max()))
+    assert all(a > b for a, b in zip(errs[:-3], errs[1:-2]))
+    assert errs[-1] < 1e-13
+    # s = 6 BF16 (48 bits) and s = 10 FP8 (50 bits) are of the same order
+    C = np.zeros((m, n), order="F")
+    orc.split_fmm_dgemm(algs["222"], A, B, C, 6)
+    e_bf16 = float(np.abs(C - ref).max())
+    assert errs[10 - 3] < 4 * e_bf16
