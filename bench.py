@@ -395,7 +395,7 @@ def run_batch(args, fmm, dev, world, rank, barrier, max_over_ranks):
     results = {}
     for form in ("split", "fp64"):
         plans = [tuner.plan(m, n, k, form, args.target) for m, n, k in shapes]
-        probs = [{"A": A, "B": B, "C": C, "fmm": alg(p.alg), "levels": p.levels, "slices": p.slices}
+        probs = [{"A": A, "B": B, "C": C, "fmm": alg(p.alg), "levels": p.levels, "slices": p.slices, "fmt": p.fmt}
                  for (A, B, C), p in zip(ops, plans)]
         arr = fmm.make_batch(probs)
         need = fmm.batch_workspace_size(arr)
@@ -419,7 +419,7 @@ def run_batch(args, fmm, dev, world, rank, barrier, max_over_ranks):
         gemm_ms, gemm_n, _ = fmm.read_kernel_timing()
         hist = {}
         for p in plans:
-            key = f"{p.alg}x{p.levels}" + (f"/s{p.slices}" if p.slices else "")
+            key = f"{p.alg}x{p.levels}" + (f"/{p.fmt}{p.slices}" if p.slices else "")
             hist[key] = hist.get(key, 0) + 1
         results[form] = {"ms": ms, "tflops": world * flops / (ms / 1e3) / 1e12, "steps": steps,
                          "launches_per_step": (fmm.launch_count() - n0) / steps, "plans": hist,
@@ -435,7 +435,7 @@ def run_batch(args, fmm, dev, world, rank, barrier, max_over_ranks):
         p = tuner.plan(m, n, k, "split", args.target)
         C1 = torch.zeros((n, m), dtype=torch.float64, device=dev).t()
         C2 = torch.zeros((n, m), dtype=torch.float64, device=dev).t()
-        fmm.split_dgemm(A, B, C1, alg(p.alg), p.levels, p.slices)
+        fmm.split_dgemm(A, B, C1, alg(p.alg), p.levels, p.slices, fmt=p.fmt)
         fmm.dgemm(A, B, C2, None, 0)
         torch.cuda.synchronize()
         errs.append(float((C1 - C2).abs().max() / C2.abs().max()))

@@ -89,23 +89,23 @@ class _GraphSlot:
     """A zero-padded operand set of one bucket shape and the graph of one
     levels-0 split call over it."""
 
-    def __init__(self, torch, fmm, dev, bm, bn, bk, slices, stream):
+    def __init__(self, torch, fmm, dev, bm, bn, bk, slices, fmt, stream):
         self.bm, self.bn, self.bk = bm, bn, bk
         self.stream = stream
         self.A = torch.zeros((bk, bm), dtype=torch.float64, device=dev).t()
         self.B = torch.zeros((bn, bk), dtype=torch.float64, device=dev).t()
         self.C = torch.zeros((bn, bm), dtype=torch.float64, device=dev).t()
-        self.ws = torch.empty(max(fmm.split_workspace_size(bm, bn, bk, None, 0, slices), 256),
+        self.ws = torch.empty(max(fmm.split_workspace_size(bm, bn, bk, None, 0, slices, fmt), 256),
                               dtype=torch.uint8, device=dev)
         self.busy_event = None
         with torch.cuda.stream(stream):
             # warm-up outside capture: tables, attributes, device error word
-            fmm.split_dgemm(self.A, self.B, self.C, None, 0, slices, workspace=self.ws, stream=stream)
+            fmm.split_dgemm(self.A, self.B, self.C, None, 0, slices, workspace=self.ws, stream=stream, fmt=fmt)
         torch.cuda.synchronize()
         self.graph = torch.cuda.CUDAGraph()
         with torch.cuda.graph(self.graph, stream=stream):
             fmm.split_dgemm(self.A, self.B, self.C, None, 0, slices, workspace=self.ws,
-                            stream=torch.cuda.current_stream())
+                            stream=torch.cuda.current_stream(), fmt=fmt)
         torch.cuda.synchronize()
 
 
@@ -154,13 +154,13 @@ class Server:
         p = r.plan
         if p.form == "fp64":
             return 4096
-        return self.fmm.batch_problem_workspace_size(r.m, r.n, r.k, self._alg(p.alg), p.levels, p.slices)
+        return self.fmm.batch_problem_workspace_size(r.m, r.n, r.k, self._alg(p.alg), p.levels, p.slices, p.fmt)
 
     def _graph_bucket(self, r: Request):
         p = r.plan
         if p.form != "split" or p.levels != 0 or max(r.m, r.n, r.k) > self.graph_max_dim:
             return None
-        return (_bucket(r.m), _bucket(r.n), _bucket(r.k), p.slices)
+        return (_bucket(r.m), _bucket(r.n), _bucket(r.k), p.slices, p.fmt)
 
     # -------------------------------------------------------------- API
     def submit(self, r: Request) -> Request:
@@ -226,7 +226,7 @@ class Server:
             ws = None
             if direct:
                 probs = [{"A": r._A, "B": r._B, "C": r.C, "fmm": self._alg(r.plan.alg), "levels": r.plan.levels,
-                          "slices": r.plan.slices} for r in direct]
+                          "slices": r.plan.slices, "fmt": r.plan.fmt} for r in direct]
                 arr = self.fmm.make_batch(probs)
                 need = self.fmm.batch_workspace_size(arr)
                 ws = torch.empty(max(need, 256), dtype=torch.uint8, device=self.dev)
@@ -243,8 +243,8 @@ class Server:
         torch = self.torch
         slots = self._slots.get(bucket)
         if slots is None:
-            bm, bn, bk, s = bucket
-            slots = [_GraphSlot(torch, self.fmm, self.dev, bm, bn, bk, s, torch.cuda.Stream(device=self.dev))
+            bm, bn, bk, s, fmt = bucket
+            slots = [_GraphSlot(torch, self.fmm, self.dev, bm, bn, bk, s, fmt, torch.cuda.Stream(device=self.dev))
                      for _ in range(self.graph_slots)]
             self._slots[bucket] = slots
         slot = None

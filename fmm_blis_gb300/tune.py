@@ -24,9 +24,12 @@ Cost model (calibrated on GB300 at m = n = k = 16384, SM clock 1.8-2.07 GHz):
     element, the row/column maxima one read of A and B.
 
 Error model (split form, uniform-like inputs): the max-norm error relative to
-max|C| of s slices is about 0.4 * 2^-8s * sqrt(k) * 1.5^levels (222 two
-levels, 6 slices, k = 16384: 1.7e-13 measured). The tuner keeps a safety
-factor of 4 on it.
+max|C| of s slices of db-bit digits is about 0.4 * 2^(-db*s) * sqrt(k) *
+1.5^levels (222 two levels, k = 16384: 6 BF16 slices 1.6e-13 measured, 4.1e-13
+modelled; 10 FP8 slices 5.8e-14 / 1.0e-13). The tuner keeps a safety factor
+of 4 on it. FP8-E4M3 slices (db = 5) run a slice pair at twice the BF16 rate
+but at about 10% lower SM clock under the power cap (GEMM 2788 vs 1477
+TFLOP/s executed at 1.67 vs 1.83 GHz): a pair costs 0.55 of a BF16 pair.
 """
 from __future__ import annotations
 
@@ -47,6 +50,9 @@ LAUNCH_S = 4e-6
 ERR_C0 = 0.4
 ERR_LEVEL_GROWTH = 1.5
 ERR_SAFETY = 4.0
+FP8_PAIR_COST = 0.55
+DIGIT_BITS = {"bf16": 8, "fp8": 5}
+SLICE_RANGE = {"bf16": (3, 8), "fp8": (3, 12)}
 
 
 def _cdiv(a: int, b: int) -> int:
@@ -103,6 +109,7 @@ class Plan:
     slices: int                # 0 for the FP64 form
     est_s: float               # modelled device time
     est_rel_err: float | None  # modelled max-norm error / max|C| (split form)
+    fmt: str = "bf16"          # slice format of the split form: "bf16" or "fp8"
     candidates: list = field(default_factory=list, repr=False)
 
 
@@ -114,21 +121,24 @@ def fp64_time(a: AlgShape, m: int, n: int, k: int) -> float:
     return per_sm * 2048.0 * ke * a.R / CLOCK_HZ / FP64_EFF * pack + 2 * LAUNCH_S
 
 
-def split_time(a: AlgShape, m: int, n: int, k: int, s: int) -> float:
+def split_time(a: AlgShape, m: int, n: int, k: int, s: int, fmt: str = "bf16") -> float:
     me, ne, ke = _cdiv(m, a.mt), _cdiv(n, a.nt), _cdiv(k, a.kt)
-    m_pad, n_pad, k_pad = _round_up(max(me, 1), 128), _round_up(max(ne, 1), 256), _round_up(max(ke, 1), 64)
+    kbe = 128 if fmt == "fp8" else 64        # k elements per 128-byte stage row
+    m_pad, n_pad, k_pad = _round_up(max(me, 1), 128), _round_up(max(ne, 1), 256), _round_up(max(ke, 1), kbe)
     items = a.R * (m_pad // 128) * (n_pad // 256)
     waves = _cdiv(items, SMS)
     pairs = s * (s + 1) // 2
     gemm = waves * pairs * (k_pad // 64) * 512.0 / (CLOCK_HZ * SPLIT_EFF)
+    if fmt == "fp8":
+        gemm *= FP8_PAIR_COST
     pack = a.R * (m_pad + n_pad) * k_pad * s * PACK_S_PER_ELEM_SLICE
     scatter = a.nnz_w * me * ne * SCATTER_S_PER_ENTRY_ELEM
     maxima = 8.0 * (m * k + k * n) / HBM_BPS
     return gemm + pack + scatter + maxima + 7 * LAUNCH_S
 
 
-def split_rel_err(a: AlgShape, k: int, s: int) -> float:
-    return ERR_C0 * 2.0 ** (-8 * s) * math.sqrt(max(k, 1)) * ERR_LEVEL_GROWTH ** a.levels
+def split_rel_err(a: AlgShape, k: int, s: int, fmt: str = "bf16") -> float:
+    return ERR_C0 * 2.0 ** (-DIGIT_BITS[fmt] * s) * math.sqrt(max(k, 1)) * ERR_LEVEL_GROWTH ** a.levels
 
 
 def _fits(a: AlgShape, m: int, n: int, k: int, min_block: int) -> bool:
@@ -144,11 +154,11 @@ class Tuner:
     one served alone."""
 
     def __init__(self, algs: list[AlgShape] | None = None, min_block_fp64: int = 256,
-                 min_block_split: int = 1024, slice_range=(3, 8)):
+                 min_block_split: int = 1024, formats=("bf16", "fp8")):
         self.algs = algs if algs is not None else alg_shapes()
         self.min_block_fp64 = min_block_fp64
         self.min_block_split = min_block_split
-        self.slice_range = slice_range
+        self.formats = tuple(formats)
         self.cache: dict = {}
 
     def plan(self, m: int, n: int, k: int, form: str = "split", target_rel_err: float = 1e-10) -> Plan:
@@ -164,11 +174,13 @@ class Tuner:
             else:
                 if not _fits(a, m, n, k, self.min_block_split):
                     continue
-                for s in range(self.slice_range[0], self.slice_range[1] + 1):
-                    err = split_rel_err(a, k, s)
-                    if err * ERR_SAFETY <= target_rel_err:
-                        cands.append(Plan("split", a.name, a.levels, s, split_time(a, m, n, k, s), err))
-                        break
+                for fmt in self.formats:
+                    lo, hi = SLICE_RANGE[fmt]
+                    for s in range(lo, hi + 1):
+                        err = split_rel_err(a, k, s, fmt)
+                        if err * ERR_SAFETY <= target_rel_err:
+                            cands.append(Plan("split", a.name, a.levels, s, split_time(a, m, n, k, s, fmt), err, fmt))
+                            break
         if not cands:
             raise ValueError(f"no plan meets the target for m={m} n={n} k={k} form={form} "
                              f"target={target_rel_err}")

@@ -50,7 +50,7 @@ def direct(fmm, torch, r, algs):
     if p.form == "fp64":
         fmm.dgemm(A, B, C, f, p.levels)
     else:
-        fmm.split_dgemm(A, B, C, f, p.levels, p.slices)
+        fmm.split_dgemm(A, B, C, f, p.levels, p.slices, fmt=p.fmt)
     torch.cuda.synchronize()
     return host(C)
 

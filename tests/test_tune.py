@@ -73,3 +73,18 @@ def test_batch_sizing_needs_no_gpu():
     sizes = [fmm.batch_problem_workspace_size(1000, 900, 800, f, 1, s) for s in (3, 5, 7)]
     assert 0 < sizes[0] < sizes[1] < sizes[2]
     assert fmm.batch_problem_workspace_size(100, 90, 80, None, 0, 5) > 0
+
+
+def test_slice_format_choice():
+    """Both slice formats are candidates; the FP8 error model uses 5 bits per
+    slice and its pair cost the measured 0.55 of a BF16 pair."""
+    t = tune.Tuner()
+    p = t.plan(16384, 16384, 16384, "split", 1e-10)
+    fmts = {c.fmt for c in p.candidates}
+    assert fmts == {"bf16", "fp8"}
+    fp8 = [c for c in p.candidates if c.fmt == "fp8"]
+    assert all(c.slices >= 8 for c in fp8)
+    only8 = tune.Tuner(formats=("fp8",)).plan(16384, 16384, 16384, "split", 1e-10)
+    assert only8.fmt == "fp8" and only8.est_rel_err * tune.ERR_SAFETY <= 1e-10
+    a = {(x.name, x.levels): x for x in tune.alg_shapes()}
+    assert tune.split_time(a[("222", 2)], 16384, 16384, 16384, 10, "fp8") == pytest.approx(0.157, rel=0.15)
