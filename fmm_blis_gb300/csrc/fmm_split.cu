@@ -1466,8 +1466,66 @@ static int split_launch_budget(const AlgView& alg, int64_t m, int64_t n, int64_t
  * covers all their (problem, product, tile) items, then each problem's C is
  * updated. A problem too large to share the workspace runs alone with
  * product groups. Every problem's result equals its single-call result. */
+/* Side streams for the per-problem work of a batch wave (maxima, exponents,
+ * packs, scatter): the small kernels of different problems overlap instead of
+ * queueing behind each other on the caller's stream. Created once per device;
+ * forked from and joined back to the caller's stream with events, which a
+ * stream capture follows. One batch at a time uses a pool (g_side_use). */
+constexpr int kSideStreams = 8;
+
+struct SidePool {
+    int device;
+    cudaStream_t s[kSideStreams];
+    cudaEvent_t fork;
+    cudaEvent_t join[kSideStreams];
+};
+
+std::mutex g_side_mu, g_side_use;
+std::vector<SidePool*> g_side;
+
+SidePool* side_pool()
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+    std::lock_guard<std::mutex> lk(g_side_mu);
+    for (SidePool* p : g_side)
+        if (p->device == dev) return p;
+    SidePool* p = new SidePool;
+    p->device = dev;
+    bool ok = cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming) == cudaSuccess;
+    for (int i = 0; i < kSideStreams && ok; ++i)
+        ok = cudaStreamCreateWithFlags(&p->s[i], cudaStreamNonBlocking) == cudaSuccess &&
+             cudaEventCreateWithFlags(&p->join[i], cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) {
+        cudaGetLastError();
+        return nullptr;   /* the batch then runs on the caller's stream alone */
+    }
+    g_side.push_back(p);
+    return p;
+}
+
+int side_fork(SidePool* p, cudaStream_t st)
+{
+    if (!p) return FMM_OK;
+    if (cudaEventRecord(p->fork, st) != cudaSuccess) return FMM_ERR_CUDA;
+    for (int i = 0; i < kSideStreams; ++i)
+        if (cudaStreamWaitEvent(p->s[i], p->fork, 0) != cudaSuccess) return FMM_ERR_CUDA;
+    return FMM_OK;
+}
+
+int side_join(SidePool* p, cudaStream_t st)
+{
+    if (!p) return FMM_OK;
+    for (int i = 0; i < kSideStreams; ++i)
+        if (cudaEventRecord(p->join[i], p->s[i]) != cudaSuccess || cudaStreamWaitEvent(st, p->join[i], 0) != cudaSuccess)
+            return FMM_ERR_CUDA;
+    return FMM_OK;
+}
+
 int fmm_split_batch(int count, const SplitJob* jobs_in, void* ws, size_t ws_bytes, cudaStream_t st)
 {
+    std::lock_guard<std::mutex> use(g_side_use);
+    SidePool* sp = side_pool();
     std::vector<SplitJob> jobs(jobs_in, jobs_in + count);
     std::vector<size_t> full(count, 0);
     for (int i = 0; i < count; ++i)
@@ -1507,14 +1565,18 @@ int fmm_split_batch(int count, const SplitJob* jobs_in, void* ws, size_t ws_byte
         size_t off = 0;
         int64_t items = 0;
         int prods = 0;
+        /* per-problem maxima, exponents and packs, spread over the side streams */
+        if (int rc = side_fork(sp, st); rc != FMM_OK) return rc;
         for (int q = i; q < e; ++q) {
             SplitJob& j = jobs[q];
+            cudaStream_t ss = sp ? sp->s[(q - i) % kSideStreams] : st;
             int rc = job_bind_group(j, (uint8_t*)ws + off, full[q], j.alg.R);
             if (rc != FMM_OK) return rc;
             off += (full[q] + 255) / 256 * 256;
-            if ((rc = job_prologue(j, st)) != FMM_OK) return rc;
-            if ((rc = job_pack(j, 0, j.alg.R, st)) != FMM_OK) return rc;
+            if ((rc = job_prologue(j, ss)) != FMM_OK) return rc;
+            if ((rc = job_pack(j, 0, j.alg.R, ss)) != FMM_OK) return rc;
         }
+        if (int rc = side_join(sp, st); rc != FMM_OK) return rc;
         /* work items of the costliest problems (slice pairs x k blocks per
          * item) first, so the CTAs' round-robin shares end evenly */
         std::vector<int> ord;
@@ -1533,7 +1595,10 @@ int fmm_split_batch(int count, const SplitJob* jobs_in, void* ws, size_t ws_byte
         }
         int rc = launch_gemm(gl, items, prods, st);
         if (rc != FMM_OK) return rc;
-        for (int q = i; q < e; ++q) job_scatter(jobs[q], 0, jobs[q].alg.R, st);
+        /* each problem's C update (disjoint C regions) on the side streams */
+        if ((rc = side_fork(sp, st)) != FMM_OK) return rc;
+        for (int q = i; q < e; ++q) job_scatter(jobs[q], 0, jobs[q].alg.R, sp ? sp->s[(q - i) % kSideStreams] : st);
+        if ((rc = side_join(sp, st)) != FMM_OK) return rc;
         i = e;
     }
     return cudaGetLastError() == cudaSuccess ? FMM_OK : FMM_ERR_CUDA;
