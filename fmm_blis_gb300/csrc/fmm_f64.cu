@@ -90,7 +90,8 @@ __device__ __forceinline__ void f64_tile(const int* __restrict__ tab, int64_t m,
                                          const double* __restrict__ B, int64_t ldb,
                                          double* __restrict__ C, int64_t ldc, int ti, int tj,
                                          double (&As)[BK][BM + 1], double (&Bs)[BK][BN + 1],
-                                         Entry* ue, Entry* ve)
+                                         Entry* ue, Entry* ve, int r_begin, int r_end,
+                                         const double* __restrict__ Sp, const double* __restrict__ Tp)
 {
     constexpr int NT = (BM / TM) * (BN / TN);
     constexpr int RT = BM / TM;  /* thread rows */
@@ -110,15 +111,31 @@ __device__ __forceinline__ void f64_tile(const int* __restrict__ tab, int64_t m,
     const int64_t i0 = (int64_t)ti * BM, j0 = (int64_t)tj * BN;
     const int tid = threadIdx.x;
     const int tr = tid % RT, tc = tid / RT;
+    /* With pre-formed operands (Sp/Tp: S_r, T_r of the products r_begin..,
+     * me x ke and ke x ne column-major) every product has one term of
+     * coefficient 1, read with those strides; its values are exactly what the
+     * fused pack forms. */
+    if (Sp) { lda = me; ldb = ke; }
+    (void)R;
 
-    for (int r = 0; r < R; ++r) {
+    for (int r = r_begin; r < r_end; ++r) {
         const int wb = w_off[r], we = w_off[r + 1];
         if (wb == we) continue;
-        const int ub = u_off[r], ue_n = u_off[r + 1] - ub;
-        const int vb = v_off[r], ve_n = v_off[r + 1] - vb;
+        int ue_n, ve_n;
         __syncthreads();  /* previous product finished with ue/ve */
-        stage_entries(u_ent, ub, ub + ue_n, kt, mt, A, lda, m, k, ue);
-        stage_entries(v_ent, vb, vb + ve_n, nt, kt, B, ldb, k, n, ve);
+        if (Sp) {
+            ue_n = ve_n = 1;
+            if (tid == 0) {
+                ue[0] = Entry{Sp + (int64_t)(r - r_begin) * me * ke, 1.0, (int)me, (int)ke, 0, 0};
+                ve[0] = Entry{Tp + (int64_t)(r - r_begin) * ke * ne, 1.0, (int)ke, (int)ne, 0, 0};
+            }
+        } else {
+            const int ub = u_off[r], vb = v_off[r];
+            ue_n = u_off[r + 1] - ub;
+            ve_n = v_off[r + 1] - vb;
+            stage_entries(u_ent, ub, ub + ue_n, kt, mt, A, lda, m, k, ue);
+            stage_entries(v_ent, vb, vb + ve_n, nt, kt, B, ldb, k, n, ve);
+        }
         __syncthreads();
 
         double acc[TM][TN];
@@ -236,14 +253,15 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN))
 fmm_f64_kernel(const int* __restrict__ tab, int64_t m, int64_t n, int64_t k,
                double alpha, const double* __restrict__ A, int64_t lda,
                const double* __restrict__ B, int64_t ldb,
-               double* __restrict__ C, int64_t ldc, int tiles_m)
+               double* __restrict__ C, int64_t ldc, int tiles_m, int r_begin, int r_end,
+               const double* __restrict__ Sp, const double* __restrict__ Tp)
 {
     __shared__ double As[BK][BM + 1];
     __shared__ double Bs[BK][BN + 1];
     __shared__ Entry ue[kMaxEntries];
     __shared__ Entry ve[kMaxEntries];
     f64_tile<BM, BN, BK, TM, TN>(tab, m, n, k, alpha, A, lda, B, ldb, C, ldc, (int)(blockIdx.x % tiles_m),
-                                 (int)(blockIdx.x / tiles_m), As, Bs, ue, ve);
+                                 (int)(blockIdx.x / tiles_m), As, Bs, ue, ve, r_begin, r_end, Sp, Tp);
 }
 
 /* ------------------------------------------------------------ batched -- */
@@ -333,7 +351,59 @@ fmm_f64_batch_kernel(const F64Prob* __restrict__ probs, int nprob, int64_t nitem
         }
         if (P.k == 0 || P.alpha == 0.0) continue;
         f64_tile<kF64Bm, kF64Bn, kF64Bk, kF64Tm, kF64Tn>(P.tab, P.m, P.n, P.k, P.alpha, P.A, P.lda, P.B, P.ldb,
-                                                        P.C, P.ldc, ti, tj, As, Bs, ue, ve);
+                                                        P.C, P.ldc, ti, tj, As, Bs, ue, ve, 0, P.tab[3],
+                                                        nullptr, nullptr);
+    }
+}
+
+/* Pre-formed operand combinations for the products r0 .. r0+np-1:
+ * S[q][i + p*me] = sum_e U[e,r] A_e[i,p] (A side) or T[q][p + j*ke] =
+ * sum_e V[e,r] B_e[p,j] (B side), zero past a smaller sub-block, summed
+ * exactly as the fused pack does (the first term's coefficient, then FMAs in
+ * entry order), so the GEMM over them gives the fused kernel's bits. One
+ * thread per element down a column (coalesced loads and stores); the product
+ * index runs fastest in the block order so the products at one position read
+ * their shared sub-blocks through L2 once. */
+template <bool A_SIDE>
+__global__ void __launch_bounds__(256)
+f64_combine_kernel(const int* __restrict__ tab, int r0, int np, const double* __restrict__ X, int64_t ldx,
+                   int64_t m, int64_t n, int64_t k, double* __restrict__ out)
+{
+    __shared__ Entry ent[kMaxEntries];
+    const int mt = tab[0], kt = tab[1], nt = tab[2], R = tab[3];
+    const int* u_off = tab + FMM_ALG_HDR;
+    const int* v_off = u_off + (R + 1);
+    const int* w_off = v_off + (R + 1);
+    const int* u_ent = w_off + (R + 1);
+    const int* v_ent = u_ent + 2 * u_off[R];
+    const int64_t me = (m + mt - 1) / mt, ne = (n + nt - 1) / nt, ke = (k + kt - 1) / kt;
+    const int64_t rows = A_SIDE ? me : ke, cols = A_SIDE ? ke : ne;
+    const int q = (int)(blockIdx.x % (unsigned)np), r = r0 + q;
+    const int64_t i = (int64_t)(blockIdx.x / (unsigned)np) * blockDim.x + threadIdx.x;
+    int ne_;
+    if (A_SIDE) {
+        ne_ = u_off[r + 1] - u_off[r];
+        stage_entries(u_ent, u_off[r], u_off[r + 1], kt, mt, X, ldx, m, k, ent);
+    } else {
+        ne_ = v_off[r + 1] - v_off[r];
+        stage_entries(v_ent, v_off[r], v_off[r + 1], nt, kt, X, ldx, k, n, ent);
+    }
+    __syncthreads();
+    if (i >= rows) return;
+    double* o = out + (int64_t)q * rows * cols;
+    for (int64_t c = blockIdx.y; c < cols; c += gridDim.y) {
+        double sv[1] = {0.0};
+        if (ne_ > 0) {
+            const Entry& x0 = ent[0];
+            sv[0] = (i < x0.rows && c < x0.cols) ? x0.base[i + c * ldx] : 0.0;
+            scale_first(x0, sv);
+        }
+        for (int e = 1; e < ne_; ++e) {
+            const Entry& x = ent[e];
+            const double v = (i < x.rows && c < x.cols) ? x.base[i + c * ldx] : 0.0;
+            sv[0] = fma(x.coef, v, sv[0]);
+        }
+        o[i + c * rows] = sv[0];
     }
 }
 
@@ -351,16 +421,31 @@ __global__ void scale_c_kernel(int64_t m, int64_t n, double beta, double* C, int
 template <int BM, int BN, int BK, int TM, int TN>
 int launch_cfg(const AlgView& alg, int64_t m, int64_t n, int64_t k, double alpha,
                const double* A, int64_t lda, const double* B, int64_t ldb, double* C,
-               int64_t ldc, cudaStream_t st)
+               int64_t ldc, int r_begin, int r_end, const double* Sp, const double* Tp, cudaStream_t st)
 {
     const int64_t me = (m + alg.mt - 1) / alg.mt, ne = (n + alg.nt - 1) / alg.nt;
     const int64_t tm = (me + BM - 1) / BM, tn = (ne + BN - 1) / BN;
     if (tm * tn > 0x7fffffffLL) return FMM_ERR_UNSUPPORTED;
     fmm_f64_kernel<BM, BN, BK, TM, TN><<<(unsigned)(tm * tn), (BM / TM) * (BN / TN), 0, st>>>(
-        alg.tab, m, n, k, alpha, A, lda, B, ldb, C, ldc, (int)tm);
+        alg.tab, m, n, k, alpha, A, lda, B, ldb, C, ldc, (int)tm, r_begin, r_end, Sp, Tp);
     fmm_count_launch(1);
     return cudaGetLastError() == cudaSuccess ? FMM_OK : FMM_ERR_CUDA;
 }
+
+int launch_pick(int pick, const AlgView& alg, int64_t m, int64_t n, int64_t k, double alpha, const double* A,
+                int64_t lda, const double* B, int64_t ldb, double* C, int64_t ldc, int r_begin, int r_end,
+                const double* Sp, const double* Tp, cudaStream_t st)
+{
+    switch (pick) {
+    case 3: return launch_cfg<64, 64, 32, 4, 4>(alg, m, n, k, alpha, A, lda, B, ldb, C, ldc, r_begin, r_end, Sp, Tp, st);
+    case 4: return launch_cfg<128, 64, 16, 8, 4>(alg, m, n, k, alpha, A, lda, B, ldb, C, ldc, r_begin, r_end, Sp, Tp, st);
+    case 5: return launch_cfg<64, 128, 16, 4, 8>(alg, m, n, k, alpha, A, lda, B, ldb, C, ldc, r_begin, r_end, Sp, Tp, st);
+    default: return launch_cfg<32, 32, 32, 2, 2>(alg, m, n, k, alpha, A, lda, B, ldb, C, ldc, r_begin, r_end, Sp, Tp, st);
+    }
+}
+
+/* bytes of pre-formed operands a product group may hold at once */
+constexpr size_t kPrepackBudget = (size_t)4 << 30;
 
 }  // namespace
 
@@ -394,7 +479,13 @@ int fmm_f64_launch(const AlgView& alg, int64_t m, int64_t n, int64_t k, double a
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int64_t me = (m + alg.mt - 1) / alg.mt, ne = (n + alg.nt - 1) / alg.nt;
+    const int64_t me = (m + alg.mt - 1) / alg.mt, ne = (n + alg.nt - 1) / alg.nt, ke = (k + alg.kt - 1) / alg.kt;
+    /* FMM algorithms form each product's operand combinations once, ahead of
+     * the tiles (a stream-ordered temporary of at most kPrepackBudget per
+     * product group), instead of once per tile position inside the kernel;
+     * the values, and so the results, are the same either way. */
+    const bool prepack = alg.R > 1;
+    const double nu = prepack ? 1.0 : alg.avg_nnz_u, nv = prepack ? 1.0 : alg.avg_nnz_v;
     struct Cand { int id, bm, bn; double eff; };
     const Cand cands[4] = {{3, 64, 64, 1.0}, {4, 128, 64, 0.99}, {5, 64, 128, 0.99}, {2, 32, 32, 0.8}};
     double best = 0;
@@ -403,17 +494,33 @@ int fmm_f64_launch(const AlgView& alg, int64_t m, int64_t n, int64_t k, double a
         const int64_t bm = cands[c].bm, bn = cands[c].bn;
         const int64_t tiles = ((me + bm - 1) / bm) * ((ne + bn - 1) / bn);
         const double waves = (double)((tiles + 2 * (int64_t)sms - 1) / (2 * (int64_t)sms));
-        const double work = (double)(bm * bn) * (1.0 + (alg.avg_nnz_u - 1.0) / (double)bn +
-                                                 (alg.avg_nnz_v - 1.0) / (double)bm + 4.0 / (double)bm);
+        const double work = (double)(bm * bn) * (1.0 + (nu - 1.0) / (double)bn + (nv - 1.0) / (double)bm +
+                                                 4.0 / (double)bm);
         const double est = waves * work / cands[c].eff;
         if (c == 0 || est < best) { best = est; pick = cands[c].id; }
     }
-    switch (pick) {
-    case 3: return launch_cfg<64, 64, 32, 4, 4>(alg, m, n, k, alpha, A, lda, B, ldb, C, ldc, st);
-    case 4: return launch_cfg<128, 64, 16, 8, 4>(alg, m, n, k, alpha, A, lda, B, ldb, C, ldc, st);
-    case 5: return launch_cfg<64, 128, 16, 4, 8>(alg, m, n, k, alpha, A, lda, B, ldb, C, ldc, st);
-    default: return launch_cfg<32, 32, 32, 2, 2>(alg, m, n, k, alpha, A, lda, B, ldb, C, ldc, st);
+    if (prepack) {
+        const size_t per = (size_t)(me * ke + ke * ne) * sizeof(double);
+        const int G = (int)std::max<size_t>(1, std::min<size_t>((size_t)alg.R, kPrepackBudget / std::max<size_t>(per, 1)));
+        void* buf = nullptr;
+        if (cudaMallocAsync(&buf, (size_t)G * per, st) == cudaSuccess) {
+            double* Sbuf = (double*)buf;
+            double* Tbuf = Sbuf + (size_t)G * me * ke;
+            for (int r0 = 0; r0 < alg.R && rc == FMM_OK; r0 += G) {
+                const int np = std::min(G, alg.R - r0);
+                f64_combine_kernel<true><<<dim3((unsigned)(np * ((me + 255) / 256)), (unsigned)std::min<int64_t>(ke, 65535)),
+                                           256, 0, st>>>(alg.tab, r0, np, A, lda, m, n, k, Sbuf);
+                f64_combine_kernel<false><<<dim3((unsigned)(np * ((ke + 255) / 256)), (unsigned)std::min<int64_t>(ne, 65535)),
+                                            256, 0, st>>>(alg.tab, r0, np, B, ldb, m, n, k, Tbuf);
+                fmm_count_launch(2);
+                rc = launch_pick(pick, alg, m, n, k, alpha, A, lda, B, ldb, C, ldc, r0, r0 + np, Sbuf, Tbuf, st);
+            }
+            if (cudaFreeAsync(buf, st) != cudaSuccess && rc == FMM_OK) rc = FMM_ERR_CUDA;
+            return rc;
+        }
+        cudaGetLastError();   /* no temporary: the combinations stay fused into the kernel */
     }
+    return launch_pick(pick, alg, m, n, k, alpha, A, lda, B, ldb, C, ldc, 0, alg.R, nullptr, nullptr, st);
 }
 
 /* Workspace of a batched FP64 launch: the work counter and the problem table. */
