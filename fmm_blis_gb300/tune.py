@@ -12,10 +12,11 @@ meets the requested relative error.
 Cost model (calibrated on GB300 at m = n = k = 16384, SM clock 1.8-2.07 GHz):
   FP64 form: a CTA per 64 x 64 tile position of the product grid runs all
     R products over it, the CTAs of an SM share its FP64 pipe (2 FMA/clk):
-    time = ceil(tiles / SMs) * 2048 * k_e * R / clock / 0.98, times
-    1 + 1.5 ((nnz(U)-1) + (nnz(V)-1)) / 64 for the fused pack sums.
-    (16384^3: classical 7.03 s measured, 7.14 s modelled; 222 one level
-    6.40 / 6.45 s; 222 two levels 6.14 / 5.97 s.)
+    time = ceil(tiles / SMs) * 2048 * k_e * R / clock / 0.98, plus, for FMM
+    algorithms, one HBM write and read of every product's operand
+    combinations (formed once ahead of the tiles). (16384^3: classical
+    7.03 s measured, 7.14 s modelled; 444 two levels 5.24 / 4.96 s;
+    333 two levels 5.86 / 5.55 s.)
   Split form: the persistent tcgen05 GEMM runs (problem, product, 128 x 256
     tile) items on 152 CTAs, each item s(s+1)/2 slice pairs x k_pad/64 blocks
     of 512 MMA clocks at about 61% of 2.07 GHz under the power cap
@@ -117,8 +118,13 @@ def fp64_time(a: AlgShape, m: int, n: int, k: int) -> float:
     me, ne, ke = _cdiv(m, a.mt), _cdiv(n, a.nt), _cdiv(k, a.kt)
     tiles = _cdiv(me, 64) * _cdiv(ne, 64)
     per_sm = _cdiv(tiles, SMS)
-    pack = 1.0 + 1.5 * ((a.nnz_u - 1.0) + (a.nnz_v - 1.0)) / 64
-    return per_sm * 2048.0 * ke * a.R / CLOCK_HZ / FP64_EFF * pack + 2 * LAUNCH_S
+    gemm = per_sm * 2048.0 * ke * a.R / CLOCK_HZ / FP64_EFF
+    if a.R == 1:
+        return gemm + 2 * LAUNCH_S
+    # FMM: each product's operand combinations are formed once ahead of the
+    # tiles (written, then read back: HBM), so the tiles see single-term operands
+    combine = a.R * (me * ke + ke * ne) * 8.0 * 2.0 / HBM_BPS
+    return gemm + combine + 4 * LAUNCH_S
 
 
 def split_time(a: AlgShape, m: int, n: int, k: int, s: int, fmt: str = "bf16") -> float:
