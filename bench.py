@@ -144,6 +144,25 @@ def dist_setup():
     return world, rank, local
 
 
+def rank_barrier(world: int) -> None:
+    """All ranks meet (replicas: no data-path collective, only timing)."""
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def rank_max(x: float, world: int, device) -> float:
+    """The largest of the ranks' values (the slowest replica's time): one
+    all-reduce of a float64 on `device` (cuda under NCCL, cpu under gloo)."""
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def host_operands(n, seed=7):
     """Column-major float64 host operands (torch's CPU generator, seeded)."""
     import torch
@@ -608,17 +627,10 @@ def main():
     flops = 2.0 * n ** 3
 
     def barrier():
-        if world > 1:
-            import torch.distributed as dist
-            dist.barrier()
+        rank_barrier(world)
 
     def max_over_ranks(x: float) -> float:
-        if world == 1:
-            return x
-        import torch.distributed as dist
-        t = torch.tensor([x], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return rank_max(x, world, dev)
 
     if args.workload == "batch":
         run_batch(args, fmm, dev, world, rank, barrier, max_over_ranks)
