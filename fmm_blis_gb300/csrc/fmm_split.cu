@@ -67,7 +67,7 @@ namespace {
 
 constexpr int kTileM = 128;
 constexpr int kTileN = 256;             /* N = 256: 128 clocks per MMA hide the accumulator dependency */
-constexpr int kBK = 64;                 /* k elements per stage (128 bytes of BF16) */
+constexpr int kBK = 64;                 /* BF16 k elements per stage (128 bytes; 128 FP8 elements) */
 constexpr int kStages = 4;
 constexpr int kChunkKB = 16;            /* k-blocks per exact FP32 chunk: 1024 terms, |sum| <= 2^24 */
 constexpr int kEpiWarps = 16;          /* four per TMEM lane quarter */
@@ -675,8 +675,9 @@ __device__ __forceinline__ Item decode_item(const GemmLaunch& L, int b)
 /* Persistent GEMM over a list of work items (problem, product of its group,
  * 128 x 256 output tile); CTA c takes items c, c + gridDim.x, ... One CTA per
  * SM: warp 0 issues the TMA loads of the digit-slice tiles, warp 1 the
- * tcgen05.mma (M=128, N=256, K=16: 128 clocks per MMA hide the accumulator
- * dependency), warps 2..17 drain each exact 1024-term chunk from the
+ * tcgen05.mma (M=128, N=256, K=16 BF16 or K=32 FP8 per the item's problem:
+ * 128 clocks per MMA hide the accumulator dependency), warps 2..17 drain
+ * each exact chunk (16 stage rows: 1024 BF16 or 2048 FP8 terms) from the
  * double-buffered TMEM accumulator into int32 level sums and fold finished
  * levels into the product's 64-bit Z tile in global memory. The pipeline,
  * TMEM allocation and barrier phases run on across items, so one item's last
@@ -1077,10 +1078,9 @@ PFN_cuTensorMapEncodeTiled_v12000 get_encode_fn()
     return fn;
 }
 
-/* 2-D map over slices[rows_total][k_pad] BF16, box 64 (k) x 128 (rows),
+/* 2-D map over slices[rows_total][k_pad] of BF16 (fmt 0) or FP8-E4M3 bytes
+ * (fmt 1): boxes one 128-byte row of k (64 or 128 elements) by box_rows rows,
  * 128-byte swizzle. */
-/* 2-D map over slices[rows_total][k_pad] BF16, box 64 (k) x box_rows, 128-byte
- * swizzle. */
 int make_slice_map(CUtensorMap* map, const void* base, int64_t k_pad, int64_t rows_total, int box_rows, int fmt)
 {
     PFN_cuTensorMapEncodeTiled_v12000 enc = get_encode_fn();

@@ -96,14 +96,6 @@ __device__ __forceinline__ void prefetch_tmap(const void* tmap)
     asm volatile("prefetch.tensormap [%0];" ::"l"(tmap) : "memory");
 }
 
-/* Per-warpgroup register reallocation (all four warps of a warpgroup execute
- * it). The decreases and increases of a kernel must sum to no more than the
- * registers the block was launched with. */
-template <int N>
-__device__ __forceinline__ void regs_dec() { asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(N)); }
-template <int N>
-__device__ __forceinline__ void regs_inc() { asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" ::"n"(N)); }
-
 /* ---- tcgen05 ---- */
 
 __device__ __forceinline__ void tmem_alloc(uint32_t* dst_smem, uint32_t ncols)
@@ -188,54 +180,13 @@ __host__ __device__ constexpr uint32_t idesc_e4m3_f32(int M, int N)
          | ((uint32_t)(M >> 4) << 24);     /* M / 16 */
 }
 
-#define SM103_TMEM_LD_X32(taddr, r)                                                              \
-    asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 "                                       \
-                 "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"                       \
-                 "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"     \
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),       \
-                   "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]),     \
-                   "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), \
-                   "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), \
-                   "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), \
-                   "=r"(r[30]), "=r"(r[31])                                                      \
-                 : "r"(taddr))
-
-#define SM103_TMEM_ST_X32(taddr, r)                                                              \
-    asm volatile("tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], "                                 \
-                 "{%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,"                      \
-                 "%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};"            \
-                 ::"r"(taddr), "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), \
-                   "r"(r[6]), "r"(r[7]), "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]),           \
-                   "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15]), "r"(r[16]), "r"(r[17]),       \
-                   "r"(r[18]), "r"(r[19]), "r"(r[20]), "r"(r[21]), "r"(r[22]), "r"(r[23]),       \
-                   "r"(r[24]), "r"(r[25]), "r"(r[26]), "r"(r[27]), "r"(r[28]), "r"(r[29]),       \
-                   "r"(r[30]), "r"(r[31])                                                        \
-                 : "memory")
-
-#define SM103_TMEM_LD_X16(taddr, r)                                                              \
-    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 "                                       \
-                 "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"              \
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),       \
-                   "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]),     \
-                   "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])                            \
-                 : "r"(taddr))
-
 #define SM103_TMEM_LD_X8(taddr, r)                                                               \
     asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"          \
                  : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),       \
                    "=r"(r[6]), "=r"(r[7])                                                        \
                  : "r"(taddr))
 
-#define SM103_TMEM_ST_X16(taddr, r)                                                              \
-    asm volatile("tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "                                 \
-                 "{%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};"                     \
-                 ::"r"(taddr), "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), \
-                   "r"(r[6]), "r"(r[7]), "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]),           \
-                   "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15])                                \
-                 : "memory")
-
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
-__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
 }  // namespace sm103
 
