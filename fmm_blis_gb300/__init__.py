@@ -108,6 +108,8 @@ def lib() -> ctypes.CDLL:
     L.fmm_gpu_dgemm.argtypes = [pf, ci, i64, i64, i64, dbl, vp, i64, vp, i64, dbl, vp, i64, vp]
     L.fmm_gpu_strassen_ab_ex.restype = ci
     L.fmm_gpu_strassen_ab_ex.argtypes = [dbl, vp, i64, vp, i64, dbl, vp, i64, i64, i64, i64, FmmT]
+    L.fmm_gpu_strassen_ab_gen.restype = ci
+    L.fmm_gpu_strassen_ab_gen.argtypes = [dbl, vp, i64, i64, vp, i64, i64, dbl, vp, i64, i64, i64, i64, i64, FmmT]
     L.fmm_gpu_strassen_ab.restype = ci
     L.fmm_gpu_strassen_ab.argtypes = [dbl, vp, i64, vp, i64, dbl, vp, i64, i64, i64, i64]
     L.fmm_gpu_split_workspace_size.restype = ctypes.c_size_t
@@ -367,13 +369,31 @@ def batch_dgemm(problems, workspace=None, stream=None) -> None:
 
 def bli_strassen_ab_ex(alpha: float, A, B, beta: float, C, fmm: FmmT) -> None:
     """Host-array drop-in for bli_strassen_ab_ex (frame/base/bli_strassen_ab.c:123):
-    numpy float64 Fortran-order arrays, C updated in place."""
+    numpy float64 arrays of any layout (Fortran order, C order, transposed or
+    strided views, like the obj_t operands of the reference), C updated in
+    place."""
     import numpy as np
     for name, x in (("A", A), ("B", B), ("C", C)):
-        if x.dtype != np.float64 or not x.flags.f_contiguous:
-            raise ValueError(f"{name} must be a Fortran-ordered float64 array")
+        if x.dtype != np.float64 or x.ndim != 2:
+            raise ValueError(f"{name} must be a 2-D float64 array")
+        if x.size > 0 and any(st <= 0 or st % 8 for st in x.strides):
+            raise ValueError(f"{name} needs positive element strides")
     m, k = A.shape
     n = B.shape[1]
-    st = lib().fmm_gpu_strassen_ab_ex(alpha, A.ctypes.data, max(m, 1), B.ctypes.data, max(k, 1), beta,
-                                      C.ctypes.data, max(m, 1), m, n, k, fmm)
-    _check(st, "fmm_gpu_strassen_ab_ex")
+    if B.shape[0] != k or C.shape != (m, n):
+        raise ValueError("shape mismatch")
+    if A.flags.f_contiguous and B.flags.f_contiguous and C.flags.f_contiguous:
+        st = lib().fmm_gpu_strassen_ab_ex(alpha, A.ctypes.data, max(m, 1), B.ctypes.data, max(k, 1), beta,
+                                          C.ctypes.data, max(m, 1), m, n, k, fmm)
+        _check(st, "fmm_gpu_strassen_ab_ex")
+        return
+
+    def rs(x):
+        return max(x.strides[0] // 8, 1)
+
+    def cs(x):
+        return max(x.strides[1] // 8, 1)
+
+    st = lib().fmm_gpu_strassen_ab_gen(alpha, A.ctypes.data, rs(A), cs(A), B.ctypes.data, rs(B), cs(B), beta,
+                                       C.ctypes.data, rs(C), cs(C), m, n, k, fmm)
+    _check(st, "fmm_gpu_strassen_ab_gen")

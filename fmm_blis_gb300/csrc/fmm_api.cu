@@ -5,6 +5,7 @@
  */
 #include "fmm_internal.h"
 
+#include <algorithm>
 #include <atomic>
 #include <cstdlib>
 #include <cstring>
@@ -256,6 +257,131 @@ extern "C" int fmm_gpu_strassen_ab_ex(double alpha, const double* A, int64_t lda
     cudaFree(dA);
     cudaFree(dB);
     cudaFree(dC);
+    return rc;
+}
+
+namespace {
+
+/* dst[i + j*rows] = src[j + i*cols] (src: a row-major rows x cols block);
+ * 32 x 32 tiles through shared memory, both sides coalesced */
+__global__ void transpose_to_colmajor(const double* __restrict__ src, double* __restrict__ dst, int64_t rows,
+                                      int64_t cols)
+{
+    __shared__ double t[32][33];
+    const int64_t i0 = (int64_t)blockIdx.y * 32, j0 = (int64_t)blockIdx.x * 32;
+    for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+        const int64_t i = i0 + r, j = j0 + threadIdx.x;
+        if (i < rows && j < cols) t[r][threadIdx.x] = src[j + i * cols];
+    }
+    __syncthreads();
+    for (int c = threadIdx.y; c < 32; c += blockDim.y) {
+        const int64_t j = j0 + c, i = i0 + threadIdx.x;
+        if (i < rows && j < cols) dst[i + j * rows] = t[threadIdx.x][c];
+    }
+}
+
+/* the reverse: dst[j + i*cols] = src[i + j*rows] */
+__global__ void transpose_from_colmajor(const double* __restrict__ src, double* __restrict__ dst, int64_t rows,
+                                        int64_t cols)
+{
+    __shared__ double t[32][33];
+    const int64_t i0 = (int64_t)blockIdx.y * 32, j0 = (int64_t)blockIdx.x * 32;
+    for (int c = threadIdx.y; c < 32; c += blockDim.y) {
+        const int64_t j = j0 + c, i = i0 + threadIdx.x;
+        if (i < rows && j < cols) t[c][threadIdx.x] = src[i + j * rows];
+    }
+    __syncthreads();
+    for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+        const int64_t i = i0 + r, j = j0 + threadIdx.x;
+        if (i < rows && j < cols) dst[j + i * cols] = t[threadIdx.x][r];
+    }
+}
+
+dim3 transpose_grid(int64_t rows, int64_t cols)
+{
+    return dim3((unsigned)((cols + 31) / 32), (unsigned)((rows + 31) / 32));
+}
+
+/* A host operand with element (i, j) at X[i*rs + j*cs] into the column-major
+ * device array dX (rows x cols): rs == 1 is one pitched copy; cs == 1 (row
+ * major, or a transposed column-major operand) is one pitched copy into
+ * dtmp and a transpose on the device; any other strides are gathered on the
+ * host. */
+int operand_to_device(const double* X, int64_t rows, int64_t cols, int64_t rs, int64_t cs, double* dX, double* dtmp)
+{
+    if (rows == 0 || cols == 0) return FMM_OK;
+    if (rs == 1) {
+        return cudaMemcpy2D(dX, sizeof(double) * rows, X, sizeof(double) * cs, sizeof(double) * rows, cols,
+                            cudaMemcpyHostToDevice) == cudaSuccess ? FMM_OK : FMM_ERR_CUDA;
+    }
+    if (cs == 1) {
+        if (cudaMemcpy2D(dtmp, sizeof(double) * cols, X, sizeof(double) * rs, sizeof(double) * cols, rows,
+                         cudaMemcpyHostToDevice) != cudaSuccess)
+            return FMM_ERR_CUDA;
+        transpose_to_colmajor<<<transpose_grid(rows, cols), dim3(32, 8)>>>(dtmp, dX, rows, cols);
+        fmm_count_launch(1);
+        return cudaGetLastError() == cudaSuccess ? FMM_OK : FMM_ERR_CUDA;
+    }
+    std::vector<double> h((size_t)(rows * cols));
+    for (int64_t j = 0; j < cols; ++j)
+        for (int64_t i = 0; i < rows; ++i) h[(size_t)(i + j * rows)] = X[i * rs + j * cs];
+    return cudaMemcpy(dX, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice) == cudaSuccess
+               ? FMM_OK : FMM_ERR_CUDA;
+}
+
+/* the reverse for C: only the elements of the operand are written */
+int operand_to_host(const double* dX, int64_t rows, int64_t cols, double* X, int64_t rs, int64_t cs, double* dtmp)
+{
+    if (rows == 0 || cols == 0) return FMM_OK;
+    if (rs == 1) {
+        return cudaMemcpy2D(X, sizeof(double) * cs, dX, sizeof(double) * rows, sizeof(double) * rows, cols,
+                            cudaMemcpyDeviceToHost) == cudaSuccess ? FMM_OK : FMM_ERR_CUDA;
+    }
+    if (cs == 1) {
+        transpose_from_colmajor<<<transpose_grid(rows, cols), dim3(32, 8)>>>(dX, dtmp, rows, cols);
+        fmm_count_launch(1);
+        if (cudaGetLastError() != cudaSuccess) return FMM_ERR_CUDA;
+        return cudaMemcpy2D(X, sizeof(double) * rs, dtmp, sizeof(double) * cols, sizeof(double) * cols, rows,
+                            cudaMemcpyDeviceToHost) == cudaSuccess ? FMM_OK : FMM_ERR_CUDA;
+    }
+    std::vector<double> h((size_t)(rows * cols));
+    if (cudaMemcpy(h.data(), dX, sizeof(double) * h.size(), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return FMM_ERR_CUDA;
+    for (int64_t j = 0; j < cols; ++j)
+        for (int64_t i = 0; i < rows; ++i) X[i * rs + j * cs] = h[(size_t)(i + j * rows)];
+    return FMM_OK;
+}
+
+}  // namespace
+
+extern "C" int fmm_gpu_strassen_ab_gen(double alpha, const double* A, int64_t rsa, int64_t csa, const double* B,
+                                       int64_t rsb, int64_t csb, double beta, double* C, int64_t rsc,
+                                       int64_t csc, int64_t m, int64_t n, int64_t k, fmm_t fmm)
+{
+    if (m < 0 || n < 0 || k < 0) return FMM_ERR_ARG;
+    if (rsa < 1 || csa < 1 || rsb < 1 || csb < 1 || rsc < 1 || csc < 1) return FMM_ERR_ARG;
+    if (m > 0 && n > 0 && C == nullptr) return FMM_ERR_ARG;
+    if (m > 0 && n > 0 && k > 0 && (A == nullptr || B == nullptr)) return FMM_ERR_ARG;
+    if (m == 0 || n == 0) return FMM_OK;
+    double *dA = nullptr, *dB = nullptr, *dC = nullptr, *dT = nullptr;
+    const int64_t ka = k > 0 ? k : 1;
+    const int64_t tmp = std::max(std::max(m * ka, ka * n), m * n);
+    int rc = FMM_OK;
+    if (cudaMalloc(&dA, sizeof(double) * (size_t)(m * ka)) != cudaSuccess ||
+        cudaMalloc(&dB, sizeof(double) * (size_t)(ka * n)) != cudaSuccess ||
+        cudaMalloc(&dC, sizeof(double) * (size_t)(m * n)) != cudaSuccess ||
+        cudaMalloc(&dT, sizeof(double) * (size_t)tmp) != cudaSuccess)
+        rc = FMM_ERR_ALLOC;
+    if (rc == FMM_OK && k > 0) rc = operand_to_device(A, m, k, rsa, csa, dA, dT);
+    if (rc == FMM_OK && k > 0) rc = operand_to_device(B, k, n, rsb, csb, dB, dT);
+    if (rc == FMM_OK) rc = operand_to_device(C, m, n, rsc, csc, dC, dT);
+    if (rc == FMM_OK) rc = fmm_gpu_dgemm(&fmm, 1, m, n, k, alpha, dA, m, dB, ka, beta, dC, m, nullptr);
+    if (rc == FMM_OK) rc = operand_to_host(dC, m, n, C, rsc, csc, dT);
+    if (rc == FMM_OK && cudaDeviceSynchronize() != cudaSuccess) rc = FMM_ERR_CUDA;
+    cudaFree(dA);
+    cudaFree(dB);
+    cudaFree(dC);
+    cudaFree(dT);
     return rc;
 }
 

@@ -147,6 +147,19 @@ int fmm_gpu_strassen_ab_ex(double alpha, const double* A, int64_t lda,
                            int64_t m, int64_t n, int64_t k,
                            fmm_t fmm);
 
+/* fmm_gpu_strassen_ab_ex for operands with any layout, the way a BLIS obj_t
+ * describes them (frame/base/bli_strassen_ab.c:143-149 reads its operands
+ * through obj_t accessors): element (i, j) of X at X[i*rs_x + j*cs_x], all
+ * strides >= 1. Row-major operands and transposed ones (a transposed
+ * column-major operand is a row-major one of the transposed shape) take one
+ * pitched copy and a transpose on the device; other strides are gathered on
+ * the host. Only C's own elements are written back. The result equals the
+ * column-major call's bit for bit. */
+int fmm_gpu_strassen_ab_gen(double alpha, const double* A, int64_t rs_a, int64_t cs_a,
+                            const double* B, int64_t rs_b, int64_t cs_b,
+                            double beta, double* C, int64_t rs_c, int64_t cs_c,
+                            int64_t m, int64_t n, int64_t k, fmm_t fmm);
+
 /* Drop-in for bli_strassen_ab (frame/base/bli_strassen_ab.c:297-300):
  * fmm_gpu_strassen_ab_ex with STRASSEN_FMM. */
 int fmm_gpu_strassen_ab(double alpha, const double* A, int64_t lda,

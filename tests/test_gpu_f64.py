@@ -140,3 +140,44 @@ def test_large_property_f64(fmm, torch_cuda, alg, levels):
     err = float((Cf - Cc).abs().max())
     eps = float(np.finfo(np.float64).eps)
     assert err <= 4 * eps * n * levels * (2 if alg == "333" else 1)
+
+
+@pytest.mark.parametrize("layout", ["c_order", "transposed_views", "strided_slices", "mixed"])
+def test_host_dropin_any_layout(fmm, orc, torch_cuda, layout):
+    """The host drop-in takes operands in any layout a BLIS obj_t can have
+    (column-major, row-major, transposed, general strides): the result equals
+    the column-major call's bit for bit, and only C's elements are written."""
+    m, n, k = 70, 53, 91
+    A, B, C = rand(m, k, 301), rand(k, n, 302), rand(m, n, 303)
+    f = fmm.strassen_fmm()
+    want = C.copy(order="F")
+    fmm.bli_strassen_ab_ex(0.5, A.copy(order="F"), B.copy(order="F"), 1.5, want, f)
+    if layout == "c_order":
+        a, b = np.ascontiguousarray(A), np.ascontiguousarray(B)
+        c_buf = np.ascontiguousarray(C)
+        c = c_buf
+    elif layout == "transposed_views":
+        a, b = np.asfortranarray(A.T).T, np.asfortranarray(B.T).T     # row-major data seen through .T
+        c_buf = np.asfortranarray(C.T)
+        c = c_buf.T
+    elif layout == "strided_slices":
+        big_a = np.zeros((2 * m, 3 * k))
+        big_a[::2, ::3] = A
+        a = big_a[::2, ::3]
+        big_b = np.zeros((3 * k, 2 * n), order="F")
+        big_b[::3, ::2] = B
+        b = big_b[::3, ::2]
+        c_buf = np.full((2 * m, 2 * n), 7.0)
+        c_buf[::2, ::2] = C
+        c = c_buf[::2, ::2]
+    else:
+        a = np.ascontiguousarray(A)
+        b = B.copy(order="F")
+        c_buf = np.ascontiguousarray(C)
+        c = c_buf
+    fmm.bli_strassen_ab_ex(0.5, a, b, 1.5, c, f)
+    assert np.array_equal(np.asarray(c), want)
+    if layout == "strided_slices":
+        mask = np.ones(c_buf.shape, bool)
+        mask[::2, ::2] = False
+        assert np.all(c_buf[mask] == 7.0)
