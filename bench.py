@@ -706,9 +706,11 @@ def main():
             traffic = json.loads(tf.read_text()).get("bytes_per_launch_16384_x2")
         except ValueError:
             traffic = None
+    # single calls take 256 x 256 CTA-pair tiles once m_e >= 1024
+    kernel = "split_gemm_pair_kernel" if me >= 1024 else "split_gemm_kernel"
     roofline = {"bound": "tensor", "achieved": achieved, "peak": peak_sus, "unit": "TFLOP/s",
                 "frac": achieved / peak_sus, "traffic": traffic,
-                "kernel": "split_gemm_kernel", "peak_kind": peak_kind,
+                "kernel": kernel, "peak_kind": peak_kind,
                 "flops_per_launch": kernel_flops, "avg_launch_ms": avg_launch_s * 1e3, "launches_timed": gemm_n,
                 "products_per_launch": gemm_products / max(gemm_n, 1)}
 

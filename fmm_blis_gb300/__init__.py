@@ -137,6 +137,8 @@ def lib() -> ctypes.CDLL:
     L.fmm_gpu_launch_count.argtypes = []
     L.fmm_gpu_take_device_error.restype = ci
     L.fmm_gpu_take_device_error.argtypes = []
+    L.fmm_gpu_set_split_pair_rows.restype = ci
+    L.fmm_gpu_set_split_pair_rows.argtypes = [ci]
     _lib = L
     return L
 
@@ -206,6 +208,13 @@ def read_kernel_timing() -> tuple[float, int, int]:
 
 def take_device_error() -> int:
     return int(lib().fmm_gpu_take_device_error())
+
+
+def set_split_pair_rows(min_rows: int) -> int:
+    """Per-product row count m_e from which split GEMMs use CTA-pair tiles
+    (default 1024; a huge value keeps single-SM tiles). Same bits either
+    way. Returns the previous value."""
+    return int(lib().fmm_gpu_set_split_pair_rows(min(int(min_rows), 2**31 - 1)))
 
 
 # ------------------------------------------------------------ GPU calls --

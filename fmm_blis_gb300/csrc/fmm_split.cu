@@ -57,6 +57,7 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <deque>
 #include <mutex>
@@ -649,7 +650,7 @@ struct Item {
     int p, r, tile_m, tile_n;
 };
 
-__device__ __forceinline__ Item decode_item(const GemmLaunch& L, int b)
+__device__ __forceinline__ Item decode_item(const GemmLaunch& L, int b, int raster = kRasterGroup)
 {
     int p = 0, hi = L.nprob - 1;        /* last problem with item_begin <= b */
     while (p < hi) {
@@ -663,9 +664,9 @@ __device__ __forceinline__ Item decode_item(const GemmLaunch& L, int b)
     it.p = p;
     it.r = local / per_prod;
     const int id = local % per_prod;
-    const int per_group = kRasterGroup * P.tiles_n;
-    const int grp = id / per_group, first_m = grp * kRasterGroup;
-    const int gm = min(P.tiles_m - first_m, kRasterGroup);
+    const int per_group = raster * P.tiles_n;
+    const int grp = id / per_group, first_m = grp * raster;
+    const int gm = min(P.tiles_m - first_m, raster);
     const int in_grp = id % per_group;
     it.tile_m = first_m + in_grp % gm;
     it.tile_n = in_grp / gm;
@@ -912,6 +913,249 @@ split_gemm_kernel(const __grid_constant__ GemmLaunch L)
     if (warp == 1) sm103::tmem_dealloc(tmem, kTmemCols);
 }
 
+/* ---------------------------------------------------- CTA-pair GEMM ---- */
+
+constexpr int kPairTileM = 256;                       /* rows of a pair tile (128 per CTA) */
+constexpr int kPairMinRows = 1024;                    /* m_e from which single calls use pair tiles */
+constexpr int kPairStages = 6;
+constexpr int kPairRasterGroup = 6;                   /* pair-tile rows per raster band (1536 rows) */
+std::atomic<int> g_pair_rows{kPairMinRows};           /* m_e from which GEMMs take pair tiles (host) */
+constexpr uint32_t kPairHalfBytes = 128 * kBK * 2;    /* 16 KB: 128 rows of one 128-byte stage row */
+constexpr uint32_t kPairStageBytes = 2 * kPairHalfBytes;
+constexpr size_t kPairSmem = (size_t)kPairStages * kPairStageBytes + 1024 + 512;
+
+/* The same GEMM as split_gemm_kernel with CTA pairs (clusters of two): a work
+ * item is a 256 x 256 tile of a product; each CTA loads its 128 rows of the A
+ * slice tile and its 128-column half of the B slice tile (32 KB per stage
+ * instead of 48 KB, so the L2 feeds each SM a third less per MMA and the
+ * six-stage ring looks 50% further ahead), and the even CTA issues
+ * tcgen05.mma cta_group::2 (M=256, N=256) into both CTAs' TMEM. Both CTAs'
+ * stage loads complete on the even CTA's barrier (TMA cta_group::2); the MMA
+ * commits arrive on both CTAs' stage and accumulator barriers; each CTA's epilogue drains its own 128 rows exactly
+ * as in split_gemm_kernel and reports the buffer free to the even CTA. All
+ * waits are bounded; the two cluster barriers (after barrier set-up, before
+ * TMEM release) are reached by every thread of both CTAs. */
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kGemmThreads, 1)
+split_gemm_pair_kernel(const __grid_constant__ GemmLaunch L)
+{
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint8_t* sA = smem;
+    uint8_t* sB = smem + kPairStages * kPairHalfBytes;
+    uint64_t* full = (uint64_t*)(smem + kPairStages * kPairStageBytes);
+    uint64_t* empty = full + kPairStages;
+    uint64_t* accf = empty + kPairStages;
+    uint64_t* acce = accf + 2;
+    uint64_t* drain = acce + 2;
+    uint32_t* tmem_slot = (uint32_t*)(drain + 1);
+    volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
+
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    const uint32_t rank = sm103::cluster_ctarank();
+    const int cl = (int)(blockIdx.x / 2), ncl = (int)(gridDim.x / 2);
+
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < kPairStages; ++i) {
+            sm103::mbar_init(&full[i], 1);
+            sm103::mbar_init(&empty[i], 1);
+        }
+        for (int i = 0; i < 2; ++i) { sm103::mbar_init(&accf[i], 1); sm103::mbar_init(&acce[i], 2 * kEpiWarps); }
+        sm103::mbar_init(drain, 1);
+        *abort_flag = 0;
+        sm103::fence_mbar_init();
+    }
+    if (warp == 1) { sm103::tmem_alloc_pair(tmem_slot, kTmemCols); sm103::tmem_relinquish_pair(); }
+    sm103::tc_fence_before();
+    sm103::cluster_sync();   /* both CTAs' barriers exist before any remote arrive */
+    sm103::tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0) {
+        /* ---------------- TMA producer (both CTAs) ---------------- */
+        if (lane == 0) {
+            int st = 0;
+            uint32_t ph = 0;
+            uint32_t armed = 0;
+            bool ok = true;
+            int last_p = -1;
+            for (int b = cl; b < L.nitems && ok; b += ncl) {
+                const Item it = decode_item(L, b, kPairRasterGroup);
+                const GemmProblem& P = L.prob[it.p];
+                if (it.p != last_p) { sm103::prefetch_tmap(&P.tmA); sm103::prefetch_tmap(&P.tmB); last_p = it.p; }
+                const int s = P.s, nkb = P.nkb;
+                const int arow = it.r * s * P.m_pad + it.tile_m * kPairTileM + 128 * (int)rank;
+                const int brow = it.r * s * P.n_pad + it.tile_n * kTileN + 128 * (int)rank;
+                int pi = 0;   /* the single-CTA kernel's pair order */
+                for (int g = 2; g <= s + 1 && ok; ++g) {
+                    const int tlo = max(1, g - s), thi = min(s, g - 1);
+                    for (int x = 0; x <= thi - tlo && ok; ++x, ++pi) {
+                        const int t = (g & 1) ? thi - x : tlo + x;
+                        const int u = g - t;
+                        for (int y = 0; y < nkb; ++y) {
+                            const int kb = (pi & 1) ? nkb - 1 - y : y;
+                            if (!sm103::mbar_wait(&empty[st], ph ^ 1, abort_flag, L.err, 11)) { ok = false; break; }
+                            /* both CTAs' loads complete on the even CTA's full[st]; the
+                             * even CTA expects the bytes of both */
+                            if (rank == 0) sm103::mbar_arrive_expect_tx(&full[st], 2 * kPairStageBytes);
+                            const uint32_t fb = sm103::mapa(sm103::smem_u32(&full[st]), 0);
+                            sm103::tma_load_2d_pair(sA + st * kPairHalfBytes, &P.tmA, fb, kb * P.kbe,
+                                                    arow + (t - 1) * P.m_pad);
+                            sm103::tma_load_2d_pair(sB + st * kPairHalfBytes, &P.tmB, fb, kb * P.kbe,
+                                                    brow + (u - 1) * P.n_pad);
+                            armed |= 1u << st;
+                            if (++st == kPairStages) { st = 0; ph ^= 1; armed = 0; }
+                        }
+                    }
+                }
+            }
+            if (!ok && rank == 0) {
+                for (int i = 0; i < kPairStages; ++i) {
+                    const uint32_t par = (armed >> i) & 1u ? ph : ph ^ 1;
+                    uint64_t t0 = sm103::globaltimer();
+                    while (!sm103::mbar_try_wait(&full[i], par) &&
+                           sm103::globaltimer() - t0 < sm103::kWaitLimitNs) {}
+                }
+            }
+            (void)armed;
+        }
+    } else if (warp == 1) {
+        if (lane == 0 && rank == 0) {
+            /* ---------------- even CTA: MMA issuer ---------------- */
+            constexpr uint32_t idesc16 = sm103::idesc_bf16_f32(kPairTileM, kTileN);
+            constexpr uint32_t idesc8 = sm103::idesc_e4m3_f32(kPairTileM, kTileN);
+            int st = 0, buf = 0;
+            uint32_t ph = 0, aph = 0;
+            bool ok = true;
+            for (int b = cl; b < L.nitems && ok; b += ncl) {
+                const Item it = decode_item(L, b, kPairRasterGroup);
+                const int s = L.prob[it.p].s, nkb = L.prob[it.p].nkb, fmt = L.prob[it.p].fmt;
+                for (int g = 2; g <= s + 1 && ok; ++g) {
+                    const int level_kb = level_pairs(g, s) * nkb;
+                    for (int jl = 0; jl < level_kb && ok; ) {
+                        if (jl % kChunkKB == 0) {
+                            if (!sm103::mbar_wait(&acce[buf], aph ^ 1, abort_flag, L.err, 13)) { ok = false; break; }
+                            sm103::tc_fence_after();
+                        }
+                        if (!sm103::mbar_wait(&full[st], ph, abort_flag, L.err, 14)) { ok = false; break; }
+                        sm103::tc_fence_after();
+                        const uint32_t a0 = sm103::smem_u32(sA + st * kPairHalfBytes);
+                        const uint32_t b0 = sm103::smem_u32(sB + st * kPairHalfBytes);
+                        if (fmt) {
+#pragma unroll
+                            for (int kk = 0; kk < 4; ++kk)
+                                sm103::mma_f8_pair(tmem + buf * kTileN, sm103::smem_desc_sw128(a0 + kk * 32),
+                                                   sm103::smem_desc_sw128(b0 + kk * 32), idesc8,
+                                                   (jl % kChunkKB != 0 || kk != 0) ? 1u : 0u);
+                        } else {
+#pragma unroll
+                            for (int kk = 0; kk < 4; ++kk)
+                                sm103::mma_bf16_pair(tmem + buf * kTileN, sm103::smem_desc_sw128(a0 + kk * 32),
+                                                     sm103::smem_desc_sw128(b0 + kk * 32), idesc16,
+                                                     (jl % kChunkKB != 0 || kk != 0) ? 1u : 0u);
+                        }
+                        sm103::mma_commit_pair(&empty[st]);
+                        if (++st == kPairStages) { st = 0; ph ^= 1; }
+                        ++jl;
+                        if (jl % kChunkKB == 0 || jl == level_kb) {
+                            sm103::mma_commit_pair(&accf[buf]);
+                            buf ^= 1;
+                            if (buf == 0) aph ^= 1;
+                        }
+                    }
+                }
+            }
+            /* all issued MMAs complete before either CTA releases TMEM */
+            sm103::mma_commit_pair(drain);
+            uint64_t t0 = sm103::globaltimer();
+            while (!sm103::mbar_try_wait(drain, 0) && sm103::globaltimer() - t0 < sm103::kWaitLimitNs) {}
+        }
+    } else {
+        /* ---------------- epilogue warps (both CTAs) ---------------- */
+        const int quarter = warp % 4;
+        const int colbase = ((warp - 2) / 4) * kEpiCols;
+        const int row = quarter * 32 + lane;
+        const uint32_t tl = tmem + ((uint32_t)(quarter * 32) << 16);
+        const uint32_t acce0 = sm103::mapa(sm103::smem_u32(acce), 0);
+        int buf = 0;
+        uint32_t aph = 0;
+        bool ok = true;
+        uint64_t pol_keep, pol_drop;
+        asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol_keep));
+        asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol_drop));
+        for (int b = cl; b < L.nitems && ok; b += ncl) {
+            const Item it = decode_item(L, b, kPairRasterGroup);
+            const GemmProblem& P = L.prob[it.p];
+            const int s = P.s, nkb = P.nkb;
+            int64_t* zrow = P.Z + (int64_t)it.r * P.n_pad * P.m_pad +
+                            (int64_t)(it.tile_n * kTileN + colbase) * P.m_pad + it.tile_m * kPairTileM +
+                            128 * (int)rank + row;
+            const struct { int zlevel, m_pad, db; } a = {P.zlevel, P.m_pad, P.db};
+            for (int g = 2; g <= s + 1 && ok; ++g) {
+                int lsum[kEpiCols];
+#pragma unroll
+                for (int x = 0; x < kEpiCols; ++x) lsum[x] = 0;
+                const int nchunks = (level_pairs(g, s) * nkb + kChunkKB - 1) / kChunkKB;
+                for (int c = 0; c < nchunks; ++c) {
+                    if (!sm103::mbar_wait(&accf[buf], aph, abort_flag, L.err, 16)) { ok = false; break; }
+                    sm103::tc_fence_after();
+#pragma unroll
+                    for (int h = 0; h < kEpiCols / 8; ++h) {
+                        uint32_t v[8];
+                        SM103_TMEM_LD_X8(tl + buf * kTileN + colbase + h * 8, v);
+                        sm103::tmem_wait_ld();
+#pragma unroll
+                        for (int x = 0; x < 8; ++x)
+                            lsum[h * 8 + x] += __float2int_rn(__uint_as_float(v[x]));   /* exact: integer, |v| <= 2^24 */
+                    }
+                    sm103::tc_fence_before();
+                    __syncwarp();
+                    if (lane == 0) sm103::mbar_arrive_cluster(acce0 + buf * 8);
+                    buf ^= 1;
+                    if (buf == 0) aph ^= 1;
+                }
+                if (!ok) break;
+                /* fold L_g into the Z tile, as in split_gemm_kernel */
+                {
+                    const int D = a.zlevel - g;
+                    const uint32_t lsh = D >= 0 ? a.db * D : 0;
+                    const uint32_t rsh = D >= 0 ? 0 : -a.db * D;
+                    const uint64_t rnd = D >= 0 ? 0 : (1ull << (rsh - 1));
+                    uint64_t zp = (uint64_t)zrow;
+                    const uint64_t zstep = (uint64_t)a.m_pad * 8;
+                    const uint64_t pol = g == s + 1 ? pol_drop : pol_keep;
+                    if (g == 2) {
+#pragma unroll
+                        for (int x = 0; x < kEpiCols; ++x)
+                            asm volatile("{\n\t.reg .b64 t;\n\t"
+                                         "cvt.s64.s32 t, %1;\n\t"
+                                         "shl.b64 t, t, %2;\n\t"
+                                         "st.global.L2::cache_hint.u64 [%0], t, %4;\n\t"
+                                         "add.u64 %0, %0, %3;\n\t}"
+                                         : "+l"(zp) : "r"(lsum[x]), "r"(lsh), "l"(zstep), "l"(pol) : "memory");
+                    } else {
+#pragma unroll
+                        for (int x = 0; x < kEpiCols; ++x)
+                            asm volatile("{\n\t.reg .b64 t;\n\t"
+                                         "cvt.s64.s32 t, %1;\n\t"
+                                         "shl.b64 t, t, %2;\n\t"
+                                         "add.s64 t, t, %4;\n\t"
+                                         "shr.s64 t, t, %3;\n\t"
+                                         "red.global.add.L2::cache_hint.u64 [%0], t, %6;\n\t"
+                                         "add.u64 %0, %0, %5;\n\t}"
+                                         : "+l"(zp) : "r"(lsum[x]), "r"(lsh), "r"(rsh), "l"(rnd), "l"(zstep), "l"(pol)
+                                         : "memory");
+                    }
+                }
+            }
+        }
+    }
+    sm103::tc_fence_before();
+    __syncthreads();
+    sm103::cluster_sync();   /* no remote arrive or MMA still targets either CTA */
+    sm103::tc_fence_after();
+    if (warp == 1) sm103::tmem_dealloc_pair(tmem, kTmemCols);
+}
+
 /* Multi-C epilogue for a group of products [r0, r0 + nprod): one thread per
  * (C sub-block p = blockIdx.y, element (i, j) of p) adds alpha*W[p,r] *
  * M_r[i,j] for the group's products in increasing order, with M_r[i,j] =
@@ -1116,7 +1360,9 @@ Dims dims_of(const AlgView& alg, int64_t m, int64_t n, int64_t k, int fmt = 0)
     d.me = (m + alg.mt - 1) / alg.mt;
     d.ne = (n + alg.nt - 1) / alg.nt;
     d.ke = (k + alg.kt - 1) / alg.kt;
-    d.m_pad = round_up(std::max<int64_t>(d.me, 1), kTileM);
+    /* rows padded to the 256-row pair tiles once m_e >= 1024 (at most 25%
+     * padding there); any multiple of 128 also serves the single-CTA kernel */
+    d.m_pad = round_up(std::max<int64_t>(d.me, 1), d.me >= kPairMinRows ? kPairTileM : kTileM);
     d.n_pad = round_up(std::max<int64_t>(d.ne, 1), kTileN);
     d.k_pad = round_up(std::max<int64_t>(d.ke, 1), kbe_of(fmt));
     return d;
@@ -1201,6 +1447,11 @@ void timing_mark(cudaStream_t st, bool before)
 }
 
 }  // namespace
+
+extern "C" int fmm_gpu_set_split_pair_rows(int min_rows)
+{
+    return g_pair_rows.exchange(std::max(min_rows, kPairMinRows));
+}
 
 extern "C" void fmm_gpu_set_kernel_timing(int enable)
 {
@@ -1435,13 +1686,20 @@ static int job_db(const SplitJob& j) { return j.fmt ? 5 : 8; }
 static int job_ebase(const SplitJob& j) { return 2 - job_db(j) * job_zlevel(j); }
 
 /* the job's product group as one problem of a GEMM launch */
-static int job_fill(const SplitJob& j, GemmProblem& gp, int np, int item_begin)
+/* pair tiles for this job's single-call GEMM launches */
+static bool job_pair(const SplitJob& j)
+{
+    return j.d.me >= g_pair_rows.load(std::memory_order_relaxed) && j.d.m_pad % kPairTileM == 0;
+}
+
+static int job_fill(const SplitJob& j, GemmProblem& gp, int np, int item_begin, bool pair = false)
 {
     const Dims& d = j.d;
     const int G = j.L.group;
     if (make_slice_map(&gp.tmA, j.w + j.L.sa, d.k_pad, (int64_t)G * j.s * d.m_pad, kTileM, j.fmt) != FMM_OK)
         return FMM_ERR_CUDA;
-    if (make_slice_map(&gp.tmB, j.w + j.L.sb, d.k_pad, (int64_t)G * j.s * d.n_pad, kTileN, j.fmt) != FMM_OK)
+    if (make_slice_map(&gp.tmB, j.w + j.L.sb, d.k_pad, (int64_t)G * j.s * d.n_pad, pair ? kTileN / 2 : kTileN,
+                       j.fmt) != FMM_OK)
         return FMM_ERR_CUDA;
     gp.Z = (int64_t*)(j.w + j.L.z);
     gp.s = j.s;
@@ -1452,16 +1710,16 @@ static int job_fill(const SplitJob& j, GemmProblem& gp, int np, int item_begin)
     gp.fmt = j.fmt;
     gp.m_pad = (int)d.m_pad;
     gp.n_pad = (int)d.n_pad;
-    gp.tiles_m = (int)(d.m_pad / kTileM);
+    gp.tiles_m = (int)(d.m_pad / (pair ? kPairTileM : kTileM));
     gp.tiles_n = (int)(d.n_pad / kTileN);
     gp.item_begin = item_begin;
     (void)np;
     return FMM_OK;
 }
 
-static int64_t job_items(const SplitJob& j, int np)
+static int64_t job_items(const SplitJob& j, int np, bool pair = false)
 {
-    return (int64_t)np * (j.d.m_pad / kTileM) * (j.d.n_pad / kTileN);
+    return (int64_t)np * (j.d.m_pad / (pair ? kPairTileM : kTileM)) * (j.d.n_pad / kTileN);
 }
 
 static void job_scatter(const SplitJob& j, int r0, int np, cudaStream_t st)
@@ -1487,12 +1745,14 @@ static void job_scatter(const SplitJob& j, int r0, int np, cudaStream_t st)
     fmm_count_launch(1);
 }
 
-static int launch_gemm(GemmLaunch& gl, int64_t nitems, int nprod_timed, cudaStream_t st)
+static int launch_gemm(GemmLaunch& gl, int64_t nitems, int nprod_timed, cudaStream_t st, bool pair = false)
 {
     static bool attr_set = false;
     if (!attr_set) {
         if (cudaFuncSetAttribute(split_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)kGemmSmem) != cudaSuccess)
+                                 (int)kGemmSmem) != cudaSuccess ||
+            cudaFuncSetAttribute(split_gemm_pair_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)kPairSmem) != cudaSuccess)
             return FMM_ERR_CUDA;
         attr_set = true;
     }
@@ -1509,7 +1769,10 @@ static int launch_gemm(GemmLaunch& gl, int64_t nitems, int nprod_timed, cudaStre
         std::lock_guard<std::mutex> lk(g_timing_mu);
         g_timed_products += (uint64_t)nprod_timed;
     }
-    split_gemm_kernel<<<(unsigned)std::min<int64_t>(nitems, sms), kGemmThreads, kGemmSmem, st>>>(gl);
+    if (pair)   /* clusters of two CTAs, one pair tile each at a time */
+        split_gemm_pair_kernel<<<(unsigned)(2 * std::min<int64_t>(nitems, sms / 2)), kGemmThreads, kPairSmem, st>>>(gl);
+    else
+        split_gemm_kernel<<<(unsigned)std::min<int64_t>(nitems, sms), kGemmThreads, kGemmSmem, st>>>(gl);
     if (timed) timing_mark(st, false);
     fmm_count_launch(1);
     return FMM_OK;
@@ -1532,8 +1795,9 @@ static int split_launch_budget(const AlgView& alg, int64_t m, int64_t n, int64_t
         GemmLaunch gl;
         memset(&gl, 0, sizeof(gl));
         gl.nprob = 1;
-        if ((rc = job_fill(j, gl.prob[0], np, 0)) != FMM_OK) return rc;
-        if ((rc = launch_gemm(gl, job_items(j, np), np, st)) != FMM_OK) return rc;
+        const bool pair = job_pair(j);
+        if ((rc = job_fill(j, gl.prob[0], np, 0, pair)) != FMM_OK) return rc;
+        if ((rc = launch_gemm(gl, job_items(j, np, pair), np, st, pair)) != FMM_OK) return rc;
         job_scatter(j, r0, np, st);
     }
     return cudaGetLastError() == cudaSuccess ? FMM_OK : FMM_ERR_CUDA;
@@ -1583,8 +1847,6 @@ int fmm_split_batch(int count, const SplitJob* jobs_in, void* ws, size_t ws_byte
         }
         if (e == i) return FMM_ERR_WORKSPACE;
         GemmLaunch gl;
-        memset(&gl, 0, sizeof(gl));
-        gl.nprob = e - i;
         size_t off = 0;
         int64_t items = 0;
         int prods = 0;
@@ -1609,19 +1871,28 @@ int fmm_split_batch(int count, const SplitJob* jobs_in, void* ws, size_t ws_byte
                    (jobs[q].fmt ? 2 : 1);   /* FP8 MMAs run at twice the BF16 rate */
         };
         std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return item_cost(a) > item_cost(b); });
-        for (size_t x = 0; x < ord.size(); ++x) {
-            SplitJob& j = jobs[ord[x]];
-            int rc = job_fill(j, gl.prob[x], j.alg.R, (int)items);
-            if (rc != FMM_OK) return rc;
-            items += job_items(j, j.alg.R);
-            prods += j.alg.R;
+        /* problems with pair tiles in one launch, the rest in another (both
+         * kernels give the same bits per tile) */
+        for (int pass = 0; pass < 2; ++pass) {
+            const bool pair = pass == 0;
+            memset(&gl, 0, sizeof(gl));
+            items = 0;
+            prods = 0;
+            for (int q : ord) {
+                SplitJob& j = jobs[q];
+                if (job_pair(j) != pair) continue;
+                int rc = job_fill(j, gl.prob[gl.nprob++], j.alg.R, (int)items, pair);
+                if (rc != FMM_OK) return rc;
+                items += job_items(j, j.alg.R, pair);
+                prods += j.alg.R;
+            }
+            if (gl.nprob == 0) continue;
+            if (int rc = launch_gemm(gl, items, prods, st, pair); rc != FMM_OK) return rc;
         }
-        int rc = launch_gemm(gl, items, prods, st);
-        if (rc != FMM_OK) return rc;
         /* each problem's C update (disjoint C regions) on the side streams */
-        if ((rc = side_fork(sp, st)) != FMM_OK) return rc;
+        if (int rc = side_fork(sp, st); rc != FMM_OK) return rc;
         for (int q = i; q < e; ++q) job_scatter(jobs[q], 0, jobs[q].alg.R, sp ? sp->s[(q - i) % kSideStreams] : st);
-        if ((rc = side_join(sp, st)) != FMM_OK) return rc;
+        if (int rc = side_join(sp, st); rc != FMM_OK) return rc;
         i = e;
     }
     return cudaGetLastError() == cudaSuccess ? FMM_OK : FMM_ERR_CUDA;

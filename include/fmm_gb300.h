@@ -281,6 +281,15 @@ int fmm_gpu_split_dgemm_noalloc(const fmm_t* fmm, int levels,
 void fmm_gpu_set_kernel_timing(int enable);
 int fmm_gpu_read_kernel_timing(double* total_ms, uint64_t* launches, uint64_t* products);
 
+/* Smallest per-product row count m_e = ceil(m / m~^levels) from which the
+ * split form's GEMM runs on CTA pairs (clusters of two SMs, 256 x 256 tiles,
+ * tcgen05.mma cta_group::2) instead of one SM per 128 x 256 tile; applies to
+ * single and batched calls. Default 1024, values below 1024 are raised to it,
+ * INT_MAX keeps every problem on single-SM tiles. Results are bit-identical
+ * either way (every tile's sums are exact); only the speed differs. Returns
+ * the previous value. No counterpart in the reference. */
+int fmm_gpu_set_split_pair_rows(int min_rows);
+
 /* Number of kernels the library launched since load (all entry points). */
 uint64_t fmm_gpu_launch_count(void);
 

@@ -25,3 +25,15 @@ def test_library_is_sm103a_build(fmm):
     from fmm_blis_gb300 import build
     assert "arch=compute_103a,code=sm_103a" in " ".join(build.ARCH)
     assert fmm.LIB_PATH.exists()
+
+
+def test_split_pair_rows_knob(fmm):
+    """The pair-tile threshold is host state: no GPU needed; values below
+    1024 are raised to 1024 and the previous value comes back."""
+    prev = fmm.set_split_pair_rows(5000)
+    try:
+        assert fmm.set_split_pair_rows(10) == 5000
+        assert fmm.set_split_pair_rows(2**40) == 1024
+        assert fmm.set_split_pair_rows(1024) == 2**31 - 1
+    finally:
+        fmm.set_split_pair_rows(prev)
