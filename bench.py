@@ -58,7 +58,7 @@ def parse():
                    help="slice format of the split form: BF16 (base-256 digits) or FP8-E4M3 (base-32 digits)")
     p.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison runs")
     p.add_argument("--no-cpu", action="store_true", help="skip the host-core baseline")
-    p.add_argument("--e2e-steps", type=int, default=2)
+    p.add_argument("--e2e-steps", type=int, default=3)
     p.add_argument("--form", choices=["split", "fp64"], default="split",
                    help="split: split-BF16 FMM (the headline); fp64: the plain FP64 FMM drop-in")
     p.add_argument("--workload", choices=["fmm", "batch", "serve", "sweep", "accuracy"], default="fmm",
@@ -714,6 +714,33 @@ def main():
                 "flops_per_launch": kernel_flops, "avg_launch_ms": avg_launch_s * 1e3, "launches_timed": gemm_n,
                 "products_per_launch": gemm_products / max(gemm_n, 1)}
 
+    # end to end through the host-buffer C-ABI call (fmm_gpu_split_strassen_ab_ex)
+    # with pinned host operands: every step uploads A, B and C and reads C back
+    e2e = None
+    if rank == 0 and args.e2e_steps > 0:
+        hA = torch.empty((n, n), dtype=torch.float64, pin_memory=True).t()
+        hB = torch.empty((n, n), dtype=torch.float64, pin_memory=True).t()
+        hC = torch.empty((n, n), dtype=torch.float64, pin_memory=True).t()
+        hA.copy_(A)
+        hB.copy_(B)
+        hC.copy_(C0)
+        torch.cuda.synchronize()
+
+        def host_step():
+            fmm.split_strassen_ab_ex(1.0, hA, hB, 1.0, hC, f, levels, s, fmt)
+
+        host_step()   # sizes the call's device buffers
+        with Clocks(torch.cuda.current_device()) as clk_e2e:
+            t0 = time.perf_counter()
+            for _ in range(args.e2e_steps):
+                host_step()
+            ms_e2e = (time.perf_counter() - t0) * 1e3 / args.e2e_steps
+        fmm.release_host_buffers()
+        e2e = {"value": flops / ms_e2e / 1e9, "unit": "TFLOP/s", "h2d_bytes_per_step": 3 * n * n * 8,
+               "d2h_bytes_per_step": n * n * 8, "ms_per_step": ms_e2e,
+               "call": "fmm_gpu_split_strassen_ab_ex (host buffers, copies overlapped with the device work)",
+               "clocks": clk_e2e.summary()}
+
     extra = {}
     if rank == 0 and not args.no_fp64:
         # classical FP64 reference result and the plain FP64 FMM, once
@@ -744,31 +771,6 @@ def main():
             "speedup_split_vs_fp64_fmm": (flops / ms / 1e9) / (flops / ms_fmm / 1e9),
             "fp64_fmm_vs_classical": ms_cls / ms_fmm,
         }
-
-    # end to end through the public API with pinned host buffers
-    e2e = None
-    if rank == 0 and args.e2e_steps > 0:
-        hA = torch.empty((n, n), dtype=torch.float64, pin_memory=True).t()
-        hB = torch.empty((n, n), dtype=torch.float64, pin_memory=True).t()
-        hC = torch.empty((n, n), dtype=torch.float64, pin_memory=True).t()
-        hA.copy_(A)
-        hB.copy_(B)
-        hC.copy_(C0)
-        dA, dB, dC = torch.empty_like(A), torch.empty_like(B), torch.empty_like(C0)
-        torch.cuda.synchronize()
-        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        t0.record(stream)
-        for _ in range(args.e2e_steps):
-            dA.copy_(hA, non_blocking=True)
-            dB.copy_(hB, non_blocking=True)
-            dC.copy_(hC, non_blocking=True)
-            fmm.split_dgemm(dA, dB, dC, f, levels, s, workspace=ws, stream=stream, fmt=fmt)
-            hC.copy_(dC, non_blocking=True)
-        t1.record(stream)
-        torch.cuda.synchronize()
-        ms_e2e = t0.elapsed_time(t1) / args.e2e_steps
-        e2e = {"value": flops / ms_e2e / 1e9, "unit": "TFLOP/s", "h2d_bytes_per_step": 3 * n * n * 8,
-               "d2h_bytes_per_step": n * n * 8, "ms_per_step": ms_e2e}
 
     cpu = None
     if rank == 0 and not args.no_cpu:

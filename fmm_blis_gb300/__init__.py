@@ -110,6 +110,10 @@ def lib() -> ctypes.CDLL:
     L.fmm_gpu_strassen_ab_ex.argtypes = [dbl, vp, i64, vp, i64, dbl, vp, i64, i64, i64, i64, FmmT]
     L.fmm_gpu_strassen_ab_gen.restype = ci
     L.fmm_gpu_strassen_ab_gen.argtypes = [dbl, vp, i64, i64, vp, i64, i64, dbl, vp, i64, i64, i64, i64, i64, FmmT]
+    L.fmm_gpu_split_strassen_ab_ex.restype = ci
+    L.fmm_gpu_split_strassen_ab_ex.argtypes = [dbl, vp, i64, vp, i64, dbl, vp, i64, i64, i64, i64, FmmT, ci, ci, ci]
+    L.fmm_gpu_release_host_buffers.restype = None
+    L.fmm_gpu_release_host_buffers.argtypes = []
     L.fmm_gpu_strassen_ab.restype = ci
     L.fmm_gpu_strassen_ab.argtypes = [dbl, vp, i64, vp, i64, dbl, vp, i64, i64, i64, i64]
     L.fmm_gpu_split_workspace_size.restype = ctypes.c_size_t
@@ -374,6 +378,41 @@ def batch_dgemm(problems, workspace=None, stream=None) -> None:
         workspace = torch.empty(max(need, 256), dtype=torch.uint8, device="cuda")
     _check(lib().fmm_gpu_batch_dgemm(count, arr, workspace.data_ptr(), workspace.numel(), _stream_ptr(stream)),
            "fmm_gpu_batch_dgemm")
+
+
+def split_strassen_ab_ex(alpha: float, A, B, beta: float, C, fmm: FmmT | None = None, levels: int = 1,
+                         slices: int = 6, fmt: str = "bf16") -> None:
+    """The split form on host arrays (Fortran-order numpy float64, or any
+    object exposing a host pointer through ``ctypes.data`` / ``data_ptr()``
+    of a pinned CPU tensor): C updated in place, synchronously, with the
+    host<->device copies overlapped with the device work."""
+    import numpy as np
+
+    def info(x, name):
+        if isinstance(x, np.ndarray):
+            if x.dtype != np.float64 or x.ndim != 2 or not (x.flags.f_contiguous or x.size == 0):
+                raise ValueError(f"{name} must be a 2-D Fortran-order float64 array")
+            return x.ctypes.data, x.shape
+        if getattr(x, "is_cuda", True) or str(x.dtype) != "torch.float64" or x.dim() != 2:
+            raise ValueError(f"{name} must be a 2-D float64 host array or CPU tensor")
+        if x.numel() > 0 and (x.stride(0) != 1 or x.stride(1) < max(x.shape[0], 1)):
+            raise ValueError(f"{name} must be column-major")
+        return x.data_ptr(), tuple(x.shape)
+
+    pa, (m, k) = info(A, "A")
+    pb, (kb, n) = info(B, "B")
+    pc, sc = info(C, "C")
+    if kb != k or sc != (m, n):
+        raise ValueError("shape mismatch")
+    st = lib().fmm_gpu_split_strassen_ab_ex(alpha, pa, max(m, 1), pb, max(k, 1), beta, pc, max(m, 1), m, n, k,
+                                            fmm if fmm is not None else FmmT(), levels if fmm is not None else 0,
+                                            slices, _fmt(fmt))
+    _check(st, "fmm_gpu_split_strassen_ab_ex")
+
+
+def release_host_buffers() -> None:
+    """Frees the device buffers kept by split_strassen_ab_ex on this device."""
+    lib().fmm_gpu_release_host_buffers()
 
 
 def bli_strassen_ab_ex(alpha: float, A, B, beta: float, C, fmm: FmmT) -> None:

@@ -421,6 +421,28 @@ extern "C" int fmm_gpu_split_dgemm(const fmm_t* fmm, int levels, int64_t m, int6
                                    FMM_SPLIT_BF16, workspace, workspace_bytes, stream);
 }
 
+extern "C" int fmm_gpu_split_strassen_ab_ex(double alpha, const double* A, int64_t lda, const double* B,
+                                            int64_t ldb, double beta, double* C, int64_t ldc, int64_t m,
+                                            int64_t n, int64_t k, fmm_t fmm, int levels, int slices, int format)
+{
+    int rc = check_gemm_args(m, n, k, A, lda, B, ldb, C, ldc);
+    if (rc != FMM_OK) return rc;
+    if (format != FMM_SPLIT_BF16 && format != FMM_SPLIT_FP8_E4M3) return FMM_ERR_ARG;
+    if (slices < 2 || slices > (format ? 12 : 8)) return FMM_ERR_ARG;
+    fmm_t flat;
+    int owned = 0;
+    rc = fmm_flatten(levels > 0 ? &fmm : nullptr, levels, &flat, &owned);
+    if (rc != FMM_OK) return rc;
+    AlgView alg;
+    rc = fmm_alg_get(&flat, &alg);
+    if (owned) free_fmm(flat);
+    if (rc != FMM_OK) return rc;
+    if (fmm_device_error_word() == nullptr) return FMM_ERR_CUDA;
+    return fmm_split_host(alg, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, slices, format);
+}
+
+extern "C" void fmm_gpu_release_host_buffers(void) { fmm_split_host_release(); }
+
 extern "C" int fmm_gpu_split_dgemm_fmt(const fmm_t* fmm, int levels, int64_t m, int64_t n, int64_t k,
                                        double alpha, const double* A, int64_t lda, const double* B, int64_t ldb,
                                        double beta, double* C, int64_t ldc, int slices, int format,

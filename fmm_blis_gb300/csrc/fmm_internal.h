@@ -88,6 +88,10 @@ int fmm_f64_batch_launch(int count, const F64BatchItem* items, void* ws, size_t 
 /* split form (fmm_split.cu) */
 /* fmt: 0 = BF16 slices, 1 = FP8-E4M3 slices */
 size_t fmm_split_ws_bytes(const AlgView& alg, int64_t m, int64_t n, int64_t k, int slices, int fmt);
+/* split form on host buffers, copies overlapped with the device work */
+int fmm_split_host(const AlgView& alg, int64_t m, int64_t n, int64_t k, double alpha, const double* A,
+                   int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc, int s, int fmt);
+void fmm_split_host_release();
 int fmm_split_launch(const AlgView& alg, int64_t m, int64_t n, int64_t k,
                      double alpha, const double* A, int64_t lda,
                      const double* B, int64_t ldb, double beta, double* C, int64_t ldc,

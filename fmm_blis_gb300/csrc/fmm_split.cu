@@ -295,21 +295,24 @@ __global__ void bmax_kernel(const double* __restrict__ B, int64_t ldb, int64_t k
     if (lane == 0) bmax[(int64_t)b * n + j] = mx;
 }
 
-/* Row exponents of S_r (rows < m_pad) and column exponents of T_r for the
- * products r = r0 + blockIdx.y of a group, into e_row[q][m_pad] and
- * f_col[q][n_pad]. */
+/* Row exponents of S_r (index < m_pad) and column exponents of T_r (index
+ * m_pad + j) for the products r = r0 + blockIdx.y of a group, into
+ * e_row[q][m_pad] and f_col[q][n_pad]; a launch covers the indices
+ * [first, end), so the row side (needs only amax) and the column side (needs
+ * only bmax) can run on different streams. */
 __global__ void exps_kernel(const int* __restrict__ tab, int r0, int64_t m, int64_t n, int64_t k,
                             int64_t m_pad, int64_t n_pad,
                             const unsigned long long* __restrict__ amax,
                             const unsigned long long* __restrict__ bmax,
-                            int* __restrict__ e_row, int* __restrict__ f_col)
+                            int* __restrict__ e_row, int* __restrict__ f_col, int64_t first, int64_t end)
 {
     const Tab t = tab_view(tab);
     const int r = r0 + (int)blockIdx.y;
     e_row += (int64_t)blockIdx.y * m_pad;
     f_col += (int64_t)blockIdx.y * n_pad;
     const int64_t me = (m + t.mt - 1) / t.mt, ne = (n + t.nt - 1) / t.nt;
-    const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t idx = first + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (idx >= end) return;
     if (idx < m_pad) {
         const int64_t i = idx;
         double bnd = 0.0;
@@ -1569,6 +1572,7 @@ struct SidePool {
     cudaStream_t s[kSideStreams];
     cudaEvent_t fork;
     cudaEvent_t join[kSideStreams];
+    cudaEvent_t gate[3];   /* host-buffer calls: A, B and C on the device */
 };
 
 std::mutex g_side_mu, g_side_use;
@@ -1584,6 +1588,7 @@ SidePool* side_pool()
     SidePool* p = new SidePool;
     p->device = dev;
     bool ok = cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming) == cudaSuccess;
+    for (int i = 0; i < 3 && ok; ++i) ok = cudaEventCreateWithFlags(&p->gate[i], cudaEventDisableTiming) == cudaSuccess;
     for (int i = 0; i < kSideStreams && ok; ++i)
         ok = cudaStreamCreateWithFlags(&p->s[i], cudaStreamNonBlocking) == cudaSuccess &&
              cudaEventCreateWithFlags(&p->join[i], cudaEventDisableTiming) == cudaSuccess;
@@ -1626,24 +1631,37 @@ int side_join1(SidePool* p, cudaStream_t st)
     return cudaStreamWaitEvent(st, p->join[0], 0) == cudaSuccess ? FMM_OK : FMM_ERR_CUDA;
 }
 
-/* C := beta*C and the per-sub-block row/column maxima of A and B */
-static int job_prologue(SplitJob& j, cudaStream_t st, SidePool* sp = nullptr)
+/* per-sub-block row maxima of A (amax) */
+static int job_maxima_a(SplitJob& j, cudaStream_t st)
 {
-    int rc = fmm_scale_c(j.m, j.n, j.beta, j.C, j.ldc, st);
-    if (rc != FMM_OK || j.trivial) return rc;
     unsigned long long* amax = (unsigned long long*)(j.w + j.L.amax);
-    unsigned long long* bmax = (unsigned long long*)(j.w + j.L.bmax);
     if (cudaMemsetAsync(amax, 0, sizeof(unsigned long long) * (size_t)j.alg.kt * (size_t)j.m, st) != cudaSuccess)
         return FMM_ERR_CUDA;
     const int cpb = 256;
     dim3 grid((unsigned)((j.m + 255) / 256), (unsigned)j.alg.kt, (unsigned)((j.d.ke + cpb - 1) / cpb));
     amax_kernel<<<grid, 256, 0, st>>>(j.A, j.lda, j.m, j.k, j.alg.kt, amax, cpb);
+    fmm_count_launch(1);
+    return FMM_OK;
+}
+
+/* per-sub-block column maxima of B (bmax) */
+static void job_maxima_b(SplitJob& j, cudaStream_t st)
+{
+    unsigned long long* bmax = (unsigned long long*)(j.w + j.L.bmax);
     const int64_t warps = j.n * j.alg.kt;
+    bmax_kernel<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, st>>>(j.B, j.ldb, j.k, j.n, j.alg.kt, bmax);
+    fmm_count_launch(1);
+}
+
+/* C := beta*C and the per-sub-block row/column maxima of A and B; with a
+ * side pool the B maxima run on its stream s[0], which job_pack joins back */
+static int job_prologue(SplitJob& j, cudaStream_t st, SidePool* sp = nullptr)
+{
+    int rc = fmm_scale_c(j.m, j.n, j.beta, j.C, j.ldc, st);
+    if (rc != FMM_OK || j.trivial) return rc;
+    if ((rc = job_maxima_a(j, st)) != FMM_OK) return rc;
     if (sp && (rc = side_fork1(sp, st)) != FMM_OK) return rc;
-    bmax_kernel<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, sp ? sp->s[0] : st>>>(j.B, j.ldb, j.k, j.n,
-                                                                                      j.alg.kt, bmax);
-    if (sp && (rc = side_join1(sp, st)) != FMM_OK) return rc;
-    fmm_count_launch(2);
+    job_maxima_b(j, sp ? sp->s[0] : st);
     return FMM_OK;
 }
 
@@ -1663,14 +1681,19 @@ static int job_pack(SplitJob& j, int r0, int np, cudaStream_t st, SidePool* sp =
     /* one launch per kernel for the whole group (grid y holds the product of
      * the exponent pass; the pack grids' x extent np * tiles stays far below
      * 2^31 since np * s * max(m_pad, n_pad) < 2^31) */
-    exps_kernel<<<dim3((unsigned)((d.m_pad + d.n_pad + 255) / 256), (unsigned)np), 256, 0, st>>>(
-        j.alg.tab, r0, j.m, j.n, j.k, d.m_pad, d.n_pad, amax, bmax, e_row, f_col);
+    /* A side (row exponents, A slices) on st; B side (column exponents, B
+     * slices) on the side stream, after the B maxima queued there */
+    cudaStream_t stb = sp ? sp->s[0] : st;
+    exps_kernel<<<dim3((unsigned)((d.m_pad + 255) / 256), (unsigned)np), 256, 0, st>>>(
+        j.alg.tab, r0, j.m, j.n, j.k, d.m_pad, d.n_pad, amax, bmax, e_row, f_col, 0, d.m_pad);
     int rc;
     if (sp && (rc = side_fork1(sp, st)) != FMM_OK) return rc;
+    exps_kernel<<<dim3((unsigned)((d.n_pad + 255) / 256), (unsigned)np), 256, 0, stb>>>(
+        j.alg.tab, r0, j.m, j.n, j.k, d.m_pad, d.n_pad, amax, bmax, e_row, f_col, d.m_pad, d.m_pad + d.n_pad);
     launch_packs(j.fmt, j.s, j.alg.tab, r0, np, j.A, j.lda, j.B, j.ldb, j.m, j.n, j.k, d.m_pad, d.n_pad, d.k_pad, e_row,
-                 f_col, sa, sb, st, sp ? sp->s[0] : st);
+                 f_col, sa, sb, st, stb);
     if (sp && (rc = side_join1(sp, st)) != FMM_OK) return rc;
-    fmm_count_launch(3);
+    fmm_count_launch(4);
     return FMM_OK;
 }
 
@@ -1722,6 +1745,19 @@ static int64_t job_items(const SplitJob& j, int np, bool pair = false)
     return (int64_t)np * (j.d.m_pad / (pair ? kPairTileM : kTileM)) * (j.d.n_pad / kTileN);
 }
 
+static int launch_gemm(GemmLaunch& gl, int64_t nitems, int nprod_timed, cudaStream_t st, bool pair);
+
+/* one GEMM launch over the job's current product group */
+static int job_gemm(const SplitJob& j, int np, cudaStream_t st)
+{
+    GemmLaunch gl;
+    memset(&gl, 0, sizeof(gl));
+    gl.nprob = 1;
+    const bool pair = job_pair(j);
+    if (int rc = job_fill(j, gl.prob[0], np, 0, pair); rc != FMM_OK) return rc;
+    return launch_gemm(gl, job_items(j, np, pair), np, st, pair);
+}
+
 static void job_scatter(const SplitJob& j, int r0, int np, cudaStream_t st)
 {
     const int64_t elems = j.d.me * j.d.ne;   /* the largest part's extent */
@@ -1745,7 +1781,7 @@ static void job_scatter(const SplitJob& j, int r0, int np, cudaStream_t st)
     fmm_count_launch(1);
 }
 
-static int launch_gemm(GemmLaunch& gl, int64_t nitems, int nprod_timed, cudaStream_t st, bool pair = false)
+static int launch_gemm(GemmLaunch& gl, int64_t nitems, int nprod_timed, cudaStream_t st, bool pair)
 {
     static bool attr_set = false;
     if (!attr_set) {
@@ -1792,15 +1828,126 @@ static int split_launch_budget(const AlgView& alg, int64_t m, int64_t n, int64_t
     for (int r0 = 0; r0 < alg.R; r0 += G) {
         const int np = std::min(G, alg.R - r0);
         if ((rc = job_pack(j, r0, np, st, sp)) != FMM_OK) return rc;
-        GemmLaunch gl;
-        memset(&gl, 0, sizeof(gl));
-        gl.nprob = 1;
-        const bool pair = job_pair(j);
-        if ((rc = job_fill(j, gl.prob[0], np, 0, pair)) != FMM_OK) return rc;
-        if ((rc = launch_gemm(gl, job_items(j, np, pair), np, st, pair)) != FMM_OK) return rc;
+        if ((rc = job_gemm(j, np, st)) != FMM_OK) return rc;
         job_scatter(j, r0, np, st);
     }
     return cudaGetLastError() == cudaSuccess ? FMM_OK : FMM_ERR_CUDA;
+}
+
+/* ---------------------------------------------------------------------------
+ * Host-buffer entry.
+ *
+ * Operands in host memory: the call owns the device copies and overlaps the
+ * host<->device traffic with the device work. Copies run on s[1] in the
+ * order A, B, C; the A side (row maxima, row exponents, A slices) starts as
+ * soon as A has arrived, the B side on s[0] as soon as B has, and C is only
+ * needed by the scatter, so its upload runs under the GEMM. The host enqueues
+ * in the same order (copy A, A side, copy B, B side, GEMM, copy C), which keeps
+ * the overlap when a copy from pageable memory blocks the host until it is
+ * staged. The operand and workspace buffers are kept per device (grow-only)
+ * until fmm_gpu_release_host_buffers.
+ * ------------------------------------------------------------------------- */
+struct HostBuffers {
+    uint8_t* p = nullptr;
+    size_t bytes = 0;
+};
+static std::mutex g_hostbuf_mu;
+static HostBuffers g_hostbuf[64];
+
+static uint8_t* host_buffers(size_t bytes)
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+    HostBuffers& h = g_hostbuf[dev];
+    if (h.bytes >= bytes) return h.p;
+    if (h.p) cudaFree(h.p);
+    h.p = nullptr;
+    h.bytes = 0;
+    if (cudaMalloc(&h.p, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        h.p = nullptr;
+        return nullptr;
+    }
+    h.bytes = bytes;
+    return h.p;
+}
+
+static size_t align256(size_t b) { return (b + 255) / 256 * 256; }
+
+int fmm_split_host(const AlgView& alg, int64_t m, int64_t n, int64_t k, double alpha, const double* A,
+                   int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc, int s, int fmt)
+{
+    if (m == 0 || n == 0) return FMM_OK;
+    std::lock_guard<std::mutex> use(g_side_use);
+    std::lock_guard<std::mutex> buf(g_hostbuf_mu);
+    SidePool* sp = side_pool();
+    if (!sp) return FMM_ERR_CUDA;
+    cudaStream_t st = sp->s[2], cs = sp->s[1];
+    const int64_t ka = std::max<int64_t>(k, 1);
+    const bool trivial = k == 0 || alpha == 0.0;
+    if (trivial && beta == 1.0) return FMM_OK;
+    const size_t bA = trivial ? 0 : align256(sizeof(double) * (size_t)(m * ka));
+    const size_t bB = trivial ? 0 : align256(sizeof(double) * (size_t)(ka * n));
+    const size_t bC = align256(sizeof(double) * (size_t)(m * n));
+    const size_t wsb = trivial ? 0 : align256(fmm_split_ws_bytes(alg, m, n, k, s, fmt));
+    uint8_t* base = host_buffers(bA + bB + bC + wsb);
+    if (!base) return FMM_ERR_ALLOC;
+    double* dA = (double*)base;
+    double* dB = (double*)(base + bA);
+    double* dC = (double*)(base + bA + bB);
+    uint8_t* ws = base + bA + bB + bC;
+    const size_t row = sizeof(double) * (size_t)m;
+    auto ok = [](cudaError_t e) { return e == cudaSuccess; };
+    if (trivial) {
+        /* C := beta*C */
+        if (beta != 0.0 && !ok(cudaMemcpy2DAsync(dC, row, C, sizeof(double) * ldc, row, n, cudaMemcpyHostToDevice, st)))
+            return FMM_ERR_CUDA;
+        if (int rc = fmm_scale_c(m, n, beta, dC, m, st); rc != FMM_OK) return rc;
+    } else {
+        SplitJob j;
+        int rc = job_init(j, alg, m, n, k, alpha, dA, m, dB, ka, 0.0, dC, m, s, fmt);
+        if (rc != FMM_OK) return rc;
+        if ((rc = job_bind(j, ws, wsb, wsb)) != FMM_OK) return rc;
+        /* A, then the A side's maxima */
+        if (!ok(cudaMemcpy2DAsync(dA, row, A, sizeof(double) * lda, row, k, cudaMemcpyHostToDevice, cs)) ||
+            !ok(cudaEventRecord(sp->gate[0], cs)) || !ok(cudaStreamWaitEvent(st, sp->gate[0], 0)))
+            return FMM_ERR_CUDA;
+        if ((rc = job_maxima_a(j, st)) != FMM_OK) return rc;
+        /* B, then the B side's maxima on s[0] */
+        if (!ok(cudaMemcpy2DAsync(dB, sizeof(double) * k, B, sizeof(double) * ldb, sizeof(double) * k, n,
+                                  cudaMemcpyHostToDevice, cs)) ||
+            !ok(cudaEventRecord(sp->gate[1], cs)) || !ok(cudaStreamWaitEvent(sp->s[0], sp->gate[1], 0)))
+            return FMM_ERR_CUDA;
+        job_maxima_b(j, sp->s[0]);
+        const int G = j.L.group;
+        for (int r0 = 0; r0 < alg.R; r0 += G) {
+            const int np = std::min(G, alg.R - r0);
+            if ((rc = job_pack(j, r0, np, st, sp)) != FMM_OK) return rc;
+            if ((rc = job_gemm(j, np, st)) != FMM_OK) return rc;
+            if (r0 == 0) {
+                /* C under the first GEMM, then C := beta*C before the first scatter */
+                if (beta != 0.0 &&
+                    (!ok(cudaMemcpy2DAsync(dC, row, C, sizeof(double) * ldc, row, n, cudaMemcpyHostToDevice, cs)) ||
+                     !ok(cudaEventRecord(sp->gate[2], cs)) || !ok(cudaStreamWaitEvent(st, sp->gate[2], 0))))
+                    return FMM_ERR_CUDA;
+                if ((rc = fmm_scale_c(m, n, beta, dC, m, st)) != FMM_OK) return rc;
+            }
+            job_scatter(j, r0, np, st);
+        }
+    }
+    if (!ok(cudaMemcpy2DAsync(C, sizeof(double) * ldc, dC, row, row, n, cudaMemcpyDeviceToHost, st)) ||
+        !ok(cudaStreamSynchronize(st)))
+        return FMM_ERR_CUDA;
+    return cudaGetLastError() == cudaSuccess ? FMM_OK : FMM_ERR_CUDA;
+}
+
+void fmm_split_host_release()
+{
+    std::lock_guard<std::mutex> buf(g_hostbuf_mu);
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return;
+    if (g_hostbuf[dev].p) cudaFree(g_hostbuf[dev].p);
+    g_hostbuf[dev] = HostBuffers();
 }
 
 /* Batched split-form GEMMs: problems are taken in order into waves of at

@@ -216,6 +216,26 @@ int fmm_gpu_split_dgemm_fmt(const fmm_t* fmm, int levels,
                             int slices, int format, void* workspace, size_t workspace_bytes,
                             void* stream);
 
+/* The split form on HOST buffers: bli_strassen_ab_ex's operands (column-major
+ * host pointers with leading dimensions, as fmm_gpu_strassen_ab_ex takes
+ * them) multiplied in the split-precision form with `levels` levels of `fmm`
+ * (0: classical), `slices` digit slices of `format` (FMM_SPLIT_*).
+ * Synchronous: returns when C holds the result. The copies overlap the
+ * device work: B and C travel while A's slices are formed and under the
+ * GEMM. Pinned host memory copies fastest; pageable memory works too. The
+ * device copies and the workspace are kept between calls (grow-only, per
+ * device) until fmm_gpu_release_host_buffers. The result equals
+ * fmm_gpu_split_dgemm_fmt's on the same values bit for bit. No counterpart
+ * in the reference. */
+int fmm_gpu_split_strassen_ab_ex(double alpha, const double* A, int64_t lda,
+                                 const double* B, int64_t ldb,
+                                 double beta, double* C, int64_t ldc,
+                                 int64_t m, int64_t n, int64_t k,
+                                 fmm_t fmm, int levels, int slices, int format);
+
+/* Frees the current device's buffers kept by fmm_gpu_split_strassen_ab_ex. */
+void fmm_gpu_release_host_buffers(void);
+
 /* ------------------------------------------------------- GPU, batched -- */
 
 /* One GEMM of a batch: C := beta*C + alpha*A*B with `levels` levels of `fmm`

@@ -37,3 +37,18 @@ def test_split_pair_rows_knob(fmm):
         assert fmm.set_split_pair_rows(1024) == 2**31 - 1
     finally:
         fmm.set_split_pair_rows(prev)
+
+
+def test_split_host_call_rejects_bad_arguments(fmm):
+    """Argument checks of the host-buffer split call come before any device
+    work, so they hold without a GPU."""
+    import numpy as np
+    L = fmm.lib()
+    A = np.zeros((4, 4), order="F")
+    f = fmm.strassen_fmm()
+    args = (1.0, A.ctypes.data, 4, A.ctypes.data, 4, 1.0, A.ctypes.data, 4, 4, 4, 4, f, 1)
+    assert L.fmm_gpu_split_strassen_ab_ex(*args, 13, 1) == 1     # FP8 slices 2..12
+    assert L.fmm_gpu_split_strassen_ab_ex(*args, 9, 0) == 1      # BF16 slices 2..8
+    assert L.fmm_gpu_split_strassen_ab_ex(*args, 6, 2) == 1      # unknown format
+    bad_ld = (1.0, A.ctypes.data, 3, A.ctypes.data, 4, 1.0, A.ctypes.data, 4, 4, 4, 4, f, 1, 6, 0)
+    assert L.fmm_gpu_split_strassen_ab_ex(*bad_ld) == 1          # lda < m

@@ -1,0 +1,95 @@
+"""The split form on host buffers (fmm_gpu_split_strassen_ab_ex): operands in
+host memory, copies overlapped with the device work inside the call. Every
+result equals the device-pointer call's (fmm_gpu_split_dgemm_fmt) bit for bit
+and, at sizes the oracle finishes, the oracle's restatement."""
+import numpy as np
+import pytest
+
+from conftest import COEFFS, rand
+from gpu_util import to_dev, to_host
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    import torch
+    assert torch.cuda.is_available()
+    return torch
+
+
+def device_call(fmm, f, levels, A, B, C, s, fmt, alpha=1.0, beta=1.0):
+    dC = to_dev(C)
+    fmm.split_dgemm(to_dev(A), to_dev(B), dC, f, levels, s, fmt=fmt, alpha=alpha, beta=beta)
+    return to_host(dC)
+
+
+@pytest.mark.parametrize("fmt,s", [("bf16", 6), ("fp8", 9)])
+@pytest.mark.parametrize("shape", [(1, 1, 1), (65, 70, 33), (300, 129, 260)])
+def test_host_call_matches_oracle(fmm, orc, algs, torch_cuda, fmt, s, shape):
+    m, n, k = shape
+    A, B, C = rand(m, k, 501), rand(k, n, 502), rand(m, n, 503)
+    got = C.copy(order="F")
+    fmm.split_strassen_ab_ex(0.5, A, B, -1.25, got, fmm.strassen_fmm(), 1, s, fmt)
+    want = orc.split_fmm_dgemm(algs["222"], A, B, C.copy(order="F"), s, 0.5, -1.25, fmt=fmt)
+    assert np.array_equal(got, want)
+    assert fmm.take_device_error() == 0
+
+
+@pytest.mark.parametrize("fmt,s,levels", [("bf16", 6, 2), ("fp8", 10, 1), ("bf16", 4, 0)])
+def test_host_call_equals_device_call(fmm, torch_cuda, fmt, s, levels):
+    """2100 x 1900 x 1500 (pair tiles at levels 0 and 1): the same bits as
+    the device-pointer call on the same values."""
+    m, n, k = 2100, 1900, 1500
+    A, B, C = rand(m, k, 511), rand(k, n, 512), rand(m, n, 513)
+    f = fmm.strassen_fmm() if levels else None
+    want = device_call(fmm, f, levels, A, B, C, s, fmt)
+    got = C.copy(order="F")
+    fmm.split_strassen_ab_ex(1.0, A, B, 1.0, got, f, levels, s, fmt)
+    assert np.array_equal(got, want)
+
+
+def test_host_call_pinned_tensors_and_leading_dims(fmm, torch_cuda):
+    """Pinned CPU tensors; operands that are column blocks of larger arrays
+    (leading dimension > rows) through the C ABI."""
+    import ctypes
+    import torch
+    m, n, k = 700, 500, 900
+    A, B, C = rand(m, k, 521), rand(k, n, 522), rand(m, n, 523)
+    want = device_call(fmm, fmm.strassen_fmm(), 1, A, B, C, 5, "bf16", 2.0, 0.5)
+    hA = torch.from_numpy(A.T.copy()).pin_memory().t()
+    hB = torch.from_numpy(B.T.copy()).pin_memory().t()
+    hC = torch.from_numpy(C.T.copy()).pin_memory().t()
+    fmm.split_strassen_ab_ex(2.0, hA, hB, 0.5, hC, fmm.strassen_fmm(), 1, 5, "bf16")
+    assert np.array_equal(hC.numpy(), want)
+    # leading dimensions larger than the row counts
+    Ab = np.zeros((m + 9, k), order="F"); Ab[:m] = A
+    Bb = np.zeros((k + 3, n), order="F"); Bb[:k] = B
+    Cb = np.full((m + 5, n), 7.0, order="F"); Cb[:m] = C
+    L = fmm.lib()
+    st = L.fmm_gpu_split_strassen_ab_ex(2.0, Ab.ctypes.data, m + 9, Bb.ctypes.data, k + 3, 0.5, Cb.ctypes.data,
+                                        m + 5, m, n, k, fmm.strassen_fmm(), 1, 5, 0)
+    assert st == 0
+    assert np.array_equal(Cb[:m], want)
+    assert np.all(Cb[m:] == 7.0)
+
+
+def test_host_call_scalar_cases(fmm, torch_cuda):
+    m, n, k = 130, 70, 90
+    A, B, C = rand(m, k, 531), rand(k, n, 532), rand(m, n, 533)
+    f = fmm.strassen_fmm()
+    # beta = 0: C's old values (NaN here) are not read
+    Cn = np.full((m, n), np.nan, order="F")
+    fmm.split_strassen_ab_ex(1.0, A, B, 0.0, Cn, f, 1, 6)
+    assert np.array_equal(Cn, device_call(fmm, f, 1, A, B, np.zeros((m, n), order="F"), 6, "bf16", 1.0, 0.0))
+    # alpha = 0 and k = 0: C := beta*C
+    Cs = C.copy(order="F")
+    fmm.split_strassen_ab_ex(0.0, A, B, -2.0, Cs, f, 1, 6)
+    assert np.array_equal(Cs, -2.0 * C)
+    Ck = C.copy(order="F")
+    fmm.split_strassen_ab_ex(1.0, np.zeros((m, 0), order="F"), np.zeros((0, n), order="F"), 3.0, Ck, f, 1, 6)
+    assert np.array_equal(Ck, 3.0 * C)
+    # m = 0: nothing to do
+    fmm.split_strassen_ab_ex(1.0, np.zeros((0, k), order="F"), B, 1.0, np.zeros((0, n), order="F"), f, 1, 6)
+    fmm.release_host_buffers()
+    assert fmm.take_device_error() == 0
