@@ -260,10 +260,22 @@ __global__ void amax_kernel(const double* __restrict__ A, int64_t lda, int64_t m
     const int64_t c0 = (int64_t)blockIdx.z * cols_per_block;
     if (c0 >= cl) return;
     const int64_t c1 = cl < c0 + cols_per_block ? cl : c0 + cols_per_block;
+    const double* col = A + i + (co + c0) * lda;
+    const int nc = (int)(c1 - c0);
     unsigned long long mx = 0;
-    for (int64_t c = c0; c < c1; ++c) {
+    int c = 0;
+    for (; c + 8 <= nc; c += 8) {   /* eight independent loads in flight */
+        unsigned long long v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+            v[u] = (unsigned long long)__double_as_longlong(__ldg(col + (int64_t)(c + u) * lda)) &
+                   0x7fffffffffffffffull;
+#pragma unroll
+        for (int u = 0; u < 8; ++u) mx = v[u] > mx ? v[u] : mx;
+    }
+    for (; c < nc; ++c) {
         const unsigned long long v =
-            (unsigned long long)__double_as_longlong(A[i + (co + c) * lda]) & 0x7fffffffffffffffull;
+            (unsigned long long)__double_as_longlong(__ldg(col + (int64_t)c * lda)) & 0x7fffffffffffffffull;
         mx = v > mx ? v : mx;
     }
     atomicMax(&amax[(int64_t)b * m + i], mx);
@@ -1241,6 +1253,7 @@ scatter_all_kernel(const int* __restrict__ tab, int r0, int nprod, int64_t m, in
                    int64_t ldc)
 {
     extern __shared__ double sm_all[];
+    __shared__ int geo[4][64];           /* per sub-block p: ro, rl, co, cl */
     const Tab t = tab_view(tab);
     const int P = t.mt * t.nt, T = (int)blockDim.x, tid = (int)threadIdx.x;
     const int eb = t.w_off[r0], E = t.w_off[r0 + nprod] - eb;
@@ -1253,19 +1266,21 @@ scatter_all_kernel(const int* __restrict__ tab, int r0, int nprod, int64_t m, in
         lam[x] = alpha * (double)t.w_ent[2 * (eb + x) + 1];
     }
     for (int x = tid; x <= nprod; x += T) off[x] = t.w_off[r0 + x] - eb;
+    for (int p = tid; p < P; p += T) {
+        fmm_part_geom32((int)m, t.mt, p / t.nt, &geo[0][p], &geo[1][p]);
+        fmm_part_geom32((int)n, t.nt, p % t.nt, &geo[2][p], &geo[3][p]);
+    }
     __syncthreads();
-    const int me = (int)((m + t.mt - 1) / t.mt), ne = (int)((n + t.nt - 1) / t.nt);
+    const uint32_t me = (uint32_t)((m + t.mt - 1) / t.mt), ne = (uint32_t)((n + t.nt - 1) / t.nt);
+    /* me * ne < 2^32 (checked on the host), so the element index fits 32 bits */
     const uint64_t idx = (uint64_t)blockIdx.x * (uint64_t)T + (uint64_t)tid;
     if (idx >= (uint64_t)me * (uint64_t)ne) return;
-    const int i = (int)(idx % (uint64_t)me), j = (int)(idx / (uint64_t)me);
+    const int i = (int)((uint32_t)idx % me), j = (int)((uint32_t)idx / me);
     uint64_t live = 0;
     for (int p = 0; p < P; ++p) {
-        int ro, rl, co, cl;
-        fmm_part_geom32((int)m, t.mt, p / t.nt, &ro, &rl);
-        fmm_part_geom32((int)n, t.nt, p % t.nt, &co, &cl);
-        if (i < rl && j < cl) {
+        if (i < geo[1][p] && j < geo[3][p]) {
             live |= 1ull << p;
-            cs[p * T + tid] = C[ro + i + (int64_t)(co + j) * ldc];
+            cs[p * T + tid] = C[geo[0][p] + i + (int64_t)(geo[2][p] + j) * ldc];
         }
     }
     const int64_t zij = (int64_t)j * m_pad + i;
@@ -1300,13 +1315,8 @@ scatter_all_kernel(const int* __restrict__ tab, int r0, int nprod, int64_t m, in
             if ((live >> p) & 1ull) cs[p * T + tid] = fma(lam[x], M, cs[p * T + tid]);
         }
     }
-    for (int p = 0; p < P; ++p) {
-        if (!((live >> p) & 1ull)) continue;
-        int ro, rl, co, cl;
-        fmm_part_geom32((int)m, t.mt, p / t.nt, &ro, &rl);
-        fmm_part_geom32((int)n, t.nt, p % t.nt, &co, &cl);
-        C[ro + i + (int64_t)(co + j) * ldc] = cs[p * T + tid];
-    }
+    for (int p = 0; p < P; ++p)
+        if ((live >> p) & 1ull) C[geo[0][p] + i + (int64_t)(geo[2][p] + j) * ldc] = cs[p * T + tid];
 }
 
 /* --------------------------------------------------------- host -------- */
@@ -1637,7 +1647,11 @@ static int job_maxima_a(SplitJob& j, cudaStream_t st)
     unsigned long long* amax = (unsigned long long*)(j.w + j.L.amax);
     if (cudaMemsetAsync(amax, 0, sizeof(unsigned long long) * (size_t)j.alg.kt * (size_t)j.m, st) != cudaSuccess)
         return FMM_ERR_CUDA;
-    const int cpb = 256;
+    /* columns per block: 256, halved (down to 32) while the grid has fewer
+     * than 8 blocks per SM, so short-and-wide A still fills the GPU */
+    const int64_t rows_blocks = (j.m + 255) / 256 * j.alg.kt;
+    int cpb = 256;
+    while (cpb > 32 && rows_blocks * ((j.d.ke + cpb - 1) / cpb) < 8 * 152) cpb /= 2;
     dim3 grid((unsigned)((j.m + 255) / 256), (unsigned)j.alg.kt, (unsigned)((j.d.ke + cpb - 1) / cpb));
     amax_kernel<<<grid, 256, 0, st>>>(j.A, j.lda, j.m, j.k, j.alg.kt, amax, cpb);
     fmm_count_launch(1);
@@ -1762,13 +1776,14 @@ static void job_scatter(const SplitJob& j, int r0, int np, cudaStream_t st)
 {
     const int64_t elems = j.d.me * j.d.ne;   /* the largest part's extent */
     /* element-major form when the sub-block values and the group's W entries
-     * fit: threads per block T = 32 KB / (8 P), a multiple of 32, at least 32 */
+     * fit beside the kernel's 1 KB of static geometry in 48 KB: threads per
+     * block T = 32 KB / (8 P), a multiple of 32, at least 32 */
     const Tab ht = tab_view(j.alg.htab);
     const int P = j.alg.mt * j.alg.nt;
     const int E = ht.w_off[r0 + np] - ht.w_off[r0];
     int T = std::min(256, kScatterAllSmem / (8 * P)) / 32 * 32;
     const size_t smem = (size_t)P * std::max(T, 0) * 8 + (size_t)E * 12 + (size_t)(np + 1) * 4;
-    if (P <= 64 && T >= 32 && smem <= 48 * 1024) {
+    if (P <= 64 && T >= 32 && smem <= 47 * 1024) {
         scatter_all_kernel<<<(unsigned)((elems + T - 1) / T), (unsigned)T, smem, st>>>(
             j.alg.tab, r0, np, j.m, j.n, (int)j.d.m_pad, (int)j.d.n_pad, job_ebase(j), j.alpha,
             (const int64_t*)(j.w + j.L.z), (const int*)(j.w + j.L.erow), (const int*)(j.w + j.L.fcol), j.C, j.ldc);
