@@ -281,16 +281,17 @@ __global__ void amax_kernel(const double* __restrict__ A, int64_t lda, int64_t m
     atomicMax(&amax[(int64_t)b * m + i], mx);
 }
 
-/* bmax[b*n + j] = max over the rows of k-block b of |B[:, j]|; one warp per
- * (j, b). */
+/* bmax[b*n + j] = max over the rows of k-block b of |B[:, j]| for the columns
+ * j in [c0, c1); one warp per (j, b). */
 __global__ void bmax_kernel(const double* __restrict__ B, int64_t ldb, int64_t k, int64_t n,
-                            int kt, unsigned long long* __restrict__ bmax)
+                            int kt, unsigned long long* __restrict__ bmax, int64_t c0, int64_t c1)
 {
     const int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / 32;
     const int lane = threadIdx.x % 32;
-    if (w >= n * kt) return;
-    const int64_t j = w % n;
-    const int b = (int)(w / n);
+    const int64_t nc = c1 - c0;
+    if (w >= nc * kt) return;
+    const int64_t j = c0 + w % nc;
+    const int b = (int)(w / nc);
     int64_t ro, rl;
     fmm_part_geom(k, kt, b, &ro, &rl);
     unsigned long long mx = 0;
@@ -488,7 +489,7 @@ template <int S, int DB>
 __global__ void __launch_bounds__(256)
 pack_b_kernel(const int* __restrict__ tab, int r0, int np, const double* __restrict__ B, int64_t ldb,
               int64_t k, int64_t n, int64_t n_pad, int64_t k_pad,
-              const int* __restrict__ f_col, uint8_t* __restrict__ sb)
+              const int* __restrict__ f_col, uint8_t* __restrict__ sb, int64_t j_first)
 {
     __shared__ PEnt ent[kPackMaxEnt];
     const Tab t = tab_view(tab);
@@ -507,7 +508,7 @@ pack_b_kernel(const int* __restrict__ tab, int r0, int np, const double* __restr
     }
     __syncthreads();
     const int kg = threadIdx.x % 8;
-    const int64_t gj = (int64_t)(blockIdx.x / (unsigned)np) * 32 + threadIdx.x / 8;
+    const int64_t gj = j_first + (int64_t)(blockIdx.x / (unsigned)np) * 32 + threadIdx.x / 8;
     const int64_t p0 = (int64_t)blockIdx.y * 64 + kg * 8;
     double v8[8];
 #pragma unroll
@@ -539,16 +540,26 @@ pack_b_kernel(const int* __restrict__ tab, int r0, int np, const double* __restr
     store_digits8<S, DB>(sb, slice0 + gj * k_pad + p0, n_pad * k_pad, Y);
 }
 
+/* Which packs a launch_packs call issues: both sides, or one side only; the
+ * B side over the T_r columns [jb0, jb1) (multiples of 32, or jb1 = n_pad). */
+struct PackSel {
+    bool a = true, b = true;
+    int64_t jb0 = 0, jb1 = -1;
+};
+
 template <int S, int DB>
 void launch_packs_t(const int* tab, int r, int np, const double* A, int64_t lda, const double* B, int64_t ldb,
                     int64_t m, int64_t n, int64_t k, int64_t m_pad, int64_t n_pad, int64_t k_pad,
                     const int* e_row, const int* f_col, uint8_t* sa, uint8_t* sb, cudaStream_t st,
-                    cudaStream_t st_b)
+                    cudaStream_t st_b, const PackSel& sel)
 {
-    pack_a_kernel<S, DB><<<dim3((unsigned)(np * (m_pad / 64)), (unsigned)(k_pad / 64)), 256, 0, st>>>(
-        tab, r, np, A, lda, m, k, m_pad, k_pad, e_row, sa);
-    pack_b_kernel<S, DB><<<dim3((unsigned)(np * (n_pad / 32)), (unsigned)(k_pad / 64)), 256, 0, st_b>>>(
-        tab, r, np, B, ldb, k, n, n_pad, k_pad, f_col, sb);
+    if (sel.a)
+        pack_a_kernel<S, DB><<<dim3((unsigned)(np * (m_pad / 64)), (unsigned)(k_pad / 64)), 256, 0, st>>>(
+            tab, r, np, A, lda, m, k, m_pad, k_pad, e_row, sa);
+    const int64_t j1 = sel.jb1 < 0 ? n_pad : sel.jb1;
+    if (sel.b && j1 > sel.jb0)
+        pack_b_kernel<S, DB><<<dim3((unsigned)(np * ((j1 - sel.jb0 + 31) / 32)), (unsigned)(k_pad / 64)), 256, 0,
+                               st_b>>>(tab, r, np, B, ldb, k, n, n_pad, k_pad, f_col, sb, sel.jb0);
 }
 
 /* digit slices of the products r .. r+np-1 (exponents already in place);
@@ -556,10 +567,11 @@ void launch_packs_t(const int* tab, int r, int np, const double* A, int64_t lda,
 void launch_packs(int fmt, int s, const int* tab, int r, int np, const double* A, int64_t lda, const double* B,
                   int64_t ldb, int64_t m, int64_t n, int64_t k, int64_t m_pad, int64_t n_pad,
                   int64_t k_pad, const int* e_row, const int* f_col, uint8_t* sa, uint8_t* sb,
-                  cudaStream_t st, cudaStream_t st_b)
+                  cudaStream_t st, cudaStream_t st_b, const PackSel& sel = PackSel())
 {
 #define FMM_PACKS(S_, DB_) \
-    launch_packs_t<S_, DB_>(tab, r, np, A, lda, B, ldb, m, n, k, m_pad, n_pad, k_pad, e_row, f_col, sa, sb, st, st_b)
+    launch_packs_t<S_, DB_>(tab, r, np, A, lda, B, ldb, m, n, k, m_pad, n_pad, k_pad, e_row, f_col, sa, sb, st, \
+                            st_b, sel)
     if (fmt == 0) {
         switch (s) {
         case 2: FMM_PACKS(2, 8); break;
@@ -1238,7 +1250,8 @@ scatter_kernel(const int* __restrict__ tab, int r0, int nprod, int64_t m, int64_
 }
 
 /* Multi-C epilogue, element-major: one thread per element (i, j) of the
- * product grid updates that element of every C sub-block p, so each product's
+ * product grid (element index i + j*m_e in [idx_first, idx_end)) updates that
+ * element of every C sub-block p, so each product's
  * Z_r[i,j] is read and converted once and shared by all sub-blocks it feeds.
  * The sub-blocks' running values live in shared memory (cs[p][thread]); for
  * every sub-block the updates still come in increasing product order, so the
@@ -1250,7 +1263,7 @@ __global__ void __launch_bounds__(256)
 scatter_all_kernel(const int* __restrict__ tab, int r0, int nprod, int64_t m, int64_t n,
                    int m_pad, int n_pad, int ebase, double alpha, const int64_t* __restrict__ Z,
                    const int* __restrict__ e_row, const int* __restrict__ f_col, double* __restrict__ C,
-                   int64_t ldc)
+                   int64_t ldc, uint64_t idx_first, uint64_t idx_end)
 {
     extern __shared__ double sm_all[];
     __shared__ int geo[4][64];           /* per sub-block p: ro, rl, co, cl */
@@ -1273,8 +1286,8 @@ scatter_all_kernel(const int* __restrict__ tab, int r0, int nprod, int64_t m, in
     __syncthreads();
     const uint32_t me = (uint32_t)((m + t.mt - 1) / t.mt), ne = (uint32_t)((n + t.nt - 1) / t.nt);
     /* me * ne < 2^32 (checked on the host), so the element index fits 32 bits */
-    const uint64_t idx = (uint64_t)blockIdx.x * (uint64_t)T + (uint64_t)tid;
-    if (idx >= (uint64_t)me * (uint64_t)ne) return;
+    const uint64_t idx = idx_first + (uint64_t)blockIdx.x * (uint64_t)T + (uint64_t)tid;
+    if (idx >= idx_end || idx >= (uint64_t)me * (uint64_t)ne) return;
     const int i = (int)((uint32_t)idx % me), j = (int)((uint32_t)idx / me);
     uint64_t live = 0;
     for (int p = 0; p < P; ++p) {
@@ -1583,6 +1596,7 @@ struct SidePool {
     cudaEvent_t fork;
     cudaEvent_t join[kSideStreams];
     cudaEvent_t gate[3];   /* host-buffer calls: A, B and C on the device */
+    cudaEvent_t chunk[16]; /* host-buffer calls: B chunks in, C chunks out */
 };
 
 std::mutex g_side_mu, g_side_use;
@@ -1599,6 +1613,7 @@ SidePool* side_pool()
     p->device = dev;
     bool ok = cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming) == cudaSuccess;
     for (int i = 0; i < 3 && ok; ++i) ok = cudaEventCreateWithFlags(&p->gate[i], cudaEventDisableTiming) == cudaSuccess;
+    for (int i = 0; i < 16 && ok; ++i) ok = cudaEventCreateWithFlags(&p->chunk[i], cudaEventDisableTiming) == cudaSuccess;
     for (int i = 0; i < kSideStreams && ok; ++i)
         ok = cudaStreamCreateWithFlags(&p->s[i], cudaStreamNonBlocking) == cudaSuccess &&
              cudaEventCreateWithFlags(&p->join[i], cudaEventDisableTiming) == cudaSuccess;
@@ -1658,12 +1673,15 @@ static int job_maxima_a(SplitJob& j, cudaStream_t st)
     return FMM_OK;
 }
 
-/* per-sub-block column maxima of B (bmax) */
-static void job_maxima_b(SplitJob& j, cudaStream_t st)
+/* per-sub-block column maxima of B (bmax) for the B columns [c0, c1) */
+static void job_maxima_b(SplitJob& j, cudaStream_t st, int64_t c0 = 0, int64_t c1 = -1)
 {
+    if (c1 < 0) c1 = j.n;
+    if (c1 <= c0) return;
     unsigned long long* bmax = (unsigned long long*)(j.w + j.L.bmax);
-    const int64_t warps = j.n * j.alg.kt;
-    bmax_kernel<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, st>>>(j.B, j.ldb, j.k, j.n, j.alg.kt, bmax);
+    const int64_t warps = (c1 - c0) * j.alg.kt;
+    bmax_kernel<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, st>>>(j.B, j.ldb, j.k, j.n, j.alg.kt, bmax, c0,
+                                                                      c1);
     fmm_count_launch(1);
 }
 
@@ -1709,6 +1727,39 @@ static int job_pack(SplitJob& j, int r0, int np, cudaStream_t st, SidePool* sp =
     if (sp && (rc = side_join1(sp, st)) != FMM_OK) return rc;
     fmm_count_launch(4);
     return FMM_OK;
+}
+
+/* The two sides of job_pack separately, for a caller that receives B in
+ * column chunks: the A side (row exponents, A slices) and the B side over
+ * the T_r columns [j0, j1) (multiples of 32, or j1 = n_pad). */
+static void job_pack_a(SplitJob& j, int r0, int np, cudaStream_t st)
+{
+    const Dims& d = j.d;
+    exps_kernel<<<dim3((unsigned)((d.m_pad + 255) / 256), (unsigned)np), 256, 0, st>>>(
+        j.alg.tab, r0, j.m, j.n, j.k, d.m_pad, d.n_pad, (unsigned long long*)(j.w + j.L.amax),
+        (unsigned long long*)(j.w + j.L.bmax), (int*)(j.w + j.L.erow), (int*)(j.w + j.L.fcol), 0, d.m_pad);
+    PackSel sel;
+    sel.b = false;
+    launch_packs(j.fmt, j.s, j.alg.tab, r0, np, j.A, j.lda, j.B, j.ldb, j.m, j.n, j.k, d.m_pad, d.n_pad, d.k_pad,
+                 (int*)(j.w + j.L.erow), (int*)(j.w + j.L.fcol), j.w + j.L.sa, j.w + j.L.sb, st, st, sel);
+    fmm_count_launch(2);
+}
+
+static void job_pack_b_cols(SplitJob& j, int r0, int np, int64_t j0, int64_t j1, cudaStream_t st)
+{
+    const Dims& d = j.d;
+    if (j1 <= j0) return;
+    exps_kernel<<<dim3((unsigned)((j1 - j0 + 255) / 256), (unsigned)np), 256, 0, st>>>(
+        j.alg.tab, r0, j.m, j.n, j.k, d.m_pad, d.n_pad, (unsigned long long*)(j.w + j.L.amax),
+        (unsigned long long*)(j.w + j.L.bmax), (int*)(j.w + j.L.erow), (int*)(j.w + j.L.fcol), d.m_pad + j0,
+        d.m_pad + j1);
+    PackSel sel;
+    sel.a = false;
+    sel.jb0 = j0;
+    sel.jb1 = j1;
+    launch_packs(j.fmt, j.s, j.alg.tab, r0, np, j.A, j.lda, j.B, j.ldb, j.m, j.n, j.k, d.m_pad, d.n_pad, d.k_pad,
+                 (int*)(j.w + j.L.erow), (int*)(j.w + j.L.fcol), j.w + j.L.sa, j.w + j.L.sb, st, st, sel);
+    fmm_count_launch(2);
 }
 
 /* G, the level whose unit Z counts in: BF16 6, or 7 when k_pad <= 128 (the
@@ -1772,6 +1823,35 @@ static int job_gemm(const SplitJob& j, int np, cudaStream_t st)
     return launch_gemm(gl, job_items(j, np, pair), np, st, pair);
 }
 
+/* the element-major scatter applies to this job (see job_scatter) */
+static bool job_scatter_all(const SplitJob& j, int r0, int np, int* T_out, size_t* smem_out)
+{
+    const Tab ht = tab_view(j.alg.htab);
+    const int P = j.alg.mt * j.alg.nt;
+    const int E = ht.w_off[r0 + np] - ht.w_off[r0];
+    const int T = std::min(256, kScatterAllSmem / (8 * P)) / 32 * 32;
+    const size_t smem = (size_t)P * std::max(T, 0) * 8 + (size_t)E * 12 + (size_t)(np + 1) * 4;
+    *T_out = T;
+    *smem_out = smem;
+    return P <= 64 && T >= 32 && smem <= 47 * 1024;
+}
+
+/* the C updates of products [r0, r0 + np) for the product-grid columns
+ * [j0, j1) (all rows), element-major form only */
+static void job_scatter_cols(const SplitJob& j, int r0, int np, int64_t j0, int64_t j1, cudaStream_t st)
+{
+    int T;
+    size_t smem;
+    job_scatter_all(j, r0, np, &T, &smem);
+    const uint64_t first = (uint64_t)j0 * (uint64_t)j.d.me, end = (uint64_t)j1 * (uint64_t)j.d.me;
+    if (end <= first) return;
+    scatter_all_kernel<<<(unsigned)((end - first + T - 1) / T), (unsigned)T, smem, st>>>(
+        j.alg.tab, r0, np, j.m, j.n, (int)j.d.m_pad, (int)j.d.n_pad, job_ebase(j), j.alpha,
+        (const int64_t*)(j.w + j.L.z), (const int*)(j.w + j.L.erow), (const int*)(j.w + j.L.fcol), j.C, j.ldc, first,
+        end);
+    fmm_count_launch(1);
+}
+
 static void job_scatter(const SplitJob& j, int r0, int np, cudaStream_t st)
 {
     const int64_t elems = j.d.me * j.d.ne;   /* the largest part's extent */
@@ -1786,7 +1866,8 @@ static void job_scatter(const SplitJob& j, int r0, int np, cudaStream_t st)
     if (P <= 64 && T >= 32 && smem <= 47 * 1024) {
         scatter_all_kernel<<<(unsigned)((elems + T - 1) / T), (unsigned)T, smem, st>>>(
             j.alg.tab, r0, np, j.m, j.n, (int)j.d.m_pad, (int)j.d.n_pad, job_ebase(j), j.alpha,
-            (const int64_t*)(j.w + j.L.z), (const int*)(j.w + j.L.erow), (const int*)(j.w + j.L.fcol), j.C, j.ldc);
+            (const int64_t*)(j.w + j.L.z), (const int*)(j.w + j.L.erow), (const int*)(j.w + j.L.fcol), j.C, j.ldc,
+            (uint64_t)0, (uint64_t)elems);
         fmm_count_launch(1);
         return;
     }
@@ -1889,6 +1970,8 @@ static uint8_t* host_buffers(size_t bytes)
 
 static size_t align256(size_t b) { return (b + 255) / 256 * 256; }
 
+constexpr int kChunks = 8;   /* B uploads and C downloads per host-buffer call */
+
 int fmm_split_host(const AlgView& alg, int64_t m, int64_t n, int64_t k, double alpha, const double* A,
                    int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc, int s, int fmt)
 {
@@ -1923,21 +2006,49 @@ int fmm_split_host(const AlgView& alg, int64_t m, int64_t n, int64_t k, double a
         int rc = job_init(j, alg, m, n, k, alpha, dA, m, dB, ka, 0.0, dC, m, s, fmt);
         if (rc != FMM_OK) return rc;
         if ((rc = job_bind(j, ws, wsb, wsb)) != FMM_OK) return rc;
-        /* A, then the A side's maxima */
+        const int G = j.L.group, nt = alg.nt;
+        const bool one_group = G >= alg.R;
+        cudaStream_t sb = sp->s[0];
+        /* A, then the A side's maxima (and, with one product group, its
+         * exponents and slices) */
         if (!ok(cudaMemcpy2DAsync(dA, row, A, sizeof(double) * lda, row, k, cudaMemcpyHostToDevice, cs)) ||
             !ok(cudaEventRecord(sp->gate[0], cs)) || !ok(cudaStreamWaitEvent(st, sp->gate[0], 0)))
             return FMM_ERR_CUDA;
         if ((rc = job_maxima_a(j, st)) != FMM_OK) return rc;
-        /* B, then the B side's maxima on s[0] */
-        if (!ok(cudaMemcpy2DAsync(dB, sizeof(double) * k, B, sizeof(double) * ldb, sizeof(double) * k, n,
-                                  cudaMemcpyHostToDevice, cs)) ||
-            !ok(cudaEventRecord(sp->gate[1], cs)) || !ok(cudaStreamWaitEvent(sp->s[0], sp->gate[1], 0)))
-            return FMM_ERR_CUDA;
-        job_maxima_b(j, sp->s[0]);
-        const int G = j.L.group;
+        if (one_group) job_pack_a(j, 0, alg.R, st);
+        /* B in kChunks chunks of T_r columns [j0, j1): chunk x holds the B
+         * columns co_c + [j0, j1) of every column part c, and the B side of
+         * those columns (maxima; with one group, exponents and slices) runs
+         * on s[0] as soon as the chunk has arrived */
+        const int64_t ne = j.d.ne, n_pad = j.d.n_pad;
+        const int64_t W = (ne + kChunks * 32 - 1) / (kChunks * 32) * 32;
+        int x = 0;
+        for (int64_t j0 = 0; j0 < n_pad; j0 += W, ++x) {
+            const int64_t j1 = std::min(j0 + W, n_pad);
+            for (int c = 0; c < nt; ++c) {
+                int64_t co, cl;
+                fmm_part_geom(n, nt, c, &co, &cl);
+                const int64_t a = co + std::min(j0, cl), b = co + std::min(j1, cl);
+                if (b > a && !ok(cudaMemcpy2DAsync(dB + a * k, sizeof(double) * k, B + a * ldb, sizeof(double) * ldb,
+                                                   sizeof(double) * k, b - a, cudaMemcpyHostToDevice, cs)))
+                    return FMM_ERR_CUDA;
+            }
+            if (!ok(cudaEventRecord(sp->chunk[x], cs)) || !ok(cudaStreamWaitEvent(sb, sp->chunk[x], 0)))
+                return FMM_ERR_CUDA;
+            for (int c = 0; c < nt; ++c) {
+                int64_t co, cl;
+                fmm_part_geom(n, nt, c, &co, &cl);
+                job_maxima_b(j, sb, co + std::min(j0, cl), co + std::min(j1, cl));
+            }
+            if (one_group) job_pack_b_cols(j, 0, alg.R, j0, j1, sb);
+        }
         for (int r0 = 0; r0 < alg.R; r0 += G) {
             const int np = std::min(G, alg.R - r0);
-            if ((rc = job_pack(j, r0, np, st, sp)) != FMM_OK) return rc;
+            if (one_group) {
+                if ((rc = side_join1(sp, st)) != FMM_OK) return rc;
+            } else if ((rc = job_pack(j, r0, np, st, sp)) != FMM_OK) {
+                return rc;
+            }
             if ((rc = job_gemm(j, np, st)) != FMM_OK) return rc;
             if (r0 == 0) {
                 /* C under the first GEMM, then C := beta*C before the first scatter */
@@ -1947,7 +2058,36 @@ int fmm_split_host(const AlgView& alg, int64_t m, int64_t n, int64_t k, double a
                     return FMM_ERR_CUDA;
                 if ((rc = fmm_scale_c(m, n, beta, dC, m, st)) != FMM_OK) return rc;
             }
-            job_scatter(j, r0, np, st);
+            int T;
+            size_t smem;
+            if (r0 + np < alg.R || !job_scatter_all(j, r0, np, &T, &smem)) {
+                job_scatter(j, r0, np, st);
+                continue;
+            }
+            /* the last group's C updates in column chunks of the product grid,
+             * each chunk's C columns (co_c + [j0, j1) of every column part)
+             * read back on s[1] while the next chunk is computed */
+            const int64_t W2 = (ne + kChunks - 1) / kChunks;
+            x = 0;
+            for (int64_t j0 = 0; j0 < ne; j0 += W2, ++x) {
+                const int64_t j1 = std::min(j0 + W2, ne);
+                job_scatter_cols(j, r0, np, j0, j1, st);
+                if (!ok(cudaEventRecord(sp->chunk[kChunks + x], st)) ||
+                    !ok(cudaStreamWaitEvent(cs, sp->chunk[kChunks + x], 0)))
+                    return FMM_ERR_CUDA;
+                for (int c = 0; c < nt; ++c) {
+                    int64_t co, cl;
+                    fmm_part_geom(n, nt, c, &co, &cl);
+                    const int64_t a = co + std::min(j0, cl), b = co + std::min(j1, cl);
+                    if (b > a && !ok(cudaMemcpy2DAsync(C + a * ldc, sizeof(double) * ldc, dC + a * m, row, row, b - a,
+                                                       cudaMemcpyDeviceToHost, cs)))
+                        return FMM_ERR_CUDA;
+                }
+            }
+            if (!ok(cudaEventRecord(sp->gate[1], cs)) || !ok(cudaStreamSynchronize(cs)) ||
+                !ok(cudaStreamSynchronize(st)))
+                return FMM_ERR_CUDA;
+            return cudaGetLastError() == cudaSuccess ? FMM_OK : FMM_ERR_CUDA;
         }
     }
     if (!ok(cudaMemcpy2DAsync(C, sizeof(double) * ldc, dC, row, row, n, cudaMemcpyDeviceToHost, st)) ||
