@@ -1588,13 +1588,17 @@ static int job_bind_group(SplitJob& j, void* ws, size_t ws_bytes, int G)
  * call, the B-side maxima and pack beside the A-side ones. Created once per
  * device; forked from and joined back to the caller's stream with events,
  * which a stream capture follows. One call at a time uses a pool (g_side_use). */
-constexpr int kSideStreams = 8;
+constexpr int kWaveStreams = 8;                  /* batched waves: pack streams, then scatter streams */
+constexpr int kSideStreams = 2 * kWaveStreams;
 
 struct SidePool {
     int device;
     cudaStream_t s[kSideStreams];
     cudaEvent_t fork;
     cudaEvent_t join[kSideStreams];
+    cudaEvent_t wave_pk[2][kWaveStreams];   /* a workspace half's packs done */
+    cudaEvent_t wave_gm[2];                 /* a workspace half's GEMM done */
+    cudaEvent_t wave_sc[2][kWaveStreams];   /* a workspace half's C updates done */
     cudaEvent_t gate[3];   /* host-buffer calls: A, B and C on the device */
     cudaEvent_t chunk[16]; /* host-buffer calls: B chunks in, C chunks out */
 };
@@ -1614,6 +1618,12 @@ SidePool* side_pool()
     bool ok = cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming) == cudaSuccess;
     for (int i = 0; i < 3 && ok; ++i) ok = cudaEventCreateWithFlags(&p->gate[i], cudaEventDisableTiming) == cudaSuccess;
     for (int i = 0; i < 16 && ok; ++i) ok = cudaEventCreateWithFlags(&p->chunk[i], cudaEventDisableTiming) == cudaSuccess;
+    for (int h = 0; h < 2 && ok; ++h) {
+        ok = cudaEventCreateWithFlags(&p->wave_gm[h], cudaEventDisableTiming) == cudaSuccess;
+        for (int i = 0; i < kWaveStreams && ok; ++i)
+            ok = cudaEventCreateWithFlags(&p->wave_pk[h][i], cudaEventDisableTiming) == cudaSuccess &&
+                 cudaEventCreateWithFlags(&p->wave_sc[h][i], cudaEventDisableTiming) == cudaSuccess;
+    }
     for (int i = 0; i < kSideStreams && ok; ++i)
         ok = cudaStreamCreateWithFlags(&p->s[i], cudaStreamNonBlocking) == cudaSuccess &&
              cudaEventCreateWithFlags(&p->join[i], cudaEventDisableTiming) == cudaSuccess;
@@ -2107,22 +2117,42 @@ void fmm_split_host_release()
 
 /* Batched split-form GEMMs: problems are taken in order into waves of at
  * most kMaxLaunchProblems whose whole workspaces (all products at once) fit
- * together; per wave every problem is packed, one persistent GEMM launch
- * covers all their (problem, product, tile) items, then each problem's C is
- * updated. A problem too large to share the workspace runs alone with
- * product groups. Every problem's result equals its single-call result. */
+ * together; per wave every problem is packed, one persistent GEMM launch per
+ * tile kind covers all their (problem, product, tile) items, then each
+ * problem's C is updated. When the batch needs more than one wave, waves
+ * alternate between the two halves of the workspace: a wave's maxima and
+ * packs (pack streams s[0..7]) wait only for the C updates of the wave before
+ * last, which used the same half, so they run beside the previous wave's GEMM
+ * and C updates (scatter streams s[8..15]); the GEMMs run in order on the
+ * caller's stream. A problem too large for its share of the workspace runs
+ * alone, after everything before it, with the whole workspace and product
+ * groups. Every problem's result equals its single-call result. */
 int fmm_split_batch(int count, const SplitJob* jobs_in, void* ws, size_t ws_bytes, cudaStream_t st)
 {
     std::lock_guard<std::mutex> use(g_side_use);
     SidePool* sp = side_pool();
     std::vector<SplitJob> jobs(jobs_in, jobs_in + count);
     std::vector<size_t> full(count, 0);
+    size_t total = 0;
+    int nontrivial = 0;
     for (int i = 0; i < count; ++i)
         if (!jobs[i].trivial) {
             const WsLayout Lf = ws_layout_g(jobs[i].alg, jobs[i].d, jobs[i].m, jobs[i].n, jobs[i].s, jobs[i].alg.R,
                                             jobs[i].fmt);
             full[i] = Lf.total;
+            total += (full[i] + 255) / 256 * 256;
+            ++nontrivial;
         }
+    /* one wave over the whole workspace when everything fits at once;
+     * otherwise two halves that waves alternate between */
+    const bool halves = sp != nullptr && (total > ws_bytes || nontrivial > kMaxLaunchProblems);
+    const size_t share = halves ? ws_bytes / 2 / 256 * 256 : ws_bytes;
+    auto pack_st = [&](int x) { return sp ? sp->s[x % kWaveStreams] : st; };
+    auto scat_st = [&](int x) { return sp ? sp->s[kWaveStreams + x % kWaveStreams] : st; };
+    auto ok = [](cudaError_t e) { return e == cudaSuccess; };
+    bool half_used[2] = {false, false};
+    int wave = 0;
+    if (int rc = side_fork(sp, st); rc != FMM_OK) return rc;   /* side streams start after the caller's work */
     int i = 0;
     while (i < count) {
         if (jobs[i].trivial) {
@@ -2131,39 +2161,51 @@ int fmm_split_batch(int count, const SplitJob* jobs_in, void* ws, size_t ws_byte
             ++i;
             continue;
         }
-        if (full[i] > ws_bytes) {
+        if (full[i] > share) {
+            /* alone, after every wave before it, with the whole workspace */
             SplitJob& j = jobs[i];
-            int rc = split_launch_budget(j.alg, j.m, j.n, j.k, j.alpha, j.A, j.lda, j.B, j.ldb, j.beta, j.C, j.ldc,
+            int rc = side_join(sp, st);
+            if (rc == FMM_OK)
+                rc = split_launch_budget(j.alg, j.m, j.n, j.k, j.alpha, j.A, j.lda, j.B, j.ldb, j.beta, j.C, j.ldc,
                                          j.s, j.fmt, ws, ws_bytes, ws_bytes, st, sp);
+            if (rc == FMM_OK) rc = side_fork(sp, st);
             if (rc != FMM_OK) return rc;
+            half_used[0] = half_used[1] = false;
             ++i;
             continue;
         }
         /* gather a wave */
         int e = i;
         size_t used = 0;
-        while (e < count && e - i < kMaxLaunchProblems && !jobs[e].trivial && used + full[e] <= ws_bytes &&
+        while (e < count && e - i < kMaxLaunchProblems && !jobs[e].trivial && used + full[e] <= share &&
                (int64_t)jobs[e].alg.R * jobs[e].s * std::max(jobs[e].d.m_pad, jobs[e].d.n_pad) <= 0x7fffffffLL) {
             used += (full[e] + 255) / 256 * 256;
             ++e;
         }
         if (e == i) return FMM_ERR_WORKSPACE;
-        GemmLaunch gl;
+        const int h = halves ? (wave & 1) : 0;
+        uint8_t* base = (uint8_t*)ws + (size_t)h * share;
+        /* per-problem maxima, exponents and packs on the pack streams, after
+         * the C updates of the last wave in this half */
+        if (sp && half_used[h])
+            for (int x = 0; x < kWaveStreams; ++x)
+                for (int y = 0; y < kWaveStreams; ++y)
+                    if (!ok(cudaStreamWaitEvent(pack_st(x), sp->wave_sc[h][y], 0))) return FMM_ERR_CUDA;
         size_t off = 0;
-        int64_t items = 0;
-        int prods = 0;
-        /* per-problem maxima, exponents and packs, spread over the side streams */
-        if (int rc = side_fork(sp, st); rc != FMM_OK) return rc;
         for (int q = i; q < e; ++q) {
             SplitJob& j = jobs[q];
-            cudaStream_t ss = sp ? sp->s[(q - i) % kSideStreams] : st;
-            int rc = job_bind_group(j, (uint8_t*)ws + off, full[q], j.alg.R);
+            cudaStream_t ss = pack_st(q - i);
+            int rc = job_bind_group(j, base + off, full[q], j.alg.R);
             if (rc != FMM_OK) return rc;
             off += (full[q] + 255) / 256 * 256;
             if ((rc = job_prologue(j, ss)) != FMM_OK) return rc;
             if ((rc = job_pack(j, 0, j.alg.R, ss)) != FMM_OK) return rc;
         }
-        if (int rc = side_join(sp, st); rc != FMM_OK) return rc;
+        if (sp)
+            for (int x = 0; x < kWaveStreams; ++x)
+                if (!ok(cudaEventRecord(sp->wave_pk[h][x], pack_st(x))) ||
+                    !ok(cudaStreamWaitEvent(st, sp->wave_pk[h][x], 0)))
+                    return FMM_ERR_CUDA;
         /* work items of the costliest problems (slice pairs x k blocks per
          * item) first, so the CTAs' round-robin shares end evenly */
         std::vector<int> ord;
@@ -2175,11 +2217,12 @@ int fmm_split_batch(int count, const SplitJob* jobs_in, void* ws, size_t ws_byte
         std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return item_cost(a) > item_cost(b); });
         /* problems with pair tiles in one launch, the rest in another (both
          * kernels give the same bits per tile) */
+        GemmLaunch gl;
         for (int pass = 0; pass < 2; ++pass) {
             const bool pair = pass == 0;
             memset(&gl, 0, sizeof(gl));
-            items = 0;
-            prods = 0;
+            int64_t items = 0;
+            int prods = 0;
             for (int q : ord) {
                 SplitJob& j = jobs[q];
                 if (job_pair(j) != pair) continue;
@@ -2191,12 +2234,21 @@ int fmm_split_batch(int count, const SplitJob* jobs_in, void* ws, size_t ws_byte
             if (gl.nprob == 0) continue;
             if (int rc = launch_gemm(gl, items, prods, st, pair); rc != FMM_OK) return rc;
         }
-        /* each problem's C update (disjoint C regions) on the side streams */
-        if (int rc = side_fork(sp, st); rc != FMM_OK) return rc;
-        for (int q = i; q < e; ++q) job_scatter(jobs[q], 0, jobs[q].alg.R, sp ? sp->s[(q - i) % kSideStreams] : st);
-        if (int rc = side_join(sp, st); rc != FMM_OK) return rc;
+        /* each problem's C update (disjoint C regions) on the scatter streams */
+        if (sp) {
+            if (!ok(cudaEventRecord(sp->wave_gm[h], st))) return FMM_ERR_CUDA;
+            for (int y = 0; y < kWaveStreams; ++y)
+                if (!ok(cudaStreamWaitEvent(scat_st(y), sp->wave_gm[h], 0))) return FMM_ERR_CUDA;
+        }
+        for (int q = i; q < e; ++q) job_scatter(jobs[q], 0, jobs[q].alg.R, scat_st(q - i));
+        if (sp)
+            for (int y = 0; y < kWaveStreams; ++y)
+                if (!ok(cudaEventRecord(sp->wave_sc[h][y], scat_st(y)))) return FMM_ERR_CUDA;
+        half_used[h] = true;
+        ++wave;
         i = e;
     }
+    if (int rc = side_join(sp, st); rc != FMM_OK) return rc;   /* the caller's stream waits for everything */
     return cudaGetLastError() == cudaSuccess ? FMM_OK : FMM_ERR_CUDA;
 }
 

@@ -42,7 +42,7 @@ def make_problems(fmm, seed, count):
     return probs, algs
 
 
-@pytest.mark.parametrize("ws_scale", [1.0, 0.02])
+@pytest.mark.parametrize("ws_scale", [1.0, 0.3, 0.02])   # one wave; waves over two halves; many waves
 def test_batch_bitexact_vs_single_calls(fmm, torch_cuda, ws_scale):
     import torch
     probs, algs = make_problems(fmm, 7, 40)
