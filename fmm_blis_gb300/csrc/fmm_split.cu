@@ -408,23 +408,26 @@ __device__ __forceinline__ void scale_first(const PEnt& x, double (&s)[N])
 }
 
 /* A side, all products r0 .. r0+np-1 of a group in one launch: CTA (q, tile)
- * forms the tile of 64 rows x 64 k of S_r, r = r0 + q, and writes its digits
+ * forms the tile of ROWS rows x 64 k of S_r, r = r0 + q, and writes its digits
  * row-major (K-major) into slices sa[q][t][m_pad][k_pad]. The product index
  * runs fastest in the block order, so the products at one tile position run
- * together and read their shared A sub-block tiles through L2 once. */
-template <int S, int DB>
-__global__ void __launch_bounds__(256)
+ * together and read their shared A sub-block tiles through L2 once. ROWS = 64
+ * (256 threads) for single calls; ROWS = 32 (128 threads, 25 KB of shared
+ * memory, at most 64 registers) for batched waves, small enough to run on an
+ * SM beside a resident GEMM CTA. */
+template <int S, int DB, int ROWS>
+__global__ void __launch_bounds__(ROWS * 4, ROWS == 64 ? 0 : 8)
 pack_a_kernel(const int* __restrict__ tab, int r0, int np, const double* __restrict__ A, int64_t lda,
               int64_t m, int64_t k, int64_t m_pad, int64_t k_pad,
               const int* __restrict__ e_row, uint8_t* __restrict__ sa)
 {
-    __shared__ double Sf[64][65];
+    __shared__ double Sf[64][ROWS + 1];
     __shared__ PEnt ent[kPackMaxEnt];
     const Tab t = tab_view(tab);
     const int64_t me = (m + t.mt - 1) / t.mt, ke = (k + t.kt - 1) / t.kt;
     const int q = (int)(blockIdx.x % (unsigned)np);
     const int r = r0 + q;
-    const int64_t i0 = (int64_t)(blockIdx.x / (unsigned)np) * 64, p0 = (int64_t)blockIdx.y * 64;
+    const int64_t i0 = (int64_t)(blockIdx.x / (unsigned)np) * ROWS, p0 = (int64_t)blockIdx.y * 64;
     e_row += (int64_t)q * m_pad;
     const int64_t slice0 = (int64_t)q * S * m_pad * k_pad;   /* element offset of this product */
     const int eb = t.u_off[r], ne_ = t.u_off[r + 1] - eb;
@@ -439,7 +442,7 @@ pack_a_kernel(const int* __restrict__ tab, int r0, int np, const double* __restr
     /* 16 elements per thread in two halves of 8: each term's 8 loads go out
      * together, and the first term's coefficient (uniform over the CTA) is
      * applied once after them */
-    const int li = threadIdx.x % 64;
+    const int li = threadIdx.x % ROWS, kq = threadIdx.x / ROWS;   /* row, k offset 0..3 */
     const int64_t gi = i0 + li;
     const bool row_ok = ne_ > 0 && gi < me;
 #pragma unroll
@@ -451,7 +454,7 @@ pack_a_kernel(const int* __restrict__ tab, int r0, int np, const double* __restr
             const PEnt& x0 = ent[0];
 #pragma unroll
             for (int y = 0; y < 8; ++y) {
-                const int64_t gp = p0 + threadIdx.x / 64 + 4 * (8 * h + y);
+                const int64_t gp = p0 + kq + 4 * (8 * h + y);
                 v8[y] = (gp < ke && gi < x0.rows && gp < x0.cols) ? x0.base[gi + gp * lda] : 0.0;
             }
             scale_first(x0, v8);
@@ -459,19 +462,19 @@ pack_a_kernel(const int* __restrict__ tab, int r0, int np, const double* __restr
                 const PEnt& x = ent[e];
 #pragma unroll
                 for (int y = 0; y < 8; ++y) {
-                    const int64_t gp = p0 + threadIdx.x / 64 + 4 * (8 * h + y);
+                    const int64_t gp = p0 + kq + 4 * (8 * h + y);
                     const double v = (gp < ke && gi < x.rows && gp < x.cols) ? x.base[gi + gp * lda] : 0.0;
                     v8[y] = fma(x.coef, v, v8[y]);
                 }
             }
         }
 #pragma unroll
-        for (int y = 0; y < 8; ++y) Sf[threadIdx.x / 64 + 4 * (8 * h + y)][li] = v8[y];
+        for (int y = 0; y < 8; ++y) Sf[kq + 4 * (8 * h + y)][li] = v8[y];
     }
     __syncthreads();
     /* thread -> (row, 8 consecutive k): 4 rows x 128 bytes per warp store */
     const int kg = threadIdx.x % 8;
-    for (int rr = threadIdx.x / 8; rr < 64; rr += 32) {
+    for (int rr = threadIdx.x / 8; rr < ROWS; rr += ROWS / 2) {
         const int64_t gi = i0 + rr;
         const int E = e_row[gi];
         Digits Y[8];
@@ -481,12 +484,13 @@ pack_a_kernel(const int* __restrict__ tab, int r0, int np, const double* __restr
     }
 }
 
-/* B side, all products of a group: CTA (q, tile) forms the tile of 32
+/* B side, all products of a group: CTA (q, tile) forms the tile of COLS
  * columns x 64 k of T_r, r = r0 + q (column j of T_r is contiguous in k
  * already), and writes its digits into slices sb[q][t][n_pad][k_pad];
- * product index fastest, as on the A side. */
-template <int S, int DB>
-__global__ void __launch_bounds__(256)
+ * product index fastest, as on the A side. COLS = 32 (256 threads) for single
+ * calls, 16 (128 threads, at most 64 registers) for batched waves. */
+template <int S, int DB, int COLS>
+__global__ void __launch_bounds__(COLS * 8, COLS == 32 ? 0 : 8)
 pack_b_kernel(const int* __restrict__ tab, int r0, int np, const double* __restrict__ B, int64_t ldb,
               int64_t k, int64_t n, int64_t n_pad, int64_t k_pad,
               const int* __restrict__ f_col, uint8_t* __restrict__ sb, int64_t j_first)
@@ -508,7 +512,7 @@ pack_b_kernel(const int* __restrict__ tab, int r0, int np, const double* __restr
     }
     __syncthreads();
     const int kg = threadIdx.x % 8;
-    const int64_t gj = j_first + (int64_t)(blockIdx.x / (unsigned)np) * 32 + threadIdx.x / 8;
+    const int64_t gj = j_first + (int64_t)(blockIdx.x / (unsigned)np) * COLS + threadIdx.x / 8;
     const int64_t p0 = (int64_t)blockIdx.y * 64 + kg * 8;
     double v8[8];
 #pragma unroll
@@ -545,6 +549,7 @@ pack_b_kernel(const int* __restrict__ tab, int r0, int np, const double* __restr
 struct PackSel {
     bool a = true, b = true;
     int64_t jb0 = 0, jb1 = -1;
+    bool small = false;   /* the 128-thread tiles that fit beside a resident GEMM CTA */
 };
 
 template <int S, int DB>
@@ -553,13 +558,19 @@ void launch_packs_t(const int* tab, int r, int np, const double* A, int64_t lda,
                     const int* e_row, const int* f_col, uint8_t* sa, uint8_t* sb, cudaStream_t st,
                     cudaStream_t st_b, const PackSel& sel)
 {
-    if (sel.a)
-        pack_a_kernel<S, DB><<<dim3((unsigned)(np * (m_pad / 64)), (unsigned)(k_pad / 64)), 256, 0, st>>>(
-            tab, r, np, A, lda, m, k, m_pad, k_pad, e_row, sa);
+    const dim3 ka((unsigned)(np * (m_pad / (sel.small ? 32 : 64))), (unsigned)(k_pad / 64));
+    if (sel.a && sel.small)
+        pack_a_kernel<S, DB, 32><<<ka, 128, 0, st>>>(tab, r, np, A, lda, m, k, m_pad, k_pad, e_row, sa);
+    else if (sel.a)
+        pack_a_kernel<S, DB, 64><<<ka, 256, 0, st>>>(tab, r, np, A, lda, m, k, m_pad, k_pad, e_row, sa);
     const int64_t j1 = sel.jb1 < 0 ? n_pad : sel.jb1;
-    if (sel.b && j1 > sel.jb0)
-        pack_b_kernel<S, DB><<<dim3((unsigned)(np * ((j1 - sel.jb0 + 31) / 32)), (unsigned)(k_pad / 64)), 256, 0,
-                               st_b>>>(tab, r, np, B, ldb, k, n, n_pad, k_pad, f_col, sb, sel.jb0);
+    if (!sel.b || j1 <= sel.jb0) return;
+    const int cols = sel.small ? 16 : 32;
+    const dim3 kb((unsigned)(np * ((j1 - sel.jb0 + cols - 1) / cols)), (unsigned)(k_pad / 64));
+    if (sel.small)
+        pack_b_kernel<S, DB, 16><<<kb, 128, 0, st_b>>>(tab, r, np, B, ldb, k, n, n_pad, k_pad, f_col, sb, sel.jb0);
+    else
+        pack_b_kernel<S, DB, 32><<<kb, 256, 0, st_b>>>(tab, r, np, B, ldb, k, n, n_pad, k_pad, f_col, sb, sel.jb0);
 }
 
 /* digit slices of the products r .. r+np-1 (exponents already in place);
@@ -1508,7 +1519,15 @@ extern "C" int fmm_gpu_read_kernel_timing(double* total_ms, uint64_t* launches, 
 
 size_t fmm_split_ws_bytes(const AlgView& alg, int64_t m, int64_t n, int64_t k, int slices, int fmt)
 {
-    return ws_layout(alg, m, n, k, slices, kGroupBudget, fmt).total;
+    const WsLayout L = ws_layout(alg, m, n, k, slices, kGroupBudget, fmt);
+    if (L.group < alg.R) return L.total;
+    /* room for the two overlapping product groups when they fit the budget */
+    const Dims d = dims_of(alg, m, n, k, fmt);
+    const int G1 = (alg.R + 1) / 2;
+    if (alg.R < 2) return L.total;
+    const WsLayout L1 = ws_layout_g(alg, d, m, n, slices, G1, fmt);
+    const size_t two = L1.total + (L1.total - L1.erow);
+    return two <= kGroupBudget ? std::max(L.total, two) : L.total;
 }
 
 /* One split-form GEMM problem being executed: its algorithm, geometry,
@@ -1601,6 +1620,7 @@ struct SidePool {
     cudaEvent_t wave_sc[2][kWaveStreams];   /* a workspace half's C updates done */
     cudaEvent_t gate[3];   /* host-buffer calls: A, B and C on the device */
     cudaEvent_t chunk[16]; /* host-buffer calls: B chunks in, C chunks out */
+    cudaStream_t hi;       /* greatest priority: GEMMs that side work runs beside */
 };
 
 std::mutex g_side_mu, g_side_use;
@@ -1615,7 +1635,10 @@ SidePool* side_pool()
         if (p->device == dev) return p;
     SidePool* p = new SidePool;
     p->device = dev;
-    bool ok = cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming) == cudaSuccess;
+    int least = 0, greatest = 0;
+    cudaDeviceGetStreamPriorityRange(&least, &greatest);
+    bool ok = cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming) == cudaSuccess &&
+              cudaStreamCreateWithPriority(&p->hi, cudaStreamNonBlocking, greatest) == cudaSuccess;
     for (int i = 0; i < 3 && ok; ++i) ok = cudaEventCreateWithFlags(&p->gate[i], cudaEventDisableTiming) == cudaSuccess;
     for (int i = 0; i < 16 && ok; ++i) ok = cudaEventCreateWithFlags(&p->chunk[i], cudaEventDisableTiming) == cudaSuccess;
     for (int h = 0; h < 2 && ok; ++h) {
@@ -1709,7 +1732,7 @@ static int job_prologue(SplitJob& j, cudaStream_t st, SidePool* sp = nullptr)
 
 /* exponents and digit slices of products [r0, r0 + np); np never exceeds
  * the group the job's workspace was laid out for */
-static int job_pack(SplitJob& j, int r0, int np, cudaStream_t st, SidePool* sp = nullptr)
+static int job_pack(SplitJob& j, int r0, int np, cudaStream_t st, SidePool* sp = nullptr, bool small = false)
 {
     if (np > j.L.group) return FMM_ERR_WORKSPACE;
     const Dims& d = j.d;
@@ -1732,8 +1755,10 @@ static int job_pack(SplitJob& j, int r0, int np, cudaStream_t st, SidePool* sp =
     if (sp && (rc = side_fork1(sp, st)) != FMM_OK) return rc;
     exps_kernel<<<dim3((unsigned)((d.n_pad + 255) / 256), (unsigned)np), 256, 0, stb>>>(
         j.alg.tab, r0, j.m, j.n, j.k, d.m_pad, d.n_pad, amax, bmax, e_row, f_col, d.m_pad, d.m_pad + d.n_pad);
+    PackSel sel;
+    sel.small = small;
     launch_packs(j.fmt, j.s, j.alg.tab, r0, np, j.A, j.lda, j.B, j.ldb, j.m, j.n, j.k, d.m_pad, d.n_pad, d.k_pad, e_row,
-                 f_col, sa, sb, st, stb);
+                 f_col, sa, sb, st, stb, sel);
     if (sp && (rc = side_join1(sp, st)) != FMM_OK) return rc;
     fmm_count_launch(4);
     return FMM_OK;
@@ -1862,7 +1887,9 @@ static void job_scatter_cols(const SplitJob& j, int r0, int np, int64_t j0, int6
     fmm_count_launch(1);
 }
 
-static void job_scatter(const SplitJob& j, int r0, int np, cudaStream_t st)
+/* small: blocks of at most 128 threads (and so at most 16 KB of sub-block
+ * values), which fit on an SM beside a resident GEMM CTA */
+static void job_scatter(const SplitJob& j, int r0, int np, cudaStream_t st, bool small = false)
 {
     const int64_t elems = j.d.me * j.d.ne;   /* the largest part's extent */
     /* element-major form when the sub-block values and the group's W entries
@@ -1871,7 +1898,7 @@ static void job_scatter(const SplitJob& j, int r0, int np, cudaStream_t st)
     const Tab ht = tab_view(j.alg.htab);
     const int P = j.alg.mt * j.alg.nt;
     const int E = ht.w_off[r0 + np] - ht.w_off[r0];
-    int T = std::min(256, kScatterAllSmem / (8 * P)) / 32 * 32;
+    int T = std::min(small ? 128 : 256, kScatterAllSmem / (8 * P)) / 32 * 32;
     const size_t smem = (size_t)P * std::max(T, 0) * 8 + (size_t)E * 12 + (size_t)(np + 1) * 4;
     if (P <= 64 && T >= 32 && smem <= 47 * 1024) {
         scatter_all_kernel<<<(unsigned)((elems + T - 1) / T), (unsigned)T, smem, st>>>(
@@ -1891,10 +1918,17 @@ static int launch_gemm(GemmLaunch& gl, int64_t nitems, int nprod_timed, cudaStre
 {
     static bool attr_set = false;
     if (!attr_set) {
+        /* the largest shared-memory carveout: the GEMM CTA's ~195-200 KB
+         * leaves room on its SM for one small block of side work (packs of
+         * the next group, C updates of the previous one) */
         if (cudaFuncSetAttribute(split_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)kGemmSmem) != cudaSuccess ||
             cudaFuncSetAttribute(split_gemm_pair_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)kPairSmem) != cudaSuccess)
+                                 (int)kPairSmem) != cudaSuccess ||
+            cudaFuncSetAttribute(split_gemm_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 (int)cudaSharedmemCarveoutMaxShared) != cudaSuccess ||
+            cudaFuncSetAttribute(split_gemm_pair_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 (int)cudaSharedmemCarveoutMaxShared) != cudaSuccess)
             return FMM_ERR_CUDA;
         attr_set = true;
     }
@@ -1920,6 +1954,73 @@ static int launch_gemm(GemmLaunch& gl, int64_t nitems, int nprod_timed, cudaStre
     return FMM_OK;
 }
 
+/* Two product groups whose work overlaps: the products split into
+ * G1 = ceil(R/2) and R - G1, each group with its own exponents, slices and
+ * Z (the second region follows the first; the maxima are shared). Group 1
+ * is packed with the whole GPU; group 2's packs (small tiles, pool stream
+ * s[3]) then run on the SMs beside group 1's GEMM, and group 1's C updates
+ * (small blocks, s[4]) beside group 2's GEMM; group 2's C updates follow on
+ * s[4], so every C element still receives the products in increasing order
+ * and the result is the single group's bit for bit. The second region's
+ * layout: the group part of L1 shifted by its own size. */
+struct OverlapPlan {
+    WsLayout L1;
+    size_t shift = 0;
+    bool ok = false;
+};
+
+static OverlapPlan overlap_plan(const AlgView& alg, const Dims& d, int64_t m, int64_t n, int s, int fmt,
+                                size_t bytes)
+{
+    OverlapPlan o;
+    if (alg.R < 2) return o;
+    const int G1 = (alg.R + 1) / 2;
+    o.L1 = ws_layout_g(alg, d, m, n, s, G1, fmt);
+    o.shift = o.L1.total - o.L1.erow;
+    /* each group's GEMM keeps every SM busy for at least 8 rounds of items */
+    const int64_t tiles = (d.m_pad / (d.me >= kPairMinRows ? kPairTileM : kTileM)) * (d.n_pad / kTileN);
+    o.ok = o.L1.total + o.shift <= bytes && (int64_t)G1 * tiles >= 8 * 152 &&
+           (int64_t)G1 * s * std::max(d.m_pad, d.n_pad) <= 0x7fffffffLL;
+    return o;
+}
+
+static int split_overlap(SplitJob& j, const OverlapPlan& o, void* ws, cudaStream_t st, SidePool* sp)
+{
+    const int R = j.alg.R, G1 = o.L1.group, G2 = R - G1;
+    j.L = o.L1;
+    j.w = (uint8_t*)ws;
+    SplitJob j2 = j;
+    j2.L.erow += o.shift;
+    j2.L.fcol += o.shift;
+    j2.L.sa += o.shift;
+    j2.L.sb += o.shift;
+    j2.L.z += o.shift;
+    j2.L.total += o.shift;
+    /* the GEMMs on the greatest-priority stream, so the block scheduler
+     * places their CTAs first and the side work fills the room they leave */
+    cudaStream_t sg = sp->hi, sp2 = sp->s[3], ssc = sp->s[4];
+    auto ok = [](cudaError_t e) { return e == cudaSuccess; };
+    int rc;
+    if ((rc = job_prologue(j, st, sp)) != FMM_OK) return rc;
+    if ((rc = job_pack(j, 0, G1, st, sp)) != FMM_OK) return rc;
+    if (!ok(cudaEventRecord(sp->chunk[0], st)) || !ok(cudaStreamWaitEvent(sg, sp->chunk[0], 0))) return FMM_ERR_CUDA;
+    if ((rc = job_gemm(j, G1, sg)) != FMM_OK) return rc;
+    if (!ok(cudaEventRecord(sp->chunk[2], sg))) return FMM_ERR_CUDA;
+    /* group 2's packs after the maxima (and group 1's packs), beside GEMM 1 */
+    if (!ok(cudaStreamWaitEvent(sp2, sp->chunk[0], 0))) return FMM_ERR_CUDA;
+    if ((rc = job_pack(j2, G1, G2, sp2, nullptr, true)) != FMM_OK) return rc;
+    if (!ok(cudaEventRecord(sp->chunk[1], sp2))) return FMM_ERR_CUDA;
+    /* group 1's C updates beside GEMM 2 */
+    if (!ok(cudaStreamWaitEvent(ssc, sp->chunk[2], 0))) return FMM_ERR_CUDA;
+    job_scatter(j, 0, G1, ssc, true);
+    if (!ok(cudaStreamWaitEvent(sg, sp->chunk[1], 0))) return FMM_ERR_CUDA;
+    if ((rc = job_gemm(j2, G2, sg)) != FMM_OK) return rc;
+    if (!ok(cudaEventRecord(sp->chunk[3], sg)) || !ok(cudaStreamWaitEvent(ssc, sp->chunk[3], 0))) return FMM_ERR_CUDA;
+    job_scatter(j2, G1, G2, ssc);
+    if (!ok(cudaEventRecord(sp->chunk[4], ssc)) || !ok(cudaStreamWaitEvent(st, sp->chunk[4], 0))) return FMM_ERR_CUDA;
+    return cudaGetLastError() == cudaSuccess ? FMM_OK : FMM_ERR_CUDA;
+}
+
 static int split_launch_budget(const AlgView& alg, int64_t m, int64_t n, int64_t k, double alpha,
                                const double* A, int64_t lda, const double* B, int64_t ldb, double beta,
                                double* C, int64_t ldc, int s, int fmt, void* ws, size_t ws_bytes, size_t budget,
@@ -1928,6 +2029,10 @@ static int split_launch_budget(const AlgView& alg, int64_t m, int64_t n, int64_t
     SplitJob j;
     int rc = job_init(j, alg, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, s, fmt);
     if (rc != FMM_OK) return rc;
+    if (!j.trivial && sp && ws != nullptr && ((uintptr_t)ws & 255) == 0) {
+        const OverlapPlan o = overlap_plan(alg, j.d, m, n, s, fmt, std::min(ws_bytes, budget));
+        if (o.ok) return split_overlap(j, o, ws, st, sp);
+    }
     if (!j.trivial && (rc = job_bind(j, ws, ws_bytes, budget)) != FMM_OK) return rc;
     if ((rc = job_prologue(j, st, sp)) != FMM_OK || j.trivial) return rc;
     const int G = j.L.group;
@@ -2199,7 +2304,7 @@ int fmm_split_batch(int count, const SplitJob* jobs_in, void* ws, size_t ws_byte
             if (rc != FMM_OK) return rc;
             off += (full[q] + 255) / 256 * 256;
             if ((rc = job_prologue(j, ss)) != FMM_OK) return rc;
-            if ((rc = job_pack(j, 0, j.alg.R, ss)) != FMM_OK) return rc;
+            if ((rc = job_pack(j, 0, j.alg.R, ss, nullptr, halves)) != FMM_OK) return rc;
         }
         if (sp)
             for (int x = 0; x < kWaveStreams; ++x)

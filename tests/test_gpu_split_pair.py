@@ -85,3 +85,26 @@ def test_batch_mixes_pair_and_single_launches(fmm, torch_cuda):
     for i, (p, r) in enumerate(zip(probs, refs)):
         assert torch.equal(p["C"], r), f"problem {i}"
     assert fmm.take_device_error() == 0
+
+
+def test_overlapped_groups_equal_one_group(fmm, torch_cuda):
+    """8192 x 8192 x 512, two Strassen levels: with the recommended workspace
+    the call runs its 49 products as two overlapping groups (group 2 packed
+    beside group 1's GEMM, group 1's C updates beside group 2's GEMM); with a
+    workspace just too small for that it runs them as one group. Same bits."""
+    import torch
+    n, k = 8192, 512
+    g = torch.Generator(device="cuda").manual_seed(29)
+    A = (torch.rand((k, n), generator=g, device="cuda", dtype=torch.float64) * 2 - 1).t()
+    B = (torch.rand((n, k), generator=g, device="cuda", dtype=torch.float64) * 2 - 1).t()
+    C0 = (torch.rand((n, n), generator=g, device="cuda", dtype=torch.float64) * 2 - 1).t()
+    f = fmm.strassen_fmm()
+    need = fmm.split_workspace_size(n, n, k, f, 2, 6)
+    C1, C2 = C0.clone(), C0.clone()
+    ws = torch.empty(need, dtype=torch.uint8, device="cuda")
+    fmm.split_dgemm(A, B, C1, f, 2, 6, workspace=ws, alpha=0.5, beta=2.0)
+    ws_one = torch.empty(need - (16 << 20), dtype=torch.uint8, device="cuda")
+    fmm.split_dgemm(A, B, C2, f, 2, 6, workspace=ws_one, alpha=0.5, beta=2.0)
+    torch.cuda.synchronize()
+    assert torch.equal(C1, C2)
+    assert fmm.take_device_error() == 0
