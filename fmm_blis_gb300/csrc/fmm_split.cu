@@ -2256,7 +2256,92 @@ int fmm_split_batch(int count, const SplitJob* jobs_in, void* ws, size_t ws_byte
     auto scat_st = [&](int x) { return sp ? sp->s[kWaveStreams + x % kWaveStreams] : st; };
     auto ok = [](cudaError_t e) { return e == cudaSuccess; };
     bool half_used[2] = {false, false};
+    struct Wave {
+        int i, e, h;
+    };
     int wave = 0;
+
+    /* a wave's maxima, exponents and packs on the pack streams, after the C
+     * updates of the last wave in its half; the GEMM stream then waits */
+    auto pack_wave = [&](const Wave& W) -> int {
+        uint8_t* base = (uint8_t*)ws + (size_t)W.h * share;
+        if (sp && half_used[W.h])
+            for (int x = 0; x < kWaveStreams; ++x)
+                for (int y = 0; y < kWaveStreams; ++y)
+                    if (!ok(cudaStreamWaitEvent(pack_st(x), sp->wave_sc[W.h][y], 0))) return FMM_ERR_CUDA;
+        size_t off = 0;
+        for (int q = W.i; q < W.e; ++q) {
+            SplitJob& j = jobs[q];
+            cudaStream_t ss = pack_st(q - W.i);
+            int rc = job_bind_group(j, base + off, full[q], j.alg.R);
+            if (rc != FMM_OK) return rc;
+            off += (full[q] + 255) / 256 * 256;
+            if ((rc = job_prologue(j, ss)) != FMM_OK) return rc;
+            if ((rc = job_pack(j, 0, j.alg.R, ss, nullptr, halves)) != FMM_OK) return rc;
+        }
+        if (sp)
+            for (int x = 0; x < kWaveStreams; ++x)
+                if (!ok(cudaEventRecord(sp->wave_pk[W.h][x], pack_st(x)))) return FMM_ERR_CUDA;
+        return FMM_OK;
+    };
+    /* one persistent GEMM launch per tile kind over the wave's items, the
+     * costliest items (slice pairs x k blocks) first so the CTAs' shares end
+     * evenly; pair-tile problems and the rest give the same bits per tile */
+    auto gemm_wave = [&](const Wave& W) -> int {
+        if (sp)
+            for (int x = 0; x < kWaveStreams; ++x)
+                if (!ok(cudaStreamWaitEvent(st, sp->wave_pk[W.h][x], 0))) return FMM_ERR_CUDA;
+        std::vector<int> ord;
+        for (int q = W.i; q < W.e; ++q) ord.push_back(q);
+        auto item_cost = [&](int q) {
+            return (int64_t)jobs[q].s * (jobs[q].s + 1) / 2 * (jobs[q].d.k_pad / kbe_of(jobs[q].fmt)) /
+                   (jobs[q].fmt ? 2 : 1);   /* FP8 MMAs run at twice the BF16 rate */
+        };
+        std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return item_cost(a) > item_cost(b); });
+        GemmLaunch gl;
+        for (int pass = 0; pass < 2; ++pass) {
+            const bool pair = pass == 0;
+            memset(&gl, 0, sizeof(gl));
+            int64_t items = 0;
+            int prods = 0;
+            for (int q : ord) {
+                SplitJob& j = jobs[q];
+                if (job_pair(j) != pair) continue;
+                int rc = job_fill(j, gl.prob[gl.nprob++], j.alg.R, (int)items, pair);
+                if (rc != FMM_OK) return rc;
+                items += job_items(j, j.alg.R, pair);
+                prods += j.alg.R;
+            }
+            if (gl.nprob == 0) continue;
+            if (int rc = launch_gemm(gl, items, prods, st, pair); rc != FMM_OK) return rc;
+        }
+        if (sp && !ok(cudaEventRecord(sp->wave_gm[W.h], st))) return FMM_ERR_CUDA;
+        return FMM_OK;
+    };
+    /* each problem's C update (disjoint C regions) on the scatter streams */
+    auto scatter_wave = [&](const Wave& W) -> int {
+        if (sp)
+            for (int y = 0; y < kWaveStreams; ++y)
+                if (!ok(cudaStreamWaitEvent(scat_st(y), sp->wave_gm[W.h], 0))) return FMM_ERR_CUDA;
+        for (int q = W.i; q < W.e; ++q) job_scatter(jobs[q], 0, jobs[q].alg.R, scat_st(q - W.i), halves);
+        if (sp)
+            for (int y = 0; y < kWaveStreams; ++y)
+                if (!ok(cudaEventRecord(sp->wave_sc[W.h][y], scat_st(y)))) return FMM_ERR_CUDA;
+        half_used[W.h] = true;
+        return FMM_OK;
+    };
+
+    /* software pipeline, enqueued as GEMM(w), packs(w+1), C updates(w): a pack
+     * stream that shares a hardware queue with a scatter stream then never
+     * has its work behind the C updates' wait for GEMM(w) */
+    bool pending = false;
+    Wave P{0, 0, 0};
+    auto flush = [&]() -> int {
+        if (!pending) return FMM_OK;
+        pending = false;
+        int rc = gemm_wave(P);
+        return rc != FMM_OK ? rc : scatter_wave(P);
+    };
     if (int rc = side_fork(sp, st); rc != FMM_OK) return rc;   /* side streams start after the caller's work */
     int i = 0;
     while (i < count) {
@@ -2269,7 +2354,8 @@ int fmm_split_batch(int count, const SplitJob* jobs_in, void* ws, size_t ws_byte
         if (full[i] > share) {
             /* alone, after every wave before it, with the whole workspace */
             SplitJob& j = jobs[i];
-            int rc = side_join(sp, st);
+            int rc = flush();
+            if (rc == FMM_OK) rc = side_join(sp, st);
             if (rc == FMM_OK)
                 rc = split_launch_budget(j.alg, j.m, j.n, j.k, j.alpha, j.A, j.lda, j.B, j.ldb, j.beta, j.C, j.ldc,
                                          j.s, j.fmt, ws, ws_bytes, ws_bytes, st, sp);
@@ -2288,71 +2374,25 @@ int fmm_split_batch(int count, const SplitJob* jobs_in, void* ws, size_t ws_byte
             ++e;
         }
         if (e == i) return FMM_ERR_WORKSPACE;
-        const int h = halves ? (wave & 1) : 0;
-        uint8_t* base = (uint8_t*)ws + (size_t)h * share;
-        /* per-problem maxima, exponents and packs on the pack streams, after
-         * the C updates of the last wave in this half */
-        if (sp && half_used[h])
-            for (int x = 0; x < kWaveStreams; ++x)
-                for (int y = 0; y < kWaveStreams; ++y)
-                    if (!ok(cudaStreamWaitEvent(pack_st(x), sp->wave_sc[h][y], 0))) return FMM_ERR_CUDA;
-        size_t off = 0;
-        for (int q = i; q < e; ++q) {
-            SplitJob& j = jobs[q];
-            cudaStream_t ss = pack_st(q - i);
-            int rc = job_bind_group(j, base + off, full[q], j.alg.R);
-            if (rc != FMM_OK) return rc;
-            off += (full[q] + 255) / 256 * 256;
-            if ((rc = job_prologue(j, ss)) != FMM_OK) return rc;
-            if ((rc = job_pack(j, 0, j.alg.R, ss, nullptr, halves)) != FMM_OK) return rc;
-        }
-        if (sp)
-            for (int x = 0; x < kWaveStreams; ++x)
-                if (!ok(cudaEventRecord(sp->wave_pk[h][x], pack_st(x))) ||
-                    !ok(cudaStreamWaitEvent(st, sp->wave_pk[h][x], 0)))
-                    return FMM_ERR_CUDA;
-        /* work items of the costliest problems (slice pairs x k blocks per
-         * item) first, so the CTAs' round-robin shares end evenly */
-        std::vector<int> ord;
-        for (int q = i; q < e; ++q) ord.push_back(q);
-        auto item_cost = [&](int q) {
-            return (int64_t)jobs[q].s * (jobs[q].s + 1) / 2 * (jobs[q].d.k_pad / kbe_of(jobs[q].fmt)) /
-                   (jobs[q].fmt ? 2 : 1);   /* FP8 MMAs run at twice the BF16 rate */
-        };
-        std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return item_cost(a) > item_cost(b); });
-        /* problems with pair tiles in one launch, the rest in another (both
-         * kernels give the same bits per tile) */
-        GemmLaunch gl;
-        for (int pass = 0; pass < 2; ++pass) {
-            const bool pair = pass == 0;
-            memset(&gl, 0, sizeof(gl));
-            int64_t items = 0;
-            int prods = 0;
-            for (int q : ord) {
-                SplitJob& j = jobs[q];
-                if (job_pair(j) != pair) continue;
-                int rc = job_fill(j, gl.prob[gl.nprob++], j.alg.R, (int)items, pair);
-                if (rc != FMM_OK) return rc;
-                items += job_items(j, j.alg.R, pair);
-                prods += j.alg.R;
-            }
-            if (gl.nprob == 0) continue;
-            if (int rc = launch_gemm(gl, items, prods, st, pair); rc != FMM_OK) return rc;
-        }
-        /* each problem's C update (disjoint C regions) on the scatter streams */
-        if (sp) {
-            if (!ok(cudaEventRecord(sp->wave_gm[h], st))) return FMM_ERR_CUDA;
-            for (int y = 0; y < kWaveStreams; ++y)
-                if (!ok(cudaStreamWaitEvent(scat_st(y), sp->wave_gm[h], 0))) return FMM_ERR_CUDA;
-        }
-        for (int q = i; q < e; ++q) job_scatter(jobs[q], 0, jobs[q].alg.R, scat_st(q - i));
-        if (sp)
-            for (int y = 0; y < kWaveStreams; ++y)
-                if (!ok(cudaEventRecord(sp->wave_sc[h][y], scat_st(y)))) return FMM_ERR_CUDA;
-        half_used[h] = true;
+        const Wave W{i, e, halves ? (wave & 1) : 0};
         ++wave;
+        int rc = FMM_OK;
+        if (halves) {
+            /* W packs into the other half than the pending wave */
+            if (pending) rc = gemm_wave(P);
+            if (rc == FMM_OK) rc = pack_wave(W);
+            if (rc == FMM_OK && pending) rc = scatter_wave(P);
+        } else {
+            /* one region: the pending wave is done with it first */
+            rc = flush();
+            if (rc == FMM_OK) rc = pack_wave(W);
+        }
+        if (rc != FMM_OK) return rc;
+        P = W;
+        pending = true;
         i = e;
     }
+    if (int rc = flush(); rc != FMM_OK) return rc;
     if (int rc = side_join(sp, st); rc != FMM_OK) return rc;   /* the caller's stream waits for everything */
     return cudaGetLastError() == cudaSuccess ? FMM_OK : FMM_ERR_CUDA;
 }
