@@ -1918,17 +1918,10 @@ static int launch_gemm(GemmLaunch& gl, int64_t nitems, int nprod_timed, cudaStre
 {
     static bool attr_set = false;
     if (!attr_set) {
-        /* the largest shared-memory carveout: the GEMM CTA's ~195-200 KB
-         * leaves room on its SM for one small block of side work (packs of
-         * the next group, C updates of the previous one) */
         if (cudaFuncSetAttribute(split_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)kGemmSmem) != cudaSuccess ||
             cudaFuncSetAttribute(split_gemm_pair_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)kPairSmem) != cudaSuccess ||
-            cudaFuncSetAttribute(split_gemm_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                 (int)cudaSharedmemCarveoutMaxShared) != cudaSuccess ||
-            cudaFuncSetAttribute(split_gemm_pair_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                 (int)cudaSharedmemCarveoutMaxShared) != cudaSuccess)
+                                 (int)kPairSmem) != cudaSuccess)
             return FMM_ERR_CUDA;
         attr_set = true;
     }
