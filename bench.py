@@ -703,10 +703,10 @@ def main():
     # the committed capture is of the default workload only
     if tf.exists() and (n, args.alg, levels, s, fmt) == (16384, "222", 2, 6, "bf16"):
         try:
-            # captured for a launch over all 49 products; a launch here covers
-            # products_per_launch of them (two overlapping groups per step)
-            per49 = json.loads(tf.read_text()).get("bytes_per_launch_16384_x2")
-            traffic = per49 * (gemm_products / max(gemm_n, 1)) / 49 if per49 else None
+            # ncu DRAM bytes of one step's GEMM launches, per launch
+            per_step = json.loads(tf.read_text()).get("bytes_per_step_16384_x2")
+            launches_per_step = gemm_n / max(args.steps, 1)
+            traffic = per_step / launches_per_step if per_step and launches_per_step else None
         except ValueError:
             traffic = None
     # single calls take 256 x 256 CTA-pair tiles once m_e >= 1024
