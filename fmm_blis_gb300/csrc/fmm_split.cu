@@ -416,7 +416,7 @@ __device__ __forceinline__ void scale_first(const PEnt& x, double (&s)[N])
  * memory, at most 64 registers) for batched waves, small enough to run on an
  * SM beside a resident GEMM CTA. */
 template <int S, int DB, int ROWS>
-__global__ void __launch_bounds__(ROWS * 4, ROWS == 64 ? 0 : 8)
+__global__ void __launch_bounds__(ROWS * 4, ROWS == 64 ? 4 : 8)
 pack_a_kernel(const int* __restrict__ tab, int r0, int np, const double* __restrict__ A, int64_t lda,
               int64_t m, int64_t k, int64_t m_pad, int64_t k_pad,
               const int* __restrict__ e_row, uint8_t* __restrict__ sa)
@@ -451,21 +451,26 @@ pack_a_kernel(const int* __restrict__ tab, int r0, int np, const double* __restr
 #pragma unroll
         for (int y = 0; y < 8; ++y) v8[y] = 0.0;
         if (row_ok) {
-            const PEnt& x0 = ent[0];
-#pragma unroll
-            for (int y = 0; y < 8; ++y) {
-                const int64_t gp = p0 + kq + 4 * (8 * h + y);
-                v8[y] = (gp < ke && gi < x0.rows && gp < x0.cols) ? x0.base[gi + gp * lda] : 0.0;
-            }
-            scale_first(x0, v8);
-            for (int e = 1; e < ne_; ++e) {
-                const PEnt& x = ent[e];
+            /* term e + 1's loads go out before term e's FMAs */
+            auto load8 = [&](const PEnt& x, double (&d)[8]) {
 #pragma unroll
                 for (int y = 0; y < 8; ++y) {
                     const int64_t gp = p0 + kq + 4 * (8 * h + y);
-                    const double v = (gp < ke && gi < x.rows && gp < x.cols) ? x.base[gi + gp * lda] : 0.0;
-                    v8[y] = fma(x.coef, v, v8[y]);
+                    d[y] = (gp < ke && gi < x.rows && gp < x.cols) ? x.base[gi + gp * lda] : 0.0;
                 }
+            };
+            double nx[8];
+            load8(ent[0], v8);
+            if (ne_ > 1) load8(ent[1], nx);
+            scale_first(ent[0], v8);
+            for (int e = 1; e < ne_; ++e) {
+                double cur[8];
+#pragma unroll
+                for (int y = 0; y < 8; ++y) cur[y] = nx[y];
+                if (e + 1 < ne_) load8(ent[e + 1], nx);
+                const double c = ent[e].coef;
+#pragma unroll
+                for (int y = 0; y < 8; ++y) v8[y] = fma(c, cur[y], v8[y]);
             }
         }
 #pragma unroll
@@ -490,7 +495,7 @@ pack_a_kernel(const int* __restrict__ tab, int r0, int np, const double* __restr
  * product index fastest, as on the A side. COLS = 32 (256 threads) for single
  * calls, 16 (128 threads, at most 64 registers) for batched waves. */
 template <int S, int DB, int COLS>
-__global__ void __launch_bounds__(COLS * 8, COLS == 32 ? 0 : 8)
+__global__ void __launch_bounds__(COLS * 8, COLS == 32 ? 4 : 8)
 pack_b_kernel(const int* __restrict__ tab, int r0, int np, const double* __restrict__ B, int64_t ldb,
               int64_t k, int64_t n, int64_t n_pad, int64_t k_pad,
               const int* __restrict__ f_col, uint8_t* __restrict__ sb, int64_t j_first)
@@ -518,23 +523,26 @@ pack_b_kernel(const int* __restrict__ tab, int r0, int np, const double* __restr
 #pragma unroll
     for (int x = 0; x < 8; ++x) v8[x] = 0.0;
     if (ne_ > 0 && gj < ne) {
-        {
-            const PEnt& x = ent[0];
+        /* term e + 1's loads go out before term e's FMAs */
+        auto load8 = [&](const PEnt& x, double (&d)[8]) {
 #pragma unroll
             for (int y = 0; y < 8; ++y) {
                 const int64_t gp = p0 + y;
-                v8[y] = (gp < ke && gp < x.rows && gj < x.cols) ? x.base[gp + gj * ldb] : 0.0;
+                d[y] = (gp < ke && gp < x.rows && gj < x.cols) ? x.base[gp + gj * ldb] : 0.0;
             }
-            scale_first(x, v8);
-        }
+        };
+        double nx[8];
+        load8(ent[0], v8);
+        if (ne_ > 1) load8(ent[1], nx);
+        scale_first(ent[0], v8);
         for (int e = 1; e < ne_; ++e) {
-            const PEnt& x = ent[e];
+            double cur[8];
 #pragma unroll
-            for (int y = 0; y < 8; ++y) {
-                const int64_t gp = p0 + y;
-                const double v = (gp < ke && gp < x.rows && gj < x.cols) ? x.base[gp + gj * ldb] : 0.0;
-                v8[y] = fma(x.coef, v, v8[y]);
-            }
+            for (int y = 0; y < 8; ++y) cur[y] = nx[y];
+            if (e + 1 < ne_) load8(ent[e + 1], nx);
+            const double c = ent[e].coef;
+#pragma unroll
+            for (int y = 0; y < 8; ++y) v8[y] = fma(c, cur[y], v8[y]);
         }
     }
     const int F = f_col[gj];

@@ -108,3 +108,31 @@ def test_overlapped_groups_equal_one_group(fmm, torch_cuda):
     torch.cuda.synchronize()
     assert torch.equal(C1, C2)
     assert fmm.take_device_error() == 0
+
+
+def test_short_launches_equal_one_launch(fmm, torch_cuda):
+    """16384 x 16384 x 128, two Strassen levels (m_e = 4096, 256 pair tiles per
+    product): the single call runs each product group's GEMM as several
+    back-to-back launches; a one-problem batch covers all 49 products in one
+    launch. Same bits."""
+    import torch
+    n, k = 16384, 128
+    g = torch.Generator(device="cuda").manual_seed(31)
+    A = (torch.rand((k, n), generator=g, device="cuda", dtype=torch.float64) * 2 - 1).t()
+    B = (torch.rand((n, k), generator=g, device="cuda", dtype=torch.float64) * 2 - 1).t()
+    C0 = (torch.rand((n, n), generator=g, device="cuda", dtype=torch.float64) * 2 - 1).t()
+    f = fmm.strassen_fmm()
+    C1, C2 = C0.clone(), C0.clone()
+    fmm.read_kernel_timing()
+    fmm.set_kernel_timing(True)
+    try:
+        fmm.split_dgemm(A, B, C1, f, 2, 6, alpha=-1.5, beta=0.5)
+        torch.cuda.synchronize()
+        _, launches, products = fmm.read_kernel_timing()
+    finally:
+        fmm.set_kernel_timing(False)
+    assert products == 49 and launches > 2
+    fmm.batch_dgemm([{"A": A, "B": B, "C": C2, "fmm": f, "levels": 2, "slices": 6, "alpha": -1.5, "beta": 0.5}])
+    torch.cuda.synchronize()
+    assert torch.equal(C1, C2)
+    assert fmm.take_device_error() == 0
