@@ -1268,45 +1268,14 @@ scatter_kernel(const int* __restrict__ tab, int r0, int nprod, int64_t m, int64_
     *cp = c;
 }
 
-/* Multi-C epilogue, element-major: one thread per element (i, j) of the
- * product grid (element index i + j*m_e in [idx_first, idx_end)) updates that
- * element of every C sub-block p, so each product's
- * Z_r[i,j] is read and converted once and shared by all sub-blocks it feeds.
- * The sub-blocks' running values live in shared memory (cs[p][thread]); for
- * every sub-block the updates still come in increasing product order, so the
- * result is identical to scatter_kernel's. Used when the sub-block count and
- * the group's W entries fit the shared-memory budget. */
-constexpr int kScatterAllSmem = 32 * 1024;   /* cs[] budget: P * threads * 8 */
-
-__global__ void __launch_bounds__(256)
-scatter_all_kernel(const int* __restrict__ tab, int r0, int nprod, int64_t m, int64_t n,
-                   int m_pad, int n_pad, int ebase, double alpha, const int64_t* __restrict__ Z,
-                   const int* __restrict__ e_row, const int* __restrict__ f_col, double* __restrict__ C,
-                   int64_t ldc, uint64_t idx_first, uint64_t idx_end)
+/* one element (i, j) of the product grid for scatter_all_kernel */
+__device__ __forceinline__ void scatter_all_element(uint64_t idx, uint32_t me, int P, int T, int tid, int nprod,
+                                                    int m_pad, int n_pad, int ebase, const int (&geo)[4][64],
+                                                    double* cs, const double* lam, const int* pidx, const int* off,
+                                                    const int64_t* __restrict__ Z, const int* __restrict__ e_row,
+                                                    const int* __restrict__ f_col, double* __restrict__ C,
+                                                    int64_t ldc)
 {
-    extern __shared__ double sm_all[];
-    __shared__ int geo[4][64];           /* per sub-block p: ro, rl, co, cl */
-    const Tab t = tab_view(tab);
-    const int P = t.mt * t.nt, T = (int)blockDim.x, tid = (int)threadIdx.x;
-    const int eb = t.w_off[r0], E = t.w_off[r0 + nprod] - eb;
-    double* cs = sm_all;                 /* [P][T] */
-    double* lam = cs + (size_t)P * T;    /* [E] */
-    int* pidx = (int*)(lam + E);         /* [E] */
-    int* off = pidx + E;                 /* [nprod + 1] */
-    for (int x = tid; x < E; x += T) {
-        pidx[x] = t.w_ent[2 * (eb + x)];
-        lam[x] = alpha * (double)t.w_ent[2 * (eb + x) + 1];
-    }
-    for (int x = tid; x <= nprod; x += T) off[x] = t.w_off[r0 + x] - eb;
-    for (int p = tid; p < P; p += T) {
-        fmm_part_geom32((int)m, t.mt, p / t.nt, &geo[0][p], &geo[1][p]);
-        fmm_part_geom32((int)n, t.nt, p % t.nt, &geo[2][p], &geo[3][p]);
-    }
-    __syncthreads();
-    const uint32_t me = (uint32_t)((m + t.mt - 1) / t.mt), ne = (uint32_t)((n + t.nt - 1) / t.nt);
-    /* me * ne < 2^32 (checked on the host), so the element index fits 32 bits */
-    const uint64_t idx = idx_first + (uint64_t)blockIdx.x * (uint64_t)T + (uint64_t)tid;
-    if (idx >= idx_end || idx >= (uint64_t)me * (uint64_t)ne) return;
     const int i = (int)((uint32_t)idx % me), j = (int)((uint32_t)idx / me);
     uint64_t live = 0;
     for (int p = 0; p < P; ++p) {
@@ -1350,6 +1319,52 @@ scatter_all_kernel(const int* __restrict__ tab, int r0, int nprod, int64_t m, in
     for (int p = 0; p < P; ++p)
         if ((live >> p) & 1ull) C[geo[0][p] + i + (int64_t)(geo[2][p] + j) * ldc] = cs[p * T + tid];
 }
+
+/* Multi-C epilogue, element-major: one thread per element (i, j) of the
+ * product grid (element index i + j*m_e in [idx_first, idx_end), grid-stride)
+ * updates that element of every C sub-block p, so each product's
+ * Z_r[i,j] is read and converted once and shared by all sub-blocks it feeds.
+ * The sub-blocks' running values live in shared memory (cs[p][thread]); for
+ * every sub-block the updates still come in increasing product order, so the
+ * result is identical to scatter_kernel's. Used when the sub-block count and
+ * the group's W entries fit the shared-memory budget. */
+constexpr int kScatterAllSmem = 32 * 1024;   /* cs[] budget: P * threads * 8 */
+
+__global__ void __launch_bounds__(256)
+scatter_all_kernel(const int* __restrict__ tab, int r0, int nprod, int64_t m, int64_t n,
+                   int m_pad, int n_pad, int ebase, double alpha, const int64_t* __restrict__ Z,
+                   const int* __restrict__ e_row, const int* __restrict__ f_col, double* __restrict__ C,
+                   int64_t ldc, uint64_t idx_first, uint64_t idx_end)
+{
+    extern __shared__ double sm_all[];
+    __shared__ int geo[4][64];           /* per sub-block p: ro, rl, co, cl */
+    const Tab t = tab_view(tab);
+    const int P = t.mt * t.nt, T = (int)blockDim.x, tid = (int)threadIdx.x;
+    const int eb = t.w_off[r0], E = t.w_off[r0 + nprod] - eb;
+    double* cs = sm_all;                 /* [P][T] */
+    double* lam = cs + (size_t)P * T;    /* [E] */
+    int* pidx = (int*)(lam + E);         /* [E] */
+    int* off = pidx + E;                 /* [nprod + 1] */
+    for (int x = tid; x < E; x += T) {
+        pidx[x] = t.w_ent[2 * (eb + x)];
+        lam[x] = alpha * (double)t.w_ent[2 * (eb + x) + 1];
+    }
+    for (int x = tid; x <= nprod; x += T) off[x] = t.w_off[r0 + x] - eb;
+    for (int p = tid; p < P; p += T) {
+        fmm_part_geom32((int)m, t.mt, p / t.nt, &geo[0][p], &geo[1][p]);
+        fmm_part_geom32((int)n, t.nt, p % t.nt, &geo[2][p], &geo[3][p]);
+    }
+    __syncthreads();
+    const uint32_t me = (uint32_t)((m + t.mt - 1) / t.mt), ne = (uint32_t)((n + t.nt - 1) / t.nt);
+    /* me * ne < 2^32 (checked on the host), so the element index fits 32 bits */
+    const uint64_t idx = idx_first + (uint64_t)blockIdx.x * (uint64_t)T + (uint64_t)tid;
+    const uint64_t end = idx_end < (uint64_t)me * (uint64_t)ne ? idx_end : (uint64_t)me * (uint64_t)ne;
+    /* grid-stride: a block's set-up above serves many elements */
+    for (uint64_t idx2 = idx; idx2 < end; idx2 += (uint64_t)gridDim.x * (uint64_t)T)
+        scatter_all_element(idx2, me, P, T, tid, nprod, m_pad, n_pad, ebase, geo, cs, lam, pidx, off, Z, e_row,
+                            f_col, C, ldc);
+}
+
 
 /* --------------------------------------------------------- host -------- */
 
@@ -1883,6 +1898,13 @@ static int job_gemm(const SplitJob& j, int np, cudaStream_t st)
     return FMM_OK;
 }
 
+/* blocks of the grid-stride element-major scatter: one per T elements, at
+ * most 16 per SM (each then serves several elements) */
+static unsigned scatter_blocks(uint64_t elems, int T)
+{
+    return (unsigned)std::min<uint64_t>((elems + T - 1) / T, 16 * 152);
+}
+
 /* the element-major scatter applies to this job (see job_scatter) */
 static bool job_scatter_all(const SplitJob& j, int r0, int np, int* T_out, size_t* smem_out)
 {
@@ -1905,7 +1927,7 @@ static void job_scatter_cols(const SplitJob& j, int r0, int np, int64_t j0, int6
     job_scatter_all(j, r0, np, &T, &smem);
     const uint64_t first = (uint64_t)j0 * (uint64_t)j.d.me, end = (uint64_t)j1 * (uint64_t)j.d.me;
     if (end <= first) return;
-    scatter_all_kernel<<<(unsigned)((end - first + T - 1) / T), (unsigned)T, smem, st>>>(
+    scatter_all_kernel<<<scatter_blocks(end - first, T), (unsigned)T, smem, st>>>(
         j.alg.tab, r0, np, j.m, j.n, (int)j.d.m_pad, (int)j.d.n_pad, job_ebase(j), j.alpha,
         (const int64_t*)(j.w + j.L.z), (const int*)(j.w + j.L.erow), (const int*)(j.w + j.L.fcol), j.C, j.ldc, first,
         end);
@@ -1926,7 +1948,7 @@ static void job_scatter(const SplitJob& j, int r0, int np, cudaStream_t st, bool
     int T = std::min(small ? 128 : 256, kScatterAllSmem / (8 * P)) / 32 * 32;
     const size_t smem = (size_t)P * std::max(T, 0) * 8 + (size_t)E * 12 + (size_t)(np + 1) * 4;
     if (P <= 64 && T >= 32 && smem <= 47 * 1024) {
-        scatter_all_kernel<<<(unsigned)((elems + T - 1) / T), (unsigned)T, smem, st>>>(
+        scatter_all_kernel<<<scatter_blocks((uint64_t)elems, T), (unsigned)T, smem, st>>>(
             j.alg.tab, r0, np, j.m, j.n, (int)j.d.m_pad, (int)j.d.n_pad, job_ebase(j), j.alpha,
             (const int64_t*)(j.w + j.L.z), (const int*)(j.w + j.L.erow), (const int*)(j.w + j.L.fcol), j.C, j.ldc,
             (uint64_t)0, (uint64_t)elems);
