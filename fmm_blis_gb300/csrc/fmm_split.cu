@@ -683,6 +683,7 @@ struct GemmLaunch {
     int nprob;
     int nitems;           /* sum over problems of products * tiles */
     int* err;
+    unsigned int* sched;  /* pair kernel: next work item, zero at launch */
     GemmProblem prob[kMaxLaunchProblems];
 };
 static_assert(sizeof(GemmLaunch) <= 32764, "GemmLaunch must fit the kernel parameter space");
@@ -970,6 +971,51 @@ constexpr uint32_t kPairHalfBytes = 128 * kBK * 2;    /* 16 KB: 128 rows of one 
 constexpr uint32_t kPairStageBytes = 2 * kPairHalfBytes;
 constexpr size_t kPairSmem = (size_t)kPairStages * kPairStageBytes + 1024 + 512;
 
+constexpr int kSchedSlots = 4;
+/* readers of each ring slot: the even CTA's MMA thread, every epilogue warp of
+ * both CTAs, the odd CTA's producer */
+constexpr int kSchedConsumers = 1 + 2 * kEpiWarps + 1;
+
+/* Consumer side of the pair kernel's work-item ring: the even CTA's producer
+ * takes items from a global counter and writes each into slot `slot` of both
+ * CTAs' rings; a consumer waits for the slot, reads it and reports it read on
+ * the even CTA's sempty barrier (release at cluster scope: the read is done
+ * before the slot can be written again). */
+struct ItemRing {
+    uint32_t base;   /* shared-memory address of sfull[0]; sempty and sitem follow */
+    int slot;
+    uint32_t ph;
+
+    __device__ __forceinline__ uint32_t full_at() const { return base + 8u * (uint32_t)slot; }
+    __device__ __forceinline__ uint32_t empty_at() const { return base + 8u * (uint32_t)(kSchedSlots + slot); }
+    __device__ __forceinline__ uint32_t item_at() const { return base + 16u * kSchedSlots + 4u * (uint32_t)slot; }
+    __device__ __forceinline__ void next()
+    {
+        if (++slot == kSchedSlots) { slot = 0; ph ^= 1; }
+    }
+    __device__ __forceinline__ bool take(int* b, volatile int* abort_flag, int* err, int code)
+    {
+        if (!sm103::mbar_wait_acq_cluster_u32(full_at(), ph, abort_flag, err, code)) return false;
+        *b = (int)sm103::ld_shared_u32(item_at());
+        sm103::mbar_arrive_release_cluster(sm103::mapa(empty_at(), 0));
+        next();
+        return true;
+    }
+    /* lane 0 of a warp takes the slot and hands the item to the other lanes */
+    __device__ __forceinline__ bool take_warp(int* b, int lane, volatile int* abort_flag, int* err, int code)
+    {
+        int got = 0, v = 0;
+        if (lane == 0) {
+            got = take(&v, abort_flag, err, code) ? 1 : 0;
+        } else {
+            next();
+        }
+        got = __shfl_sync(0xffffffffu, got, 0);
+        *b = __shfl_sync(0xffffffffu, v, 0);
+        return got != 0;
+    }
+};
+
 /* The same GEMM as split_gemm_kernel with CTA pairs (clusters of two): a work
  * item is a 256 x 256 tile of a product; each CTA loads its 128 rows of the A
  * slice tile and its 128-column half of the B slice tile (32 KB per stage
@@ -993,12 +1039,14 @@ split_gemm_pair_kernel(const __grid_constant__ GemmLaunch L)
     uint64_t* accf = empty + kPairStages;
     uint64_t* acce = accf + 2;
     uint64_t* drain = acce + 2;
-    uint32_t* tmem_slot = (uint32_t*)(drain + 1);
+    uint64_t* sfull = drain + 1;                  /* item ring: slot written */
+    uint64_t* sempty = sfull + kSchedSlots;       /* item ring: slot read by every consumer (even CTA) */
+    int* sitem = (int*)(sempty + kSchedSlots);
+    uint32_t* tmem_slot = (uint32_t*)(sitem + kSchedSlots);
     volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
 
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
     const uint32_t rank = sm103::cluster_ctarank();
-    const int cl = (int)(blockIdx.x / 2), ncl = (int)(gridDim.x / 2);
 
     if (threadIdx.x == 0) {
         for (int i = 0; i < kPairStages; ++i) {
@@ -1007,6 +1055,10 @@ split_gemm_pair_kernel(const __grid_constant__ GemmLaunch L)
         }
         for (int i = 0; i < 2; ++i) { sm103::mbar_init(&accf[i], 1); sm103::mbar_init(&acce[i], 2 * kEpiWarps); }
         sm103::mbar_init(drain, 1);
+        for (int i = 0; i < kSchedSlots; ++i) {
+            sm103::mbar_init(&sfull[i], 1);
+            sm103::mbar_init(&sempty[i], kSchedConsumers);
+        }
         *abort_flag = 0;
         sm103::fence_mbar_init();
     }
@@ -1024,7 +1076,28 @@ split_gemm_pair_kernel(const __grid_constant__ GemmLaunch L)
             uint32_t armed = 0;
             bool ok = true;
             int last_p = -1;
-            for (int b = cl; b < L.nitems && ok; b += ncl) {
+            ItemRing ring{sm103::smem_u32(sfull), 0, 0};
+            for (;;) {
+                int b;
+                if (rank == 0) {
+                    /* the even producer takes the next item and publishes it
+                     * to both CTAs' rings */
+                    if (!sm103::mbar_wait_acq_cluster_u32(ring.empty_at(), ring.ph ^ 1, abort_flag, L.err, 17)) {
+                        ok = false;
+                        break;
+                    }
+                    b = (int)atomicAdd(L.sched, 1u);
+                    if (b >= L.nitems) b = -1;
+                    sitem[ring.slot] = b;
+                    sm103::st_shared_cluster_u32(sm103::mapa(sm103::smem_u32(&sitem[ring.slot]), 1), (uint32_t)b);
+                    sm103::mbar_arrive(&sfull[ring.slot]);
+                    sm103::mbar_arrive_release_cluster(sm103::mapa(sm103::smem_u32(&sfull[ring.slot]), 1));
+                    ring.next();
+                } else if (!ring.take(&b, abort_flag, L.err, 18)) {
+                    ok = false;
+                    break;
+                }
+                if (b < 0) break;
                 const Item it = decode_item(L, b, kPairRasterGroup);
                 const GemmProblem& P = L.prob[it.p];
                 if (it.p != last_p) { sm103::prefetch_tmap(&P.tmA); sm103::prefetch_tmap(&P.tmB); last_p = it.p; }
@@ -1072,7 +1145,11 @@ split_gemm_pair_kernel(const __grid_constant__ GemmLaunch L)
             int st = 0, buf = 0;
             uint32_t ph = 0, aph = 0;
             bool ok = true;
-            for (int b = cl; b < L.nitems && ok; b += ncl) {
+            ItemRing ring{sm103::smem_u32(sfull), 0, 0};
+            for (;;) {
+                int b;
+                if (!ring.take(&b, abort_flag, L.err, 19)) { ok = false; break; }
+                if (b < 0) break;
                 const Item it = decode_item(L, b, kPairRasterGroup);
                 const int s = L.prob[it.p].s, nkb = L.prob[it.p].nkb, fmt = L.prob[it.p].fmt;
                 for (int g = 2; g <= s + 1 && ok; ++g) {
@@ -1128,7 +1205,11 @@ split_gemm_pair_kernel(const __grid_constant__ GemmLaunch L)
         uint64_t pol_keep, pol_drop;
         asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol_keep));
         asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol_drop));
-        for (int b = cl; b < L.nitems && ok; b += ncl) {
+        ItemRing ring{sm103::smem_u32(sfull), 0, 0};
+        for (;;) {
+            int b;
+            if (!ring.take_warp(&b, lane, abort_flag, L.err, 20)) { ok = false; break; }
+            if (b < 0) break;
             const Item it = decode_item(L, b, kPairRasterGroup);
             const GemmProblem& P = L.prob[it.p];
             const int s = P.s, nkb = P.nkb;
@@ -1446,7 +1527,7 @@ int group_size(const AlgView& alg, const Dims& d, int s, size_t budget, int fmt)
 }
 
 struct WsLayout {
-    size_t amax, bmax, erow, fcol, sa, sb, z, total;
+    size_t amax, bmax, sched, erow, fcol, sa, sb, z, total;
     int group;
 };
 
@@ -1459,6 +1540,7 @@ WsLayout ws_layout_g(const AlgView& alg, const Dims& d, int64_t m, int64_t n, in
     L.group = G;
     L.amax = take(sizeof(unsigned long long) * (size_t)alg.kt * (size_t)m);
     L.bmax = take(sizeof(unsigned long long) * (size_t)alg.kt * (size_t)n);
+    L.sched = take(sizeof(unsigned int));   /* the pair GEMM's work-item counter */
     L.erow = take(sizeof(int) * (size_t)G * (size_t)d.m_pad);
     L.fcol = take(sizeof(int) * (size_t)G * (size_t)d.n_pad);
     L.sa = take(esz * (size_t)G * s * (size_t)d.m_pad * (size_t)d.k_pad);
@@ -1892,6 +1974,7 @@ static int job_gemm(const SplitJob& j, int np, cudaStream_t st)
         const int cnt = std::min(K, np - r);
         memset(&gl, 0, sizeof(gl));
         gl.nprob = 1;
+        gl.sched = (unsigned int*)(j.w + j.L.sched);
         if (int rc = job_fill(j, gl.prob[0], cnt, 0, pair, r); rc != FMM_OK) return rc;
         if (int rc = launch_gemm(gl, job_items(j, cnt, pair), cnt, st, pair); rc != FMM_OK) return rc;
     }
@@ -1985,8 +2068,11 @@ static int launch_gemm(GemmLaunch& gl, int64_t nitems, int nprod_timed, cudaStre
         std::lock_guard<std::mutex> lk(g_timing_mu);
         g_timed_products += (uint64_t)nprod_timed;
     }
-    if (pair)   /* clusters of two CTAs, one pair tile each at a time */
+    if (pair) {   /* clusters of two CTAs, one pair tile each at a time, items from gl.sched */
+        if (gl.sched == nullptr || cudaMemsetAsync(gl.sched, 0, sizeof(unsigned int), st) != cudaSuccess)
+            return FMM_ERR_CUDA;
         split_gemm_pair_kernel<<<(unsigned)(2 * std::min<int64_t>(nitems, sms / 2)), kGemmThreads, kPairSmem, st>>>(gl);
+    }
     else
         split_gemm_kernel<<<(unsigned)std::min<int64_t>(nitems, sms), kGemmThreads, kGemmSmem, st>>>(gl);
     if (timed) timing_mark(st, false);
@@ -2347,6 +2433,7 @@ int fmm_split_batch(int count, const SplitJob* jobs_in, void* ws, size_t ws_byte
             for (int q : ord) {
                 SplitJob& j = jobs[q];
                 if (job_pair(j) != pair) continue;
+                if (gl.sched == nullptr) gl.sched = (unsigned int*)(j.w + j.L.sched);
                 int rc = job_fill(j, gl.prob[gl.nprob++], j.alg.R, (int)items, pair);
                 if (rc != FMM_OK) return rc;
                 items += job_items(j, j.alg.R, pair);

@@ -104,6 +104,88 @@ __device__ __forceinline__ uint32_t mapa(uint32_t smem_addr, uint32_t rank)
     return r;
 }
 
+/* arrive on an mbarrier of a CTA of the cluster, ordering this thread's
+ * earlier loads and stores (also to other CTAs' shared memory) before it */
+__device__ __forceinline__ void mbar_arrive_release_cluster(uint32_t cluster_addr)
+{
+    asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(cluster_addr) : "memory");
+}
+
+/* the same wait on a barrier given by its shared-memory address */
+__device__ __forceinline__ bool mbar_wait_acq_cluster_u32(uint32_t bar, uint32_t parity, volatile int* abort_flag,
+                                                          int* err, int code);
+
+__device__ __forceinline__ uint32_t ld_shared_u32(uint32_t addr)
+{
+    uint32_t v;
+    asm volatile("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(addr) : "memory");
+    return v;
+}
+
+/* store to the shared memory of a CTA of the cluster (address from mapa) */
+__device__ __forceinline__ void st_shared_cluster_u32(uint32_t cluster_addr, uint32_t v)
+{
+    asm volatile("st.shared::cluster.u32 [%0], %1;" ::"r"(cluster_addr), "r"(v) : "memory");
+}
+
+/* mbar_wait for a phase completed by arrivals (with release.cluster) from
+ * either CTA of the cluster: acquire at cluster scope */
+__device__ __forceinline__ bool mbar_try_wait_acq_cluster(uint64_t* bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok) : "r"(smem_u32(bar)), "r"(parity) : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ bool mbar_try_wait_acq_cluster_u32(uint32_t bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ bool mbar_wait_acq_cluster(uint64_t* bar, uint32_t parity, volatile int* abort_flag,
+                                                      int* err, int code)
+{
+    if (mbar_try_wait_acq_cluster(bar, parity)) return true;
+    uint64_t t0 = globaltimer();
+    for (uint32_t it = 0;; ++it) {
+        if (mbar_try_wait_acq_cluster(bar, parity)) return true;
+        if ((it & 255u) == 255u) {
+            if (*abort_flag) return false;
+            if (globaltimer() - t0 > kWaitLimitNs) {
+                *abort_flag = 1;
+                atomicCAS(err, 0, code);
+                return false;
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ bool mbar_wait_acq_cluster_u32(uint32_t bar, uint32_t parity, volatile int* abort_flag,
+                                                          int* err, int code)
+{
+    if (mbar_try_wait_acq_cluster_u32(bar, parity)) return true;
+    uint64_t t0 = globaltimer();
+    for (uint32_t it = 0;; ++it) {
+        if (mbar_try_wait_acq_cluster_u32(bar, parity)) return true;
+        if ((it & 255u) == 255u) {
+            if (*abort_flag) return false;
+            if (globaltimer() - t0 > kWaitLimitNs) {
+                *abort_flag = 1;
+                atomicCAS(err, 0, code);
+                return false;
+            }
+        }
+    }
+}
+
 /* 2-D TMA tiled load into this CTA's shared memory whose completion is
  * counted on an mbarrier of either CTA of the pair (bar_cluster from mapa) */
 __device__ __forceinline__ void tma_load_2d_pair(void* dst, const void* tmap, uint32_t bar_cluster, int x, int y)
