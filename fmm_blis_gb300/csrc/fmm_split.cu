@@ -1016,7 +1016,12 @@ struct ItemRing {
     }
 };
 
-/* The same GEMM as split_gemm_kernel with CTA pairs (clusters of two): a work
+/* The same GEMM as split_gemm_kernel with CTA pairs (clusters of two), with
+ * work items drawn dynamically: the even CTA's producer takes the next item
+ * from L.sched (atomicAdd) and writes it into both CTAs' item rings; every
+ * other role reads the ring, so the clusters' items in flight stay
+ * contiguous and share operand panels in L2 (a static round robin lets them
+ * drift apart). A work */
  * item is a 256 x 256 tile of a product; each CTA loads its 128 rows of the A
  * slice tile and its 128-column half of the B slice tile (32 KB per stage
  * instead of 48 KB, so the L2 feeds each SM a third less per MMA and the
@@ -1956,11 +1961,13 @@ static int launch_gemm(GemmLaunch& gl, int64_t nitems, int nprod_timed, cudaStre
 
 /* The GEMM of the job's current product group, as back-to-back launches of
  * at most K products, K the fewest products that give each launch about 24
- * rounds of work items over the GPU. The persistent CTAs take items round
- * robin; over a long launch they drift apart and share fewer operand panels
- * in L2, and a new launch starts them together again (measured at 16384,
- * two Strassen levels: 92-96 ms of GEMM per step in one launch of 49
- * products, 86-87 ms in launches of 7). */
+ * rounds of work items over the GPU. The single-SM kernel's persistent CTAs
+ * take items round robin and drift apart over a long launch, sharing fewer
+ * operand panels in L2; a new launch starts them together again (measured at
+ * 16384, two Strassen levels, when the pair kernel also took items round
+ * robin: 92-96 ms of GEMM per step in one launch of 49 products, 86-87 ms in
+ * launches of 7). The pair kernel now draws items dynamically and measured
+ * the same with 2 or 7 launches per step. */
 static int job_gemm(const SplitJob& j, int np, cudaStream_t st)
 {
     const bool pair = job_pair(j);
