@@ -1021,8 +1021,7 @@ struct ItemRing {
  * from L.sched (atomicAdd) and writes it into both CTAs' item rings; every
  * other role reads the ring, so the clusters' items in flight stay
  * contiguous and share operand panels in L2 (a static round robin lets them
- * drift apart). A work */
- * item is a 256 x 256 tile of a product; each CTA loads its 128 rows of the A
+ * drift apart). A work item is a 256 x 256 tile of a product; each CTA loads its 128 rows of the A
  * slice tile and its 128-column half of the B slice tile (32 KB per stage
  * instead of 48 KB, so the L2 feeds each SM a third less per MMA and the
  * six-stage ring looks 50% further ahead), and the even CTA issues
