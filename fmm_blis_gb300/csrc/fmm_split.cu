@@ -720,6 +720,51 @@ __device__ __forceinline__ Item decode_item(const GemmLaunch& L, int b, int rast
     return it;
 }
 
+constexpr int kSchedSlots = 4;
+/* readers of each ring slot: the even CTA's MMA thread, every epilogue warp of
+ * both CTAs, the odd CTA's producer */
+constexpr int kSchedConsumers = 1 + 2 * kEpiWarps + 1;
+
+/* Consumer side of the pair kernel's work-item ring: the even CTA's producer
+ * takes items from a global counter and writes each into slot `slot` of both
+ * CTAs' rings; a consumer waits for the slot, reads it and reports it read on
+ * the even CTA's sempty barrier (release at cluster scope: the read is done
+ * before the slot can be written again). */
+struct ItemRing {
+    uint32_t base;   /* shared-memory address of sfull[0]; sempty and sitem follow */
+    int slot;
+    uint32_t ph;
+
+    __device__ __forceinline__ uint32_t full_at() const { return base + 8u * (uint32_t)slot; }
+    __device__ __forceinline__ uint32_t empty_at() const { return base + 8u * (uint32_t)(kSchedSlots + slot); }
+    __device__ __forceinline__ uint32_t item_at() const { return base + 16u * kSchedSlots + 4u * (uint32_t)slot; }
+    __device__ __forceinline__ void next()
+    {
+        if (++slot == kSchedSlots) { slot = 0; ph ^= 1; }
+    }
+    __device__ __forceinline__ bool take(int* b, volatile int* abort_flag, int* err, int code)
+    {
+        if (!sm103::mbar_wait_acq_cluster_u32(full_at(), ph, abort_flag, err, code)) return false;
+        *b = (int)sm103::ld_shared_u32(item_at());
+        sm103::mbar_arrive_release_cluster(sm103::mapa(empty_at(), 0));
+        next();
+        return true;
+    }
+    /* lane 0 of a warp takes the slot and hands the item to the other lanes */
+    __device__ __forceinline__ bool take_warp(int* b, int lane, volatile int* abort_flag, int* err, int code)
+    {
+        int got = 0, v = 0;
+        if (lane == 0) {
+            got = take(&v, abort_flag, err, code) ? 1 : 0;
+        } else {
+            next();
+        }
+        got = __shfl_sync(0xffffffffu, got, 0);
+        *b = __shfl_sync(0xffffffffu, v, 0);
+        return got != 0;
+    }
+};
+
 /* Persistent GEMM over a list of work items (problem, product of its group,
  * 128 x 256 output tile); CTA c takes items c, c + gridDim.x, ... One CTA per
  * SM: warp 0 issues the TMA loads of the digit-slice tiles, warp 1 the
@@ -742,7 +787,10 @@ split_gemm_kernel(const __grid_constant__ GemmLaunch L)
     uint64_t* accf = empty + kStages;
     uint64_t* acce = accf + 2;
     uint64_t* drain = acce + 2;
-    uint32_t* tmem_slot = (uint32_t*)(drain + 1);
+    uint64_t* sfull = drain + 1;                  /* item ring: slot written */
+    uint64_t* sempty = sfull + kSchedSlots;       /* item ring: slot read by every consumer */
+    int* sitem = (int*)(sempty + kSchedSlots);
+    uint32_t* tmem_slot = (uint32_t*)(sitem + kSchedSlots);
     volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
 
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
@@ -751,6 +799,10 @@ split_gemm_kernel(const __grid_constant__ GemmLaunch L)
         for (int i = 0; i < kStages; ++i) { sm103::mbar_init(&full[i], 1); sm103::mbar_init(&empty[i], 1); }
         for (int i = 0; i < 2; ++i) { sm103::mbar_init(&accf[i], 1); sm103::mbar_init(&acce[i], kEpiWarps); }
         sm103::mbar_init(drain, 1);
+        for (int i = 0; i < kSchedSlots; ++i) {
+            sm103::mbar_init(&sfull[i], 1);
+            sm103::mbar_init(&sempty[i], 1 + kEpiWarps);   /* the MMA thread and every epilogue warp */
+        }
         *abort_flag = 0;
         sm103::fence_mbar_init();
     }
@@ -768,7 +820,19 @@ split_gemm_kernel(const __grid_constant__ GemmLaunch L)
             uint32_t armed = 0;  /* stages armed in the current pass (bit mask) */
             bool ok = true;
             int last_p = -1;
-            for (int b = blockIdx.x; b < L.nitems && ok; b += gridDim.x) {
+            ItemRing ring{sm103::smem_u32(sfull), 0, 0};
+            for (;;) {
+                /* the producer takes the next item from L.sched and publishes it */
+                if (!sm103::mbar_wait_acq_cluster_u32(ring.empty_at(), ring.ph ^ 1, abort_flag, L.err, 7)) {
+                    ok = false;
+                    break;
+                }
+                int b = (int)atomicAdd(L.sched, 1u);
+                if (b >= L.nitems) b = -1;
+                sitem[ring.slot] = b;
+                sm103::mbar_arrive(&sfull[ring.slot]);
+                ring.next();
+                if (b < 0) break;
                 const Item it = decode_item(L, b);
                 const GemmProblem& P = L.prob[it.p];
                 if (it.p != last_p) { sm103::prefetch_tmap(&P.tmA); sm103::prefetch_tmap(&P.tmB); last_p = it.p; }
@@ -822,7 +886,11 @@ split_gemm_kernel(const __grid_constant__ GemmLaunch L)
             int st = 0, buf = 0;
             uint32_t ph = 0, aph = 0;
             bool ok = true;
-            for (int b = blockIdx.x; b < L.nitems && ok; b += gridDim.x) {
+            ItemRing ring{sm103::smem_u32(sfull), 0, 0};
+            for (;;) {
+                int b;
+                if (!ring.take(&b, abort_flag, L.err, 8)) { ok = false; break; }
+                if (b < 0) break;
                 const Item it = decode_item(L, b);
                 const int s = L.prob[it.p].s, nkb = L.prob[it.p].nkb, fmt = L.prob[it.p].fmt;
                 for (int g = 2; g <= s + 1 && ok; ++g) {
@@ -883,7 +951,11 @@ split_gemm_kernel(const __grid_constant__ GemmLaunch L)
         uint64_t pol_keep, pol_drop;
         asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol_keep));
         asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol_drop));
-        for (int b = blockIdx.x; b < L.nitems && ok; b += gridDim.x) {
+        ItemRing ring{sm103::smem_u32(sfull), 0, 0};
+        for (;;) {
+            int b;
+            if (!ring.take_warp(&b, lane, abort_flag, L.err, 9)) { ok = false; break; }
+            if (b < 0) break;
             const Item it = decode_item(L, b);
             const GemmProblem& P = L.prob[it.p];
             const int s = P.s, nkb = P.nkb;
@@ -971,50 +1043,7 @@ constexpr uint32_t kPairHalfBytes = 128 * kBK * 2;    /* 16 KB: 128 rows of one 
 constexpr uint32_t kPairStageBytes = 2 * kPairHalfBytes;
 constexpr size_t kPairSmem = (size_t)kPairStages * kPairStageBytes + 1024 + 512;
 
-constexpr int kSchedSlots = 4;
-/* readers of each ring slot: the even CTA's MMA thread, every epilogue warp of
- * both CTAs, the odd CTA's producer */
-constexpr int kSchedConsumers = 1 + 2 * kEpiWarps + 1;
 
-/* Consumer side of the pair kernel's work-item ring: the even CTA's producer
- * takes items from a global counter and writes each into slot `slot` of both
- * CTAs' rings; a consumer waits for the slot, reads it and reports it read on
- * the even CTA's sempty barrier (release at cluster scope: the read is done
- * before the slot can be written again). */
-struct ItemRing {
-    uint32_t base;   /* shared-memory address of sfull[0]; sempty and sitem follow */
-    int slot;
-    uint32_t ph;
-
-    __device__ __forceinline__ uint32_t full_at() const { return base + 8u * (uint32_t)slot; }
-    __device__ __forceinline__ uint32_t empty_at() const { return base + 8u * (uint32_t)(kSchedSlots + slot); }
-    __device__ __forceinline__ uint32_t item_at() const { return base + 16u * kSchedSlots + 4u * (uint32_t)slot; }
-    __device__ __forceinline__ void next()
-    {
-        if (++slot == kSchedSlots) { slot = 0; ph ^= 1; }
-    }
-    __device__ __forceinline__ bool take(int* b, volatile int* abort_flag, int* err, int code)
-    {
-        if (!sm103::mbar_wait_acq_cluster_u32(full_at(), ph, abort_flag, err, code)) return false;
-        *b = (int)sm103::ld_shared_u32(item_at());
-        sm103::mbar_arrive_release_cluster(sm103::mapa(empty_at(), 0));
-        next();
-        return true;
-    }
-    /* lane 0 of a warp takes the slot and hands the item to the other lanes */
-    __device__ __forceinline__ bool take_warp(int* b, int lane, volatile int* abort_flag, int* err, int code)
-    {
-        int got = 0, v = 0;
-        if (lane == 0) {
-            got = take(&v, abort_flag, err, code) ? 1 : 0;
-        } else {
-            next();
-        }
-        got = __shfl_sync(0xffffffffu, got, 0);
-        *b = __shfl_sync(0xffffffffu, v, 0);
-        return got != 0;
-    }
-};
 
 /* The same GEMM as split_gemm_kernel with CTA pairs (clusters of two), with
  * work items drawn dynamically: the even CTA's producer takes the next item
@@ -2074,11 +2103,11 @@ static int launch_gemm(GemmLaunch& gl, int64_t nitems, int nprod_timed, cudaStre
         std::lock_guard<std::mutex> lk(g_timing_mu);
         g_timed_products += (uint64_t)nprod_timed;
     }
-    if (pair) {   /* clusters of two CTAs, one pair tile each at a time, items from gl.sched */
-        if (gl.sched == nullptr || cudaMemsetAsync(gl.sched, 0, sizeof(unsigned int), st) != cudaSuccess)
-            return FMM_ERR_CUDA;
+    /* both kernels draw their work items from gl.sched, zero at launch */
+    if (gl.sched == nullptr || cudaMemsetAsync(gl.sched, 0, sizeof(unsigned int), st) != cudaSuccess)
+        return FMM_ERR_CUDA;
+    if (pair)   /* clusters of two CTAs, one pair tile each at a time */
         split_gemm_pair_kernel<<<(unsigned)(2 * std::min<int64_t>(nitems, sms / 2)), kGemmThreads, kPairSmem, st>>>(gl);
-    }
     else
         split_gemm_kernel<<<(unsigned)std::min<int64_t>(nitems, sms), kGemmThreads, kGemmSmem, st>>>(gl);
     if (timed) timing_mark(st, false);
