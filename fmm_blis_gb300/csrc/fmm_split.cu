@@ -766,7 +766,9 @@ struct ItemRing {
 };
 
 /* Persistent GEMM over a list of work items (problem, product of its group,
- * 128 x 256 output tile); CTA c takes items c, c + gridDim.x, ... One CTA per
+ * 128 x 256 output tile), drawn dynamically: the producer takes the next item
+ * from L.sched and passes it to the other roles through a CTA-local item
+ * ring, so the CTAs' items in flight stay contiguous. One CTA per
  * SM: warp 0 issues the TMA loads of the digit-slice tiles, warp 1 the
  * tcgen05.mma (M=128, N=256, K=16 BF16 or K=32 FP8 per the item's problem:
  * 128 clocks per MMA hide the accumulator dependency), warps 2..17 drain
@@ -1989,13 +1991,13 @@ static int launch_gemm(GemmLaunch& gl, int64_t nitems, int nprod_timed, cudaStre
 
 /* The GEMM of the job's current product group, as back-to-back launches of
  * at most K products, K the fewest products that give each launch about 24
- * rounds of work items over the GPU. The single-SM kernel's persistent CTAs
- * take items round robin and drift apart over a long launch, sharing fewer
- * operand panels in L2; a new launch starts them together again (measured at
- * 16384, two Strassen levels, when the pair kernel also took items round
- * robin: 92-96 ms of GEMM per step in one launch of 49 products, 86-87 ms in
- * launches of 7). The pair kernel now draws items dynamically and measured
- * the same with 2 or 7 launches per step. */
+ * rounds of work items over the GPU. When the kernels took their items round
+ * robin, the persistent CTAs drifted apart over a long launch and shared
+ * fewer operand panels in L2, and a new launch started them together again
+ * (measured at 16384, two Strassen levels: 92-96 ms of GEMM per step in one
+ * launch of 49 products, 86-87 ms in launches of 7). With items drawn
+ * dynamically the pair kernel measured the same with 2 or 7 launches per
+ * step. */
 static int job_gemm(const SplitJob& j, int np, cudaStream_t st)
 {
     const bool pair = job_pair(j);
