@@ -170,10 +170,13 @@ int fmm_gpu_strassen_ab(double alpha, const double* A, int64_t lda,
 /* ------------------------------------ GPU, split-precision (Ozaki) form -- */
 
 /* Bytes of device workspace recommended for fmm_gpu_split_dgemm: products
- * are processed in groups (all products of a group are packed, multiplied in
- * one launch and added into C in one pass), and this size holds the largest
- * group that fits in 32 GiB. Any smaller workspace that holds one product's
- * digit slices and level accumulators also works, with smaller groups. */
+ * are processed in groups (all products of a group are packed, multiplied and
+ * added into C in one pass), and this size holds the largest group that fits
+ * in 32 GiB; when that is all R products, it holds two groups of ceil(R/2)
+ * instead, whose packs and C updates overlap the other group's GEMM. Any
+ * smaller workspace that holds one product's digit slices and level
+ * accumulators also works, with smaller groups; the result is the same bit
+ * for bit whatever the grouping. */
 size_t fmm_gpu_split_workspace_size(const fmm_t* fmm, int levels,
                                     int64_t m, int64_t n, int64_t k,
                                     int slices);
