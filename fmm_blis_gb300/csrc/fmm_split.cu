@@ -2083,21 +2083,23 @@ static void job_scatter(const SplitJob& j, int r0, int np, cudaStream_t st, bool
 
 static int launch_gemm(GemmLaunch& gl, int64_t nitems, int nprod_timed, cudaStream_t st, bool pair)
 {
-    static bool attr_set = false;
-    if (!attr_set) {
+    /* the kernels' shared-memory limit is a per-device attribute: set once per device */
+    static std::atomic<uint64_t> attr_set{0};
+    int dev = 0, sms = 152;
+    if (cudaGetDevice(&dev) != cudaSuccess) return FMM_ERR_CUDA;
+    const uint64_t bit = dev < 64 ? 1ull << dev : 0;
+    if (bit == 0 || !(attr_set.load(std::memory_order_acquire) & bit)) {
         if (cudaFuncSetAttribute(split_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)kGemmSmem) != cudaSuccess ||
             cudaFuncSetAttribute(split_gemm_pair_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)kPairSmem) != cudaSuccess)
             return FMM_ERR_CUDA;
-        attr_set = true;
+        attr_set.fetch_or(bit, std::memory_order_acq_rel);
     }
     if (nitems > 0x7fffffffLL) return FMM_ERR_UNSUPPORTED;
     if (nitems == 0) return FMM_OK;
     gl.nitems = (int)nitems;
     gl.err = fmm_device_error_word();
-    int dev = 0, sms = 152;
-    cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const bool timed = g_timing;
     if (timed) {
