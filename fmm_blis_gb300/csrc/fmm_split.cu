@@ -48,6 +48,21 @@
  *
  * Limits: k_e = ceil(k/k~) <= 16384 per call (level sums stay inside int32
  * and Z inside int64); slices 2..8 (BF16) or 2..12 (FP8); finite inputs.
+ *
+ * Execution. Two persistent GEMM kernels: split_gemm_kernel (one CTA per SM,
+ * 128 x 256 tiles) and split_gemm_pair_kernel (clusters of two CTAs, 256 x 256
+ * tiles, tcgen05.mma cta_group::2), used from m_e = 1024; both draw their
+ * (problem, product, tile) work items dynamically from a counter, so the
+ * items in flight stay contiguous. A single call packs, multiplies and
+ * updates C per product group; when the workspace holds all products it runs
+ * them as two groups, the second group's packs and the first group's C
+ * updates on pool streams beside the other group's GEMM, and a group's GEMM
+ * as launches of about 24 rounds of items. The host-buffer call overlaps the
+ * copies with the work (B in column chunks chased by its packs, C read back
+ * in column chunks behind the last C updates). Batched calls run waves of up
+ * to 80 problems, one GEMM launch per tile kind per wave, waves alternating
+ * between two workspace halves so a wave's packs overlap the previous wave.
+ * Every path gives the same bits for a problem.
  */
 #include "fmm_internal.h"
 #include "sm103_ptx.cuh"
