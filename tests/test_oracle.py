@@ -120,3 +120,44 @@ def test_split_oracle_fp8_digits(orc, algs):
     orc.split_fmm_dgemm(algs["222"], A, B, C, 6)
     e_bf16 = float(np.abs(C - ref).max())
     assert errs[10 - 3] < 4 * e_bf16
+
+
+@pytest.mark.parametrize("alg,levels,shape,s,fmt,ab", [
+    ("222", 1, (7, 9, 5), 6, "bf16", (1.0, 1.0)),
+    ("222", 1, (13, 11, 17), 3, "bf16", (-0.75, 0.5)),
+    ("232", 1, (9, 10, 8), 8, "bf16", (1.0, 0.0)),
+    ("333", 1, (10, 8, 11), 2, "bf16", (2.0, 1.0)),
+    ("222", 2, (9, 10, 11), 6, "bf16", (1.0, 1.0)),
+    ("222", 1, (6, 5, 300), 6, "bf16", (1.0, 1.0)),     # k_pad > 128: Z in units of level 6
+    ("222", 1, (7, 9, 5), 9, "fp8", (1.0, 1.0)),
+    ("322", 1, (11, 7, 9), 12, "fp8", (0.5, -1.0)),
+    ("222", 1, (8, 6, 40), 4, "fp8", (1.0, 1.0)),
+])
+def test_split_oracle_equals_independent_restatement(orc, algs, alg, levels, shape, s, fmt, ab):
+    """The C oracle's split form equals, bit for bit, a second restatement in
+    exact arithmetic written from the definitions (tests/split_restatement.py)."""
+    from oracle import coeffs as oc
+    from split_restatement import split_fmm
+    m, n, k = shape
+    a = oc.power(algs[alg], levels)
+    A, B, C = rand(m, k, 61 + m), rand(k, n, 62 + n), rand(m, n, 63 + k)
+    alpha, beta = ab
+    want = split_fmm(a, A, B, C, s, alpha, beta, fmt)
+    got = orc.split_fmm_dgemm(a, A, B, C.copy(order="F"), s, alpha, beta, fmt=fmt)
+    assert np.array_equal(got, want), float(np.max(np.abs(got - want)))
+
+
+def test_split_restatement_wide_range_inputs(orc, algs):
+    """Entries spread over many binades (digits of small entries far below
+    their row's maximum) and exact zeros: still bit for bit."""
+    from split_restatement import split_fmm
+    rng = np.random.default_rng(5)
+    A = np.asfortranarray(rng.uniform(-1, 1, (9, 12)) * np.exp2(rng.integers(-40, 10, (9, 12))))
+    B = np.asfortranarray(rng.uniform(-1, 1, (12, 7)) * np.exp2(rng.integers(-30, 30, (12, 7))))
+    A[2, :] = 0.0
+    B[:, 3] = 0.0
+    C = np.asfortranarray(rng.uniform(-1, 1, (9, 7)))
+    for fmt, s in (("bf16", 5), ("fp8", 10)):
+        want = split_fmm(algs["222"], A, B, C, s, 1.0, 1.0, fmt)
+        got = orc.split_fmm_dgemm(algs["222"], A, B, C.copy(order="F"), s, fmt=fmt)
+        assert np.array_equal(got, want)
