@@ -112,6 +112,9 @@ def lib() -> ctypes.CDLL:
     L.fmm_gpu_strassen_ab_gen.argtypes = [dbl, vp, i64, i64, vp, i64, i64, dbl, vp, i64, i64, i64, i64, i64, FmmT]
     L.fmm_gpu_split_strassen_ab_ex.restype = ci
     L.fmm_gpu_split_strassen_ab_ex.argtypes = [dbl, vp, i64, vp, i64, dbl, vp, i64, i64, i64, i64, FmmT, ci, ci, ci]
+    L.fmm_gpu_split_strassen_ab_gen.restype = ci
+    L.fmm_gpu_split_strassen_ab_gen.argtypes = [dbl, vp, i64, i64, vp, i64, i64, dbl, vp, i64, i64, i64, i64, i64,
+                                                FmmT, ci, ci, ci]
     L.fmm_gpu_release_host_buffers.restype = None
     L.fmm_gpu_release_host_buffers.argtypes = []
     L.fmm_gpu_strassen_ab.restype = ci
@@ -382,11 +385,36 @@ def batch_dgemm(problems, workspace=None, stream=None) -> None:
 
 def split_strassen_ab_ex(alpha: float, A, B, beta: float, C, fmm: FmmT | None = None, levels: int = 1,
                          slices: int = 6, fmt: str = "bf16") -> None:
-    """The split form on host arrays (Fortran-order numpy float64, or any
-    object exposing a host pointer through ``ctypes.data`` / ``data_ptr()``
-    of a pinned CPU tensor): C updated in place, synchronously, with the
-    host<->device copies overlapped with the device work."""
+    """The split form on host arrays: numpy float64 arrays of any layout
+    (Fortran order, C order, transposed or strided views) or column-major CPU
+    tensors (pinned copies fastest). C updated in place, synchronously; with
+    column-major operands the host<->device copies overlap the device work."""
     import numpy as np
+
+    arrays = [x for x in (A, B, C) if isinstance(x, np.ndarray)]
+    if len(arrays) == 3 and not all(x.flags.f_contiguous or x.size == 0 for x in arrays):
+        for name, x in (("A", A), ("B", B), ("C", C)):
+            if x.dtype != np.float64 or x.ndim != 2:
+                raise ValueError(f"{name} must be a 2-D float64 array")
+            if x.size > 0 and any(st <= 0 or st % 8 for st in x.strides):
+                raise ValueError(f"{name} needs positive element strides")
+        m, k = A.shape
+        n = B.shape[1]
+        if B.shape[0] != k or C.shape != (m, n):
+            raise ValueError("shape mismatch")
+
+        def rs(x):
+            return max(x.strides[0] // 8, 1)
+
+        def cs(x):
+            return max(x.strides[1] // 8, 1)
+
+        st = lib().fmm_gpu_split_strassen_ab_gen(alpha, A.ctypes.data, rs(A), cs(A), B.ctypes.data, rs(B), cs(B),
+                                                 beta, C.ctypes.data, rs(C), cs(C), m, n, k,
+                                                 fmm if fmm is not None else FmmT(),
+                                                 levels if fmm is not None else 0, slices, _fmt(fmt))
+        _check(st, "fmm_gpu_split_strassen_ab_gen")
+        return
 
     def info(x, name):
         if isinstance(x, np.ndarray):

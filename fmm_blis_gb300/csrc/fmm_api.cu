@@ -443,6 +443,54 @@ extern "C" int fmm_gpu_split_strassen_ab_ex(double alpha, const double* A, int64
 
 extern "C" void fmm_gpu_release_host_buffers(void) { fmm_split_host_release(); }
 
+extern "C" int fmm_gpu_split_strassen_ab_gen(double alpha, const double* A, int64_t rsa, int64_t csa,
+                                             const double* B, int64_t rsb, int64_t csb, double beta, double* C,
+                                             int64_t rsc, int64_t csc, int64_t m, int64_t n, int64_t k, fmm_t fmm,
+                                             int levels, int slices, int format)
+{
+    if (m < 0 || n < 0 || k < 0) return FMM_ERR_ARG;
+    if (rsa < 1 || csa < 1 || rsb < 1 || csb < 1 || rsc < 1 || csc < 1) return FMM_ERR_ARG;
+    if (m > 0 && n > 0 && C == nullptr) return FMM_ERR_ARG;
+    if (m > 0 && n > 0 && k > 0 && (A == nullptr || B == nullptr)) return FMM_ERR_ARG;
+    if (format != FMM_SPLIT_BF16 && format != FMM_SPLIT_FP8_E4M3) return FMM_ERR_ARG;
+    if (slices < 2 || slices > (format ? 12 : 8)) return FMM_ERR_ARG;
+    if (m == 0 || n == 0) return FMM_OK;
+    /* column-major operands: the overlapped host-buffer pipeline */
+    if (rsa == 1 && rsb == 1 && rsc == 1 && csa >= m && csb >= std::max<int64_t>(k, 1) && csc >= m)
+        return fmm_gpu_split_strassen_ab_ex(alpha, A, csa, B, csb, beta, C, csc, m, n, k, fmm, levels, slices,
+                                            format);
+    /* other layouts: column-major device copies (transposed on the device or
+     * gathered on the host), the device call, C written back in place */
+    const fmm_t* pf = levels > 0 ? &fmm : nullptr;
+    const size_t wsb = fmm_gpu_split_workspace_size_fmt(pf, levels, m, n, k, slices, format);
+    if (wsb == 0) return FMM_ERR_ARG;
+    double *dA = nullptr, *dB = nullptr, *dC = nullptr, *dT = nullptr;
+    void* ws = nullptr;
+    const int64_t ka = k > 0 ? k : 1;
+    const int64_t tmp = std::max(std::max(m * ka, ka * n), m * n);
+    int rc = FMM_OK;
+    if (cudaMalloc(&dA, sizeof(double) * (size_t)(m * ka)) != cudaSuccess ||
+        cudaMalloc(&dB, sizeof(double) * (size_t)(ka * n)) != cudaSuccess ||
+        cudaMalloc(&dC, sizeof(double) * (size_t)(m * n)) != cudaSuccess ||
+        cudaMalloc(&dT, sizeof(double) * (size_t)tmp) != cudaSuccess || cudaMalloc(&ws, wsb) != cudaSuccess)
+        rc = FMM_ERR_ALLOC;
+    if (rc == FMM_OK && k > 0) rc = operand_to_device(A, m, k, rsa, csa, dA, dT);
+    if (rc == FMM_OK && k > 0) rc = operand_to_device(B, k, n, rsb, csb, dB, dT);
+    if (rc == FMM_OK) rc = operand_to_device(C, m, n, rsc, csc, dC, dT);
+    if (rc == FMM_OK)
+        rc = fmm_gpu_split_dgemm_fmt(pf, levels, m, n, k, alpha, dA, m, dB, ka, beta, dC, m, slices, format, ws, wsb,
+                                     nullptr);
+    if (rc == FMM_OK) rc = operand_to_host(dC, m, n, C, rsc, csc, dT);
+    if (rc == FMM_OK && cudaDeviceSynchronize() != cudaSuccess) rc = FMM_ERR_CUDA;
+    cudaGetLastError();
+    cudaFree(dA);
+    cudaFree(dB);
+    cudaFree(dC);
+    cudaFree(dT);
+    cudaFree(ws);
+    return rc;
+}
+
 extern "C" int fmm_gpu_split_dgemm_fmt(const fmm_t* fmm, int levels, int64_t m, int64_t n, int64_t k,
                                        double alpha, const double* A, int64_t lda, const double* B, int64_t ldb,
                                        double beta, double* C, int64_t ldc, int slices, int format,

@@ -236,6 +236,19 @@ int fmm_gpu_split_strassen_ab_ex(double alpha, const double* A, int64_t lda,
                                  int64_t m, int64_t n, int64_t k,
                                  fmm_t fmm, int levels, int slices, int format);
 
+/* fmm_gpu_split_strassen_ab_ex for operands of any layout, as
+ * fmm_gpu_strassen_ab_gen takes them (element (i, j) of X at
+ * X[i*rs_x + j*cs_x], all strides >= 1): column-major operands go through the
+ * overlapped host-buffer call, others are made column-major on the device,
+ * multiplied and C written back in place (only C's own elements). The result
+ * equals the column-major call's bit for bit. No counterpart in the
+ * reference. */
+int fmm_gpu_split_strassen_ab_gen(double alpha, const double* A, int64_t rs_a, int64_t cs_a,
+                                  const double* B, int64_t rs_b, int64_t cs_b,
+                                  double beta, double* C, int64_t rs_c, int64_t cs_c,
+                                  int64_t m, int64_t n, int64_t k,
+                                  fmm_t fmm, int levels, int slices, int format);
+
 /* Frees the current device's buffers kept by fmm_gpu_split_strassen_ab_ex. */
 void fmm_gpu_release_host_buffers(void);
 

@@ -52,3 +52,19 @@ def test_split_host_call_rejects_bad_arguments(fmm):
     assert L.fmm_gpu_split_strassen_ab_ex(*args, 6, 2) == 1      # unknown format
     bad_ld = (1.0, A.ctypes.data, 3, A.ctypes.data, 4, 1.0, A.ctypes.data, 4, 4, 4, 4, f, 1, 6, 0)
     assert L.fmm_gpu_split_strassen_ab_ex(*bad_ld) == 1          # lda < m
+
+
+def test_split_host_gen_rejects_bad_arguments(fmm):
+    """The general-layout split host call checks strides, format and slices
+    before any device work."""
+    import numpy as np
+    L = fmm.lib()
+    A = np.zeros((4, 4))
+    f = fmm.strassen_fmm()
+    p = A.ctypes.data
+    ok = (1.0, p, 4, 1, p, 4, 1, 1.0, p, 4, 1, 4, 4, 4, f, 1)
+    assert L.fmm_gpu_split_strassen_ab_gen(*ok, 13, 1) == 1                            # slices
+    assert L.fmm_gpu_split_strassen_ab_gen(*ok, 6, 3) == 1                             # format
+    bad = (1.0, p, 0, 1, p, 4, 1, 1.0, p, 4, 1, 4, 4, 4, f, 1, 6, 0)                   # row stride 0
+    assert L.fmm_gpu_split_strassen_ab_gen(*bad) == 1
+    assert L.fmm_gpu_split_strassen_ab_gen(1.0, p, 4, 1, p, 4, 1, 1.0, p, 4, 1, -1, 4, 4, f, 1, 6, 0) == 1

@@ -93,3 +93,24 @@ def test_host_call_scalar_cases(fmm, torch_cuda):
     fmm.split_strassen_ab_ex(1.0, np.zeros((0, k), order="F"), B, 1.0, np.zeros((0, n), order="F"), f, 1, 6)
     fmm.release_host_buffers()
     assert fmm.take_device_error() == 0
+
+
+@pytest.mark.parametrize("fmt,s", [("bf16", 6), ("fp8", 10)])
+def test_host_call_any_layout(fmm, torch_cuda, fmt, s):
+    """Row-major A, a transposed view for B, a strided view for C (general
+    strides, like BLIS obj_t): the same bits as the Fortran-order call."""
+    m, n, k = 300, 170, 260
+    A, B, C = rand(m, k, 541), rand(k, n, 542), rand(m, n, 543)
+    f = fmm.strassen_fmm()
+    want = C.copy(order="F")
+    fmm.split_strassen_ab_ex(0.5, A, B, 2.0, want, f, 1, s, fmt)
+    Ar = np.ascontiguousarray(A)                       # row-major
+    Bt = np.asfortranarray(B.T).T                      # transposed view (row-major storage of B)
+    big = np.full((2 * m, 3 * n), 9.0)
+    Cv = big[::2, ::3]                                 # general strides
+    Cv[...] = C
+    fmm.split_strassen_ab_ex(0.5, Ar, Bt, 2.0, Cv, f, 1, s, fmt)
+    assert np.array_equal(Cv, want)
+    mask = np.ones_like(big, dtype=bool)
+    mask[::2, ::3] = False
+    assert np.all(big[mask] == 9.0)                    # only C's own elements written
