@@ -2619,15 +2619,15 @@ int fmm_split_launch(const AlgView& alg, int64_t m, int64_t n, int64_t k, double
 /* ---------------------------------------------------------------------------
  * Allocation-free entry point.
  *
- * For callers that must not allocate device memory while they run: code
- * inside a CUDA graph capture or a stream callback, plug-ins that run on
- * memory handed to them by a host application with its own allocator, or
- * processes whose device memory is already fully reserved. Such callers
- * cannot use fmm_gpu_split_dgemm, whose workspace they would have to obtain,
- * nor the table cache, which allocates on first use of an algorithm. This
- * variant keeps the algorithm table and the whole workspace in one
- * file-scope device array of kNoAllocScratchBytes (64 MiB), which every GPU
- * that loads the library holds until the process exits.
+ * For callers that must not allocate device memory while they run: stream
+ * callbacks and host functions, plug-ins that run on memory handed to them by
+ * a host application with its own allocator, or processes whose device memory
+ * is already fully reserved. Such callers cannot use fmm_gpu_split_dgemm,
+ * whose workspace they would have to obtain, nor the table cache, which
+ * allocates on first use of an algorithm. This variant keeps the algorithm
+ * table and the whole workspace in one file-scope device array of
+ * kNoAllocScratchBytes (64 MiB), which every GPU that loads the library holds
+ * until the process exits.
  * ------------------------------------------------------------------------- */
 constexpr size_t kNoAllocScratchBytes = (size_t)64 << 20;
 static __device__ __align__(256) uint8_t g_noalloc_scratch[kNoAllocScratchBytes];
@@ -2635,6 +2635,19 @@ static __device__ __align__(256) uint8_t g_noalloc_scratch[kNoAllocScratchBytes]
 namespace {
 std::mutex g_noalloc_mu;
 uint8_t* g_noalloc_ptr[64];
+
+/* One piece of an algorithm table, passed by value: the launch copies the
+ * values when it is enqueued, so no host buffer has to outlive the call. */
+constexpr int kTabChunkInts = 4000;
+struct TabChunk {
+    int n;
+    int v[kTabChunkInts];
+};
+
+__global__ void __launch_bounds__(256) noalloc_table_kernel(int* __restrict__ dst, const __grid_constant__ TabChunk c)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < c.n; i += gridDim.x * blockDim.x) dst[i] = c.v[i];
+}
 }  // namespace
 
 extern "C" int fmm_gpu_split_dgemm_noalloc(const fmm_t* fmm, int levels, int64_t m, int64_t n, int64_t k,
@@ -2676,11 +2689,17 @@ extern "C" int fmm_gpu_split_dgemm_noalloc(const fmm_t* fmm, int levels, int64_t
         return FMM_ERR_SCRATCH;
     if (fmm_device_error_word() == nullptr) return FMM_ERR_CUDA;
     cudaStream_t st = (cudaStream_t)stream;
-    /* the table goes to the front of the scratch (the pageable source is
-     * consumed before cudaMemcpyAsync returns) */
-    if (cudaMemcpyAsync(scratch, table.data(), sizeof(int) * table.size(), cudaMemcpyHostToDevice, st) !=
-        cudaSuccess)
-        return FMM_ERR_CUDA;
+    /* the table goes to the front of the scratch, written by kernels that
+     * carry it as their parameter (never a copy from this call's host vector,
+     * which is gone once the call returns) */
+    for (size_t off = 0; off < table.size(); off += kTabChunkInts) {
+        TabChunk c;
+        c.n = (int)std::min<size_t>(kTabChunkInts, table.size() - off);
+        std::memcpy(c.v, table.data() + off, sizeof(int) * (size_t)c.n);
+        noalloc_table_kernel<<<(c.n + 255) / 256, 256, 0, st>>>((int*)scratch + off, c);
+        if (cudaGetLastError() != cudaSuccess) return FMM_ERR_CUDA;
+        fmm_count_launch(1);
+    }
     alg.tab = (const int*)scratch;
     alg.htab = table.data();
     return split_launch_budget(alg, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, slices, 0, scratch + tab_bytes,

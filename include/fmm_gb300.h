@@ -290,17 +290,22 @@ int fmm_gpu_batch_dgemm(int count, const fmm_batch_problem* problems,
                         void* workspace, size_t workspace_bytes, void* stream);
 
 /* fmm_gpu_split_dgemm for callers that must not allocate device memory
- * while they run (code inside a CUDA graph capture or a stream callback,
- * plug-ins working in memory a host application hands them, processes whose
- * device memory is fully reserved): it calls no cudaMalloc, cudaFree or other
- * device allocator. No counterpart in the reference. The algorithm table and
- * the workspace live in one static device array of 64 MiB that every GPU
- * loading the library keeps until exit; a problem whose workspace (slices and
- * level accumulators for at least one product) does not fit returns
- * FMM_ERR_SCRATCH. The first call on a device looks up the array's device
- * address; make that first call before any stream capture. All calls share
- * the array and each call rewrites what it uses, so calls whose GPU work
- * overlaps (other streams, other threads) race: serialize them. */
+ * while they run: a plug-in working in memory a host application hands it
+ * (the application's own caching allocator owns the device, and a cudaMalloc
+ * behind its back can fail or fragment its pool), a process whose device
+ * memory is fully reserved, a latency-bound loop that cannot afford
+ * cudaFree's implicit device synchronization. It calls no cudaMalloc, cudaFree or other device
+ * allocator. No counterpart in the reference. The algorithm table and the
+ * workspace live in one static device array of 64 MiB that every GPU loading
+ * the library keeps until exit; a problem whose workspace (slices and level
+ * accumulators for at least one product) does not fit returns
+ * FMM_ERR_SCRATCH. The table is written by kernels that carry it as their
+ * launch parameter, so no host buffer outlives the call. The first call on a
+ * device looks up the array's device address and keeps it for the process;
+ * make that first call before any stream capture, and do not use the entry
+ * point after cudaDeviceReset on that device. All calls share the array and
+ * each call rewrites what it uses, so calls whose GPU work overlaps (other
+ * streams, other threads) race: serialize them. */
 int fmm_gpu_split_dgemm_noalloc(const fmm_t* fmm, int levels,
                                 int64_t m, int64_t n, int64_t k,
                                 double alpha, const double* A, int64_t lda,

@@ -1,13 +1,14 @@
 """The allocation-free split entry point (fmm_gpu_split_dgemm_noalloc).
 
-It exists for callers that cannot allocate device memory while they run:
-code being captured into a CUDA graph, stream callbacks, plug-ins working in
-memory a host application owns, processes whose device memory is already
-reserved. Instead of a caller workspace it uses the library's static 64 MiB
-device scratch. These tests call it through the C ABI and require the same
-bits as the workspace entry point, on two calls in a row (the scratch keeps
-the previous call's contents, so the second call checks that nothing stale
-leaks into its result)."""
+It exists for callers that cannot allocate device memory while they run: a
+plug-in working in memory that its host application's allocator owns, a
+process whose device memory is already reserved, a loop that cannot afford
+cudaFree's implicit device synchronization. Instead of a caller workspace it
+uses the library's static 64 MiB device scratch. These tests call it through
+the C ABI and require the same bits as the workspace entry point, on two calls
+in a row (the scratch keeps the previous call's contents, so the second call
+checks that nothing stale leaks into its result), and require the device's
+free memory to be the same before and after calls."""
 import ctypes
 
 import numpy as np
@@ -64,4 +65,24 @@ def test_noalloc_rejects_problems_beyond_the_scratch(fmm, torch_cuda):
     A = torch.zeros((n, n), dtype=torch.float64, device="cuda").t()
     C = torch.zeros((n, n), dtype=torch.float64, device="cuda").t()
     assert call_noalloc(fmm, None, 0, A, A, C, 6) == FMM_ERR_SCRATCH
+    assert fmm.take_device_error() == 0
+
+
+def test_noalloc_leaves_device_memory_unchanged(fmm, torch_cuda):
+    import torch
+    m, n, k = 700, 650, 900
+    A, B, C = rand(m, k, 11), rand(k, n, 12), rand(m, n, 13)
+    dA, dB = to_dev(A), to_dev(B)
+    ref, got = to_dev(C), to_dev(C)
+    fmm.split_dgemm(dA, dB, ref, None, 0, 6)
+    fmm.split_dgemm(dA, dB, ref, None, 0, 6)
+    warm = to_dev(C)
+    assert call_noalloc(fmm, None, 0, dA, dB, warm, 6) == 0   # loads the kernels before the count starts
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(2):
+        assert call_noalloc(fmm, None, 0, dA, dB, got, 6) == 0
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+    assert np.array_equal(to_host(got), to_host(ref))
     assert fmm.take_device_error() == 0
