@@ -134,6 +134,36 @@ extern "C" int fmm_gpu_take_device_error(void)
     return v;
 }
 
+namespace {
+std::mutex g_brent_mu;
+std::vector<std::vector<int>> g_brent_ok;   /* algorithms already verified, serialized */
+}  // namespace
+
+/* The Brent check, once per distinct algorithm of the process (a flat
+ * two-level algorithm has up to 16.7 M equations; calls reuse the verdict). */
+static int brent_checked(const fmm_t* f)
+{
+    const size_t a = (size_t)f->m_tilde * f->k_tilde * f->R, b = (size_t)f->k_tilde * f->n_tilde * f->R,
+                 c = (size_t)f->m_tilde * f->n_tilde * f->R;
+    std::vector<int> key;
+    key.reserve(4 + a + b + c);
+    key.insert(key.end(), {f->m_tilde, f->k_tilde, f->n_tilde, f->R});
+    key.insert(key.end(), f->U, f->U + a);
+    key.insert(key.end(), f->V, f->V + b);
+    key.insert(key.end(), f->W, f->W + c);
+    {
+        std::lock_guard<std::mutex> lk(g_brent_mu);
+        for (const auto& k : g_brent_ok)
+            if (k == key) return FMM_OK;
+    }
+    const int rc = fmm_check_brent(f, nullptr);
+    if (rc == FMM_OK) {
+        std::lock_guard<std::mutex> lk(g_brent_mu);
+        if (g_brent_ok.size() < 64) g_brent_ok.push_back(std::move(key));
+    }
+    return rc;
+}
+
 /* flat <- levels-fold Kronecker power of fmm (levels 0: the classical
  * 1x1x1 algorithm). *owned says whether flat's arrays must be freed. */
 int fmm_flatten(const fmm_t* fmm, int levels, fmm_t* flat, int* owned)
@@ -146,7 +176,7 @@ int fmm_flatten(const fmm_t* fmm, int levels, fmm_t* flat, int* owned)
         return FMM_OK;
     }
     if (!valid_fmm(fmm)) return FMM_ERR_ARG;
-    if (fmm_check_brent(fmm, nullptr) != FMM_OK) return FMM_ERR_BRENT;
+    if (brent_checked(fmm) != FMM_OK) return FMM_ERR_BRENT;
     if (levels == 1) {
         *flat = *fmm;
         return FMM_OK;
