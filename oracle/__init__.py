@@ -32,6 +32,18 @@ def build(force: bool = False) -> Path:
     return LIB
 
 
+def build_ref() -> bool:
+    """Builds the reference itself into oracle/_ref/ (build_ref.sh) where its
+    sources are mounted; returns False, doing nothing, where they are not
+    (the GPU machine). Only the fixture generator runs what it builds."""
+    p = subprocess.run(["bash", str(HERE / "build_ref.sh")], capture_output=True, text=True)
+    if p.returncode == 2:
+        return False
+    if p.returncode != 0:
+        raise RuntimeError("reference build failed:\n" + p.stdout[-4000:] + p.stderr[-4000:])
+    return True
+
+
 def lib() -> ctypes.CDLL:
     global _lib
     if _lib is None:
@@ -47,6 +59,8 @@ def lib() -> ctypes.CDLL:
                                              i64, dbl, vp, i64, ci]
         L.oracle_split_fmm_dgemm_fmt.restype = ci
         L.oracle_split_fmm_dgemm_fmt.argtypes = L.oracle_split_fmm_dgemm.argtypes + [ci]
+        L.oracle_split_fmm_dgemm_rows.restype = ci
+        L.oracle_split_fmm_dgemm_rows.argtypes = L.oracle_split_fmm_dgemm_fmt.argtypes + [vp, i64]
         L.oracle_dgemm.restype = None
         L.oracle_dgemm.argtypes = [i64, i64, i64, dbl, vp, i64, vp, i64, dbl, vp, i64]
         L.oracle_naive_dgemm.restype = None
@@ -101,6 +115,38 @@ def split_fmm_dgemm(alg, A, B, C, slices, alpha=1.0, beta=1.0, fmt="bf16"):
     if rc != 0:
         raise ValueError("oracle_split_fmm_dgemm: unsupported size or allocation failure")
     return C
+
+
+def split_fmm_dgemm_rows(alg, A, B, C, slices, rows, alpha=1.0, beta=1.0, fmt="bf16"):
+    """split_fmm_dgemm restricted to the listed rows i of the product grid
+    (0 <= i < ceil(m/m~)): C rows part_offset + i of every C part row get
+    exactly the values the full call gives them; other rows get only beta's
+    scaling. For checking large problems on a few rows."""
+    A, B, C = _f64(A), _f64(B), _f64(C)
+    m, k = A.shape
+    n = B.shape[1]
+    args, keep = _alg(alg)
+    rows = np.ascontiguousarray(rows, dtype=np.int64)
+    rc = lib().oracle_split_fmm_dgemm_rows(*args, m, n, k, alpha, A.ctypes.data, max(m, 1), B.ctypes.data,
+                                           max(k, 1), beta, C.ctypes.data, max(m, 1), slices,
+                                           {"bf16": 0, "fp8": 1}[fmt], rows.ctypes.data, len(rows))
+    if rc != 0:
+        raise ValueError("oracle_split_fmm_dgemm_rows: bad rows, unsupported size or allocation failure")
+    return C
+
+
+def part_rows(d, t, i):
+    """Rows (or columns) of a d-long dimension split t ways that local index i
+    of the product grid lands on: offset of part p plus i, for every part p
+    long enough (frame/base/bli_strassen_ab.c:86-121)."""
+    q, r = divmod(d, t)
+    out, off = [], 0
+    for p in range(t):
+        ln = q + (1 if p < r else 0)
+        if i < ln:
+            out.append(off + i)
+        off += ln
+    return out
 
 
 def dgemm(A, B, C, alpha=1.0, beta=1.0):

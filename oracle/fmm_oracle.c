@@ -255,12 +255,17 @@ static double o_scale2(double v, int e)
 
 /* C := beta*C + alpha*A*B through the split form with `s` slices: fmt 0 =
  * BF16 digits (base 256, s = 2..8), fmt 1 = FP8-E4M3 digits (base 32,
- * s = 2..12). Returns 0, or -1 on allocation failure / unsupported size. */
-int oracle_split_fmm_dgemm_fmt(int mt, int kt, int nt, int R,
-                               const int* U, const int* V, const int* W,
-                               int64_t m, int64_t n, int64_t k, double alpha,
-                               const double* A, int64_t lda, const double* B, int64_t ldb,
-                               double beta, double* C, int64_t ldc, int s, int fmt)
+ * s = 2..12). With a row list, only the listed rows i of the product grid
+ * (0 <= i < ceil(m/m~)) are computed: C rows ro_p + i of every C part row p
+ * get their final values, the other rows only beta's scaling; the arithmetic
+ * of every computed element is the same as without the list (rows do not
+ * interact). Returns 0, or -1 on allocation failure / unsupported size. */
+static int split_core(int mt, int kt, int nt, int R,
+                      const int* U, const int* V, const int* W,
+                      int64_t m, int64_t n, int64_t k, double alpha,
+                      const double* A, int64_t lda, const double* B, int64_t ldb,
+                      double beta, double* C, int64_t ldc, int s, int fmt,
+                      const int64_t* rows, int64_t nrows)
 {
     if (beta != 1.0)
         for (int64_t j = 0; j < n; ++j)
@@ -270,8 +275,13 @@ int oracle_split_fmm_dgemm_fmt(int mt, int kt, int nt, int R,
     if (fmt != 0 && fmt != 1) return -1;
     const int db = fmt ? 5 : 8;               /* digit bits */
     if (s < 2 || s > (fmt ? 12 : 8)) return -1;
-    const int64_t me = (m + mt - 1) / mt, ke = (k + kt - 1) / kt, ne = (n + nt - 1) / nt;
+    const int64_t me_all = (m + mt - 1) / mt, ke = (k + kt - 1) / kt, ne = (n + nt - 1) / nt;
     if (ke > 16384) return -1;
+    if (rows)
+        for (int64_t x = 0; x < nrows; ++x)
+            if (rows[x] < 0 || rows[x] >= me_all) return -1;
+    const int64_t me = rows ? nrows : me_all;   /* rows held; row x is grid row ROW(x) */
+#define ROW(x) (rows ? rows[(x)] : (x))
     double* amax = (double*)calloc((size_t)(kt * m), sizeof(double));
     double* bmax = (double*)calloc((size_t)(kt * n), sizeof(double));
     int* Er = (int*)malloc(sizeof(int) * (size_t)me);
@@ -308,7 +318,8 @@ int oracle_split_fmm_dgemm_fmt(int mt, int kt, int nt, int R,
         for (int p = 0; p < mt * nt; ++p) any_w |= W[(size_t)p * R + r] != 0;
         if (!any_w) continue;
         /* exponents from the FP64 bounds, in part order */
-        for (int64_t i = 0; i < me; ++i) {
+        for (int64_t x = 0; x < me; ++x) {
+            const int64_t i = ROW(x);
             double bnd = 0.0;
             int first = 1;
             for (int q = 0; q < mt * kt; ++q) {
@@ -321,7 +332,7 @@ int oracle_split_fmm_dgemm_fmt(int mt, int kt, int nt, int R,
                 bnd = first ? ac * mx : fma(ac, mx, bnd);
                 first = 0;
             }
-            Er[i] = o_exp_above(bnd);
+            Er[x] = o_exp_above(bnd);
         }
         for (int64_t j = 0; j < ne; ++j) {
             double bnd = 0.0;
@@ -339,8 +350,10 @@ int oracle_split_fmm_dgemm_fmt(int mt, int kt, int nt, int R,
             Fc[j] = o_exp_above(bnd);
         }
         /* operand sums: first nonzero coefficient times its element, then fma */
+#pragma omp parallel for schedule(static)
         for (int64_t p = 0; p < ke; ++p)
-            for (int64_t i = 0; i < me; ++i) {
+            for (int64_t x = 0; x < me; ++x) {
+                const int64_t i = ROW(x);
                 double sum = 0.0;
                 int first = 1;
                 for (int q = 0; q < mt * kt; ++q) {
@@ -353,8 +366,9 @@ int oracle_split_fmm_dgemm_fmt(int mt, int kt, int nt, int R,
                     sum = first ? (double)c * v : fma((double)c, v, sum);
                     first = 0;
                 }
-                S[i + p * me] = sum;
+                S[x + p * me] = sum;
             }
+#pragma omp parallel for schedule(static)
         for (int64_t j = 0; j < ne; ++j)
             for (int64_t p = 0; p < ke; ++p) {
                 double sum = 0.0;
@@ -372,12 +386,14 @@ int oracle_split_fmm_dgemm_fmt(int mt, int kt, int nt, int R,
                 T[p + j * ke] = sum;
             }
         /* digits */
+#pragma omp parallel for schedule(static)
         for (int64_t p = 0; p < ke; ++p)
             for (int64_t i = 0; i < me; ++i) {
                 int d[12];
                 o_split_digits(S[i + p * me], Er[i], s, db, d);
                 for (int t = 0; t < s; ++t) DA[((size_t)t * ke + p) * me + i] = (int16_t)d[t];
             }
+#pragma omp parallel for schedule(static)
         for (int64_t j = 0; j < ne; ++j)
             for (int64_t p = 0; p < ke; ++p) {
                 int d[12];
@@ -421,15 +437,39 @@ int oracle_split_fmm_dgemm_fmt(int mt, int kt, int nt, int R,
             part_geom(n, nt, p % nt, &co, &cl);
             double lam = alpha * (double)w;
             for (int64_t j = 0; j < cl; ++j)
-                for (int64_t i = 0; i < rl; ++i) {
-                    double v = o_scale2((double)Z[i + j * me], Er[i] + Fc[j] + 2 - db * G);
+                for (int64_t x = 0; x < me; ++x) {
+                    const int64_t i = ROW(x);
+                    if (i >= rl) continue;
+                    double v = o_scale2((double)Z[x + j * me], Er[x] + Fc[j] + 2 - db * G);
                     double* c = C + ro + i + (co + j) * ldc;
                     *c = fma(lam, v, *c);
                 }
         }
     }
+#undef ROW
     free(amax); free(bmax); free(Er); free(Fc); free(S); free(T); free(DA); free(DB); free(Z);
     return 0;
+}
+
+int oracle_split_fmm_dgemm_fmt(int mt, int kt, int nt, int R,
+                               const int* U, const int* V, const int* W,
+                               int64_t m, int64_t n, int64_t k, double alpha,
+                               const double* A, int64_t lda, const double* B, int64_t ldb,
+                               double beta, double* C, int64_t ldc, int s, int fmt)
+{
+    return split_core(mt, kt, nt, R, U, V, W, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, s, fmt, NULL, 0);
+}
+
+/* The split form on the listed rows of the product grid only (see split_core). */
+int oracle_split_fmm_dgemm_rows(int mt, int kt, int nt, int R,
+                                const int* U, const int* V, const int* W,
+                                int64_t m, int64_t n, int64_t k, double alpha,
+                                const double* A, int64_t lda, const double* B, int64_t ldb,
+                                double beta, double* C, int64_t ldc, int s, int fmt,
+                                const int64_t* rows, int64_t nrows)
+{
+    if (rows == NULL || nrows <= 0) return -1;
+    return split_core(mt, kt, nt, R, U, V, W, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, s, fmt, rows, nrows);
 }
 
 /* BF16 split form (fmt 0) */

@@ -12,6 +12,12 @@ if str(ROOT) not in sys.path:
 
 ALGS = ["222", "232", "322", "333", "444"]
 
+# c of the plain FP64 form's normwise bound |C - C_other| <= c * eps64 * k * max|A| * max|B| (+ 4 eps max|C0|),
+# per (algorithm, levels): the same bound holds between this library's GPU FP64 form, the oracle and the
+# reference's own bli_strassen_ab_ex (tests/golden/ref/), which differ only in the order of their k-sums.
+C_BOUND = {("222", 1): 4, ("232", 1): 4, ("322", 1): 4, ("333", 1): 8, ("444", 1): 8,
+           ("222", 2): 8, ("232", 2): 8, ("322", 2): 8, ("333", 2): 16, ("444", 2): 16}
+
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (sm_103a); run with -m gpu")

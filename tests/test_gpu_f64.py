@@ -1,18 +1,15 @@
 """Plain FP64 form on the GPU against the oracle (same algorithm, same inputs).
 
 Bound: max|C_gpu - C_oracle| <= c * eps64 * k * max|A| * max|B| (+ 4 eps max|C0|),
-with c per (algorithm, levels) from C_BOUND below. The two sides differ only in
+with c per (algorithm, levels) from conftest.C_BOUND. The two sides differ only in
 the order of the k-sums of each product, so c stays small."""
 import numpy as np
 import pytest
 
-from conftest import ALGS, COEFFS, GOLDEN, fmm_bound, rand
+from conftest import ALGS, C_BOUND, COEFFS, GOLDEN, fmm_bound, rand
 from gpu_util import to_dev, to_host
 
 pytestmark = pytest.mark.gpu
-
-C_BOUND = {("222", 1): 4, ("232", 1): 4, ("322", 1): 4, ("333", 1): 8, ("444", 1): 8,
-           ("222", 2): 8, ("232", 2): 8, ("322", 2): 8, ("333", 2): 16, ("444", 2): 16}
 
 SHAPES = [(1, 1, 1), (3, 13, 7), (17, 9, 23), (64, 64, 64), (130, 67, 95), (257, 129, 300)]
 

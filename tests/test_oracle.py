@@ -161,3 +161,24 @@ def test_split_restatement_wide_range_inputs(orc, algs):
         want = split_fmm(algs["222"], A, B, C, s, 1.0, 1.0, fmt)
         got = orc.split_fmm_dgemm(algs["222"], A, B, C.copy(order="F"), s, fmt=fmt)
         assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("alg,levels,shape,s,fmt", [("222", 2, (130, 95, 77), 6, "bf16"),
+                                                    ("333", 1, (100, 64, 81), 5, "bf16"),
+                                                    ("444", 1, (70, 90, 66), 10, "fp8")])
+def test_split_rows_mode_equals_full(orc, algs, alg, levels, shape, s, fmt):
+    """The oracle's row-subset mode (used to check the GPU at sizes where the
+    full restatement would take too long) gives the listed rows exactly the
+    full call's bits and touches no other row beyond beta's scaling."""
+    from oracle import coeffs as oc
+    m, n, k = shape
+    a = oc.power(algs[alg], levels)
+    A, B, C = rand(m, k, 71), rand(k, n, 72), rand(m, n, 73)
+    full = orc.split_fmm_dgemm(a, A, B, C.copy(order="F"), s, alpha=0.75, beta=1.5, fmt=fmt)
+    me = -(-m // a[0])
+    local = [0, me // 2, me - 1]
+    part = orc.split_fmm_dgemm_rows(a, A, B, C.copy(order="F"), s, local, alpha=0.75, beta=1.5, fmt=fmt)
+    rows = sorted({r for i in local for r in orc.part_rows(m, a[0], i)})
+    assert rows and np.array_equal(part[rows], full[rows])
+    other = np.setdiff1d(np.arange(m), rows)
+    assert np.array_equal(part[other], 1.5 * C[other])
