@@ -36,6 +36,7 @@ from pathlib import Path
 import numpy as np
 
 ROOT = Path(__file__).resolve().parent
+COEFFS = ROOT / "fmm_blis_gb300" / "coeffs"     # the algorithms shipped with the package
 sys.path.insert(0, str(ROOT))
 # many differently sized request buffers (served workload): grow segments
 # instead of fragmenting fixed ones
@@ -178,7 +179,7 @@ def cpu_reference(alg, levels, n, target_s, arrays=None):
     import oracle
     from oracle import coeffs as oc
 
-    flat = oc.power(oc.read(ROOT / "tests" / "golden" / "coeffs" / f"{alg}.txt"), levels)
+    flat = oc.power(oc.read(COEFFS / f"{alg}.txt"), levels)
     R = flat[3]
     oracle.set_threads(os.cpu_count() or 1)
     A, B, C = arrays if arrays is not None else host_operands(n)
@@ -295,7 +296,7 @@ def run_sweep(args, fmm, dev, rank):
 
     shapes = [(n, n, n) for n in (4096, 8192, 12288, 16384)] + [(16384, 16384, 4096), (8192, 8192, 16384)]
     rows = []
-    algs = {a: fmm.new_fmm(ROOT / "tests" / "golden" / "coeffs" / f"{a}.txt") for a in ("232", "322", "333", "444")}
+    algs = {a: fmm.new_fmm(COEFFS / f"{a}.txt") for a in ("232", "322", "333", "444")}
     for (m, n, k) in shapes:
         A = _dev_operand(torch, m, k, 11, dev)
         B = _dev_operand(torch, k, n, 12, dev)
@@ -340,8 +341,8 @@ def run_accuracy(args, fmm, dev, rank):
     relative Frobenius; the plain FP64 FMM's error beside them."""
     import torch
 
-    algs = {"222": (fmm.new_fmm(ROOT / "tests" / "golden" / "coeffs" / "222.txt"), 2),
-            "333": (fmm.new_fmm(ROOT / "tests" / "golden" / "coeffs" / "333.txt"), 1)}
+    algs = {"222": (fmm.new_fmm(COEFFS / "222.txt"), 2),
+            "333": (fmm.new_fmm(COEFFS / "333.txt"), 1)}
     rows = []
     for n in (8192, 16384):
         for dist, phi in (("uniform", None), ("hard_phi1", 1.0), ("hard_phi4", 4.0)):
@@ -403,7 +404,7 @@ def run_batch(args, fmm, dev, world, rank, barrier, max_over_ranks):
         if name == "classical":
             return None
         if name not in algs:
-            algs[name] = fmm.new_fmm(tune.COEFF_DIR / f"{name}.txt")
+            algs[name] = fmm.new_fmm(COEFFS / f"{name}.txt")
         return algs[name]
 
     g = torch.Generator(device=dev).manual_seed(77 + rank)
@@ -564,8 +565,9 @@ def run_fp64(args, fmm, f, dev, world, rank, barrier, max_over_ranks):
     mt, kt, nt, R = f.m_tilde ** levels, f.k_tilde ** levels, f.n_tilde ** levels, f.R ** levels
     executed = 2.0 * (-(-n // mt)) * (-(-n // nt)) * (-(-n // kt)) * R
     clk_sum = clk.summary()
-    sm_max = clk_sum.get("sm_max_mhz") or 2070.0
-    peak = 2.0 * 2.0 * 152 * sm_max * 1e6 / 1e12      # 2 FMA/clk/SM, 2 flops per FMA
+    # the FP64 pipe's measured peak on this GPU: a compute-only DFMA kernel over every SM (and the FP64 MMA path beside it)
+    dfma_peak, dmma_peak = fmm.fp64_pipe_rates()
+    peak = dfma_peak
     achieved = executed / (ms / 1e3) / 1e12
     extra = {}
     if rank == 0 and not args.no_fp64:
@@ -598,8 +600,10 @@ def run_fp64(args, fmm, f, dev, world, rank, barrier, max_over_ranks):
                        "parallelism": f"replicas x{world}"},
             "roofline": {"bound": "fp64_pipe", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved / peak, "traffic": None, "kernel": "fmm_f64_kernel",
-                         "peak_kind": "nominal DFMA rate, 2 FMA/clk/SM at the max SM clock",
+                         "peak_kind": "measured DFMA peak (compute-only kernel, fmm_gpu_fp64_pipe_rates)",
                          "executed_flops_per_step": executed},
+            "fp64_pipes": {"dfma_tflops": dfma_peak, "dmma_tflops": dmma_peak,
+                           "sms": torch.cuda.get_device_properties(dev).multi_processor_count},
             "cpu_baseline": None, "e2e": None, "gpu_launches": launches, "clocks": clk_sum, **extra}))
 
 
@@ -623,7 +627,7 @@ def main():
     fbuild.build()
     dev = torch.device("cuda", torch.cuda.current_device())
     n, levels, s = args.n, args.levels, args.slices
-    f = fmm.new_fmm(ROOT / "tests" / "golden" / "coeffs" / f"{args.alg}.txt")
+    f = fmm.new_fmm(COEFFS / f"{args.alg}.txt")
     flops = 2.0 * n ** 3
 
     def barrier():

@@ -133,6 +133,8 @@ def lib() -> ctypes.CDLL:
     L.fmm_gpu_batch_workspace_size.argtypes = [ci, ctypes.POINTER(BatchProblem)]
     L.fmm_gpu_batch_dgemm.restype = ci
     L.fmm_gpu_batch_dgemm.argtypes = [ci, ctypes.POINTER(BatchProblem), vp, ctypes.c_size_t, vp]
+    L.fmm_gpu_fp64_pipe_rates.restype = ci
+    L.fmm_gpu_fp64_pipe_rates.argtypes = [ctypes.POINTER(dbl), ctypes.POINTER(dbl)]
     L.fmm_gpu_split_dgemm_noalloc.restype = ci
     L.fmm_gpu_split_dgemm_noalloc.argtypes = [pf, ci, i64, i64, i64, dbl, vp, i64, vp, i64, dbl, vp, i64, ci, vp]
     L.fmm_gpu_set_kernel_timing.restype = None
@@ -211,6 +213,13 @@ def read_kernel_timing() -> tuple[float, int, int]:
     _check(lib().fmm_gpu_read_kernel_timing(ctypes.byref(ms), ctypes.byref(n), ctypes.byref(p)),
            "read_kernel_timing")
     return ms.value, int(n.value), int(p.value)
+
+
+def fp64_pipe_rates() -> tuple[float, float]:
+    """(DFMA, FP64 MMA) peak TFLOP/s measured on the current GPU."""
+    a, b = ctypes.c_double(), ctypes.c_double()
+    _check(lib().fmm_gpu_fp64_pipe_rates(ctypes.byref(a), ctypes.byref(b)), "fmm_gpu_fp64_pipe_rates")
+    return a.value, b.value
 
 
 def take_device_error() -> int:

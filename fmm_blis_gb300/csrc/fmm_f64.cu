@@ -587,3 +587,90 @@ int fmm_f64_batch_launch(int count, const F64BatchItem* items, void* ws, size_t 
     fmm_count_launch(1);
     return cudaGetLastError() == cudaSuccess ? FMM_OK : FMM_ERR_CUDA;
 }
+
+/* ---------------------------------------------------------------------------
+ * Peak rates of the two FP64 paths of the SM, measured by compute-only
+ * kernels (no memory traffic inside the loop): DFMA (fma.rn.f64, the plain
+ * form's micro-kernel) and the FP64 tensor-core MMA (mma.sync m8n8k4 f64).
+ * Each thread (DFMA) or warp (MMA) runs independent accumulation chains, so
+ * the issue rate, not a dependency, bounds the loop.
+ * ------------------------------------------------------------------------- */
+namespace {
+
+constexpr int kRateChains = 8;
+
+__global__ void __launch_bounds__(256) dfma_rate_kernel(double* __restrict__ out, int iters)
+{
+    double a[kRateChains];
+#pragma unroll
+    for (int u = 0; u < kRateChains; ++u) a[u] = 1e-3 * (threadIdx.x + u);
+    const double b = 0.999999, c = 1e-9;
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int u = 0; u < kRateChains; ++u) a[u] = fma(a[u], b, c);
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int u = 0; u < kRateChains; ++u) s += a[u];
+    out[blockIdx.x * (int64_t)blockDim.x + threadIdx.x] = s;
+}
+
+__global__ void __launch_bounds__(256) dmma_rate_kernel(double* __restrict__ out, int iters)
+{
+    const int lane = threadIdx.x % 32;
+    const double a = 1e-3 * (lane + 1), b = 0.5;
+    double d[kRateChains][2];
+#pragma unroll
+    for (int u = 0; u < kRateChains; ++u) { d[u][0] = 0.0; d[u][1] = 0.0; }
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int u = 0; u < kRateChains; ++u)
+            asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0, %1}, {%2}, {%3}, {%0, %1};"
+                         : "+d"(d[u][0]), "+d"(d[u][1])
+                         : "d"(a), "d"(b));
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int u = 0; u < kRateChains; ++u) s += d[u][0] + d[u][1];
+    out[blockIdx.x * (int64_t)blockDim.x + threadIdx.x] = s;
+}
+
+}  // namespace
+
+extern "C" int fmm_gpu_fp64_pipe_rates(double* dfma_tflops, double* dmma_tflops)
+{
+    if (dfma_tflops == nullptr || dmma_tflops == nullptr) return FMM_ERR_ARG;
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
+        return FMM_ERR_CUDA;
+    const int blocks = 8 * sms, threads = 256, iters = 4096;
+    double* out = nullptr;
+    if (cudaMalloc(&out, sizeof(double) * (size_t)blocks * threads) != cudaSuccess) return FMM_ERR_ALLOC;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    int rc = FMM_OK;
+    float ms[2] = {0.f, 0.f};
+    for (int which = 0; which < 2 && rc == FMM_OK; ++which) {
+        for (int rep = 0; rep < 3; ++rep) {   /* the first launch warms up */
+            cudaEventRecord(e0);
+            if (which == 0) dfma_rate_kernel<<<blocks, threads>>>(out, iters);
+            else dmma_rate_kernel<<<blocks, threads>>>(out, iters);
+            cudaEventRecord(e1);
+            fmm_count_launch(1);
+            if (cudaEventSynchronize(e1) != cudaSuccess || cudaGetLastError() != cudaSuccess) { rc = FMM_ERR_CUDA; break; }
+            float t = 0.f;
+            cudaEventElapsedTime(&t, e0, e1);
+            if (rep > 0 && (ms[which] == 0.f || t < ms[which])) ms[which] = t;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    if (rc != FMM_OK) return rc;
+    const double threads_total = (double)blocks * threads;
+    *dfma_tflops = threads_total * iters * kRateChains * 2.0 / (ms[0] * 1e-3) / 1e12;
+    *dmma_tflops = threads_total / 32.0 * iters * kRateChains * (2.0 * 8 * 8 * 4) / (ms[1] * 1e-3) / 1e12;
+    return FMM_OK;
+}

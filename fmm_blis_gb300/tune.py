@@ -41,7 +41,7 @@ import math
 from dataclasses import dataclass, field
 from pathlib import Path
 
-COEFF_DIR = Path(__file__).resolve().parent.parent / "tests" / "golden" / "coeffs"
+COEFF_DIR = Path(__file__).resolve().parent / "coeffs"   # the algorithms shipped with the package
 
 SMS = 152
 CLOCK_HZ = 2.07e9

@@ -112,3 +112,15 @@ def test_bl_clock_monotonic(fmm):
     a = fmm.bl_clock()
     b = fmm.bl_clock()
     assert b >= a >= 0.0
+
+
+def test_package_ships_the_reference_coefficient_files():
+    """The algorithms the package and its tuner load (fmm_blis_gb300/coeffs/)
+    are the reference's files byte for byte (the pinned fixtures)."""
+    import hashlib
+    import json
+    from conftest import ROOT
+    man = json.loads((GOLDEN / "manifest.json").read_text())
+    for a in ALGS:
+        data = (ROOT / "fmm_blis_gb300" / "coeffs" / f"{a}.txt").read_bytes()
+        assert hashlib.sha256(data).hexdigest() == man[a]["sha256"]
