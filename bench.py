@@ -60,6 +60,8 @@ def parse():
     p.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison runs")
     p.add_argument("--no-cpu", action="store_true", help="skip the host-core baseline")
     p.add_argument("--e2e-steps", type=int, default=3)
+    p.add_argument("--serve-seconds", type=float, default=10.0,
+                   help="default workload: seconds of the bounded served stream (Poisson 200/s); 0 skips it")
     p.add_argument("--form", choices=["split", "fp64"], default="split",
                    help="split: split-BF16 FMM (the headline); fp64: the plain FP64 FMM drop-in")
     p.add_argument("--workload", choices=["fmm", "batch", "serve", "sweep", "accuracy"], default="fmm",
@@ -478,60 +480,100 @@ def run_batch(args, fmm, dev, world, rank, barrier, max_over_ranks):
             "clocks": sp["clocks"]}))
 
 
-def run_serve(args, fmm, dev, world, rank, barrier, max_over_ranks):
-    """Served GEMM stream: Poisson arrivals at --rate per second for
-    --duration seconds, m, n, k log-uniform in [128, 16384] (scaled down to fit
-    HBM), each tagged split-BF16 at --target (share --split-fraction) or FP64
-    drop-in, served by the continuous-batching Server with HBM admission.
-    Latency = completion - arrival; throughput = completed 2mnk over the
-    window. Requests still running at the end of the drain are counted."""
-    import torch
+def copy_rates(torch, h_src, d_dst, h_dst, d_src, reps=3):
+    """Host-link throughput with the caller's pinned buffers: best of `reps`
+    host-to-device copies of h_src into d_dst and device-to-host copies of
+    d_src into h_dst, timed with CUDA events on a side stream (GB/s)."""
+    st = torch.cuda.Stream()
+    nbytes = h_src.numel() * h_src.element_size()
+    best = {"h2d": float("inf"), "d2h": float("inf")}
+    for _ in range(reps):
+        for kind, dst, src in (("h2d", d_dst, h_src), ("d2h", h_dst, d_src)):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(st):
+                e0.record()
+                dst.copy_(src, non_blocking=True)
+                e1.record()
+            e1.synchronize()
+            best[kind] = min(best[kind], e0.elapsed_time(e1))
+    return {"h2d_gbs": nbytes / best["h2d"] / 1e6, "d2h_gbs": nbytes / best["d2h"] / 1e6}
 
+
+def serve_window(torch, dev, rate, duration, split_fraction, target, seed, clocks=True):
+    """Poisson arrivals at `rate` per second for `duration` seconds, m, n, k
+    log-uniform in [128, 16384] (scaled down to fit HBM), each tagged
+    split-BF16 at `target` (share split_fraction) or FP64 drop-in, served by
+    the continuous-batching Server (per-form queues, HBM admission).
+    Latency = completion - arrival; throughput = 2mnk of the requests that
+    completed inside the window, over the window. Requests still unfinished
+    at the end of the drain (2 x duration) count with their elapsed time."""
     from fmm_blis_gb300 import serve
 
     free, total = torch.cuda.mem_get_info(dev)
     srv = serve.Server(hbm_budget=int(free * 0.75), streams=4, max_batch=64, keep_results=False)
-    reqs = serve.poisson_arrivals(args.rate, args.duration, seed=31 + rank, split_fraction=args.split_fraction,
-                                  target_rel_err=args.target, cap_bytes=int(free * 0.1))
+    reqs = serve.poisson_arrivals(rate, duration, seed=seed, split_fraction=split_fraction,
+                                  target_rel_err=target, cap_bytes=int(free * 0.1))
     # warm-up: one request of each form and a small graph bucket
-    srv.run([serve.Request(1024, 1024, 1024, "split", args.target, 1, 0.0),
-             serve.Request(256, 256, 256, "split", args.target, 2, 0.0),
-             serve.Request(1024, 1024, 1024, "fp64", args.target, 3, 0.0)])
+    srv.run([serve.Request(1024, 1024, 1024, "split", target, 1, 0.0),
+             serve.Request(256, 256, 256, "split", target, 2, 0.0),
+             serve.Request(1024, 1024, 1024, "fp64", target, 3, 0.0)])
     srv.completed.clear()
-    barrier()
-    with Clocks(torch.cuda.current_device()) as clk:
-        t0 = time.perf_counter()
-        srv.run(reqs, until_idle=True, max_s=args.duration * 2)
-        t_end = time.perf_counter()
+    clk = Clocks(torch.cuda.current_device()) if clocks else None
+    if clk:
+        clk.__enter__()
+    t0 = time.perf_counter()
+    srv.run(reqs, until_idle=True, max_s=duration * 2)
+    t_end = time.perf_counter()
+    if clk:
+        clk.__exit__(None, None, None)
     done = [r for r in reqs if r.done is not None]
     lat = sorted(r.latency * 1e3 for r in done)
-    # requests not finished by the end count with their elapsed time (a lower bound)
     open_lat = sorted((t_end - r.arrival) * 1e3 for r in reqs if r.done is None and r.rid >= 0)
     lat_all = sorted(lat + open_lat)
-    window = max(t_end - t0, 1e-9)
-    flops_done = sum(r.flops for r in done if r.done <= t0 + args.duration)
-    pct = lambda xs, q: xs[min(len(xs) - 1, int(q * len(xs)))] if xs else None
+    flops_done = sum(r.flops for r in done if r.done <= t0 + duration)
+
+    def pct(xs, q):
+        return xs[min(len(xs) - 1, int(q * len(xs)))] if xs else None
+
     by_form = {}
     for form in ("split", "fp64"):
         ls = sorted(r.latency * 1e3 for r in done if r.form == form)
-        by_form[form] = {"completed": len(ls), "p50_ms": pct(ls, 0.50), "p99_ms": pct(ls, 0.99)}
-    value = world * flops_done / args.duration / 1e12
+        lo = sorted((t_end - r.arrival) * 1e3 for r in reqs if r.form == form and r.done is None and r.rid >= 0)
+        by_form[form] = {"arrivals": sum(1 for r in reqs if r.form == form), "completed": len(ls),
+                         "p50_ms": pct(sorted(ls + lo), 0.50), "p99_ms": pct(sorted(ls + lo), 0.99)}
+    out = {"rate_per_s": rate, "duration_s": duration, "split_fraction": split_fraction, "target_rel_err": target,
+           "arrivals": len(reqs), "submitted": sum(1 for r in reqs if r.rid >= 0), "completed": len(done),
+           "unfinished": len(open_lat), "p50_ms": pct(lat_all, 0.50), "p99_ms": pct(lat_all, 0.99),
+           "p50_ms_completed": pct(lat, 0.50), "p99_ms_completed": pct(lat, 0.99),
+           "sustained_tflops": flops_done / duration / 1e12, "by_form": by_form,
+           "graph_path_requests": sum(1 for r in done if r.path == "graph"), "batches": srv.launched_batches,
+           "peak_hbm_gib": srv.peak_used / 2**30, "hbm_budget_gib": srv.budget / 2**30,
+           "fp64_ctas": srv.fp64_ctas, "wall_s": t_end - t0}
+    if clk:
+        out["clocks"] = clk.summary()
     srv.close()
+    return out
+
+
+def run_serve(args, fmm, dev, world, rank, barrier, max_over_ranks):
+    """Served GEMM stream (config 5): serve_window at --rate for --duration,
+    --split-fraction split-tagged at --target, the rest FP64 drop-in."""
+    import torch
+
+    barrier()
+    w = serve_window(torch, dev, args.rate, args.duration, args.split_fraction, args.target, seed=31 + rank)
+    value = world * w["sustained_tflops"]
     if rank == 0:
         print(json.dumps({
             "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": 1, "warmup": 1,
-            "ms_per_step": window * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "ms_per_step": w["wall_s"] * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "bf16+f64", "data": "synthetic",
             "config": {"workload": f"served GEMM stream: Poisson {args.rate:g}/s for {args.duration:g} s, "
                                    f"m,n,k log-uniform [128, 16384], {args.split_fraction:.0%} split-BF16 at "
                                    f"{args.target:g}, the rest FP64 drop-in",
-                       "rate_per_s": args.rate, "duration_s": args.duration, "hbm_budget_gib": srv.budget / 2**30,
+                       "rate_per_s": args.rate, "duration_s": args.duration, "hbm_budget_gib": w["hbm_budget_gib"],
                        "l2": "operands resident per request; no flush", "parallelism": f"replicas x{world}"},
-            "submitted": sum(1 for r in reqs if r.rid >= 0), "arrivals": len(reqs), "completed": len(done),
-            "unfinished": len(open_lat), "p50_ms": pct(lat_all, 0.50), "p99_ms": pct(lat_all, 0.99),
-            "p50_ms_completed": pct(lat, 0.50), "p99_ms_completed": pct(lat, 0.99), "by_form": by_form,
-            "graph_path_requests": sum(1 for r in done if r.path == "graph"), "batches": srv.launched_batches,
-            "peak_hbm_gib": srv.peak_used / 2**30, "wall_s": window, "clocks": clk.summary()}))
+            **{k: v for k, v in w.items() if k not in ("rate_per_s", "duration_s", "hbm_budget_gib")}}))
 
 
 def run_fp64(args, fmm, f, dev, world, rank, barrier, max_over_ranks):
@@ -743,9 +785,19 @@ def main():
                 host_step()
             ms_e2e = (time.perf_counter() - t0) * 1e3 / args.e2e_steps
         fmm.release_host_buffers()
+        # the host link on this machine, with the same pinned buffers: one operand up, C down (CUDA events)
+        link = copy_rates(torch, hA, A, hC, C)
+        op_bytes = n * n * 8
+        up_ab = 2 * op_bytes / link["h2d_gbs"] / 1e6
         e2e = {"value": flops / ms_e2e / 1e9, "unit": "TFLOP/s", "h2d_bytes_per_step": 3 * n * n * 8,
                "d2h_bytes_per_step": n * n * 8, "ms_per_step": ms_e2e,
                "call": "fmm_gpu_split_strassen_ab_ex (host buffers, copies overlapped with the device work)",
+               "link": {**link,
+                        "serial_copies_ms": 3 * op_bytes / link["h2d_gbs"] / 1e6 + op_bytes / link["d2h_gbs"] / 1e6,
+                        "upload_A_B_ms": up_ab,
+                        # the call cannot start the GEMM before A and B are up, nor finish before C's last
+                        # column chunk (1/8 of C) is down
+                        "overlap_floor_ms": up_ab + ms + op_bytes / 8 / link["d2h_gbs"] / 1e6},
                "clocks": clk_e2e.summary()}
 
     extra = {}
@@ -787,6 +839,11 @@ def main():
                "sample": (f"oracle FP64 FMM {args.alg} x{levels} at m=n=k={n}: products 0..{info['products']} "
                           f"of {info['of']} ({info['seconds']:.1f} s), extrapolated")}
 
+    served = None
+    if rank == 0 and args.serve_seconds > 0:
+        # config 5's served stream, bounded: Poisson 200/s for serve_seconds, split-tagged at 1e-10
+        served = serve_window(torch, dev, 200.0, args.serve_seconds, 1.0, 1e-10, seed=31)
+
     assert fmm.take_device_error() == 0
     if rank == 0:
         out = {
@@ -801,6 +858,8 @@ def main():
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
             "clocks": clk.summary(), **extra,
         }
+        if served is not None:
+            out["served"] = served
         print(json.dumps(out))
     if world > 1:
         import torch.distributed as dist

@@ -133,6 +133,10 @@ def lib() -> ctypes.CDLL:
     L.fmm_gpu_batch_workspace_size.argtypes = [ci, ctypes.POINTER(BatchProblem)]
     L.fmm_gpu_batch_dgemm.restype = ci
     L.fmm_gpu_batch_dgemm.argtypes = [ci, ctypes.POINTER(BatchProblem), vp, ctypes.c_size_t, vp]
+    L.fmm_gpu_selftest_wait_expiry.restype = ci
+    L.fmm_gpu_selftest_wait_expiry.argtypes = [ctypes.POINTER(ci)]
+    L.fmm_gpu_set_f64_batch_ctas.restype = ci
+    L.fmm_gpu_set_f64_batch_ctas.argtypes = [ci]
     L.fmm_gpu_fp64_pipe_rates.restype = ci
     L.fmm_gpu_fp64_pipe_rates.argtypes = [ctypes.POINTER(dbl), ctypes.POINTER(dbl)]
     L.fmm_gpu_split_dgemm_noalloc.restype = ci
@@ -222,8 +226,23 @@ def fp64_pipe_rates() -> tuple[float, float]:
     return a.value, b.value
 
 
+def selftest_wait_expiry() -> tuple[int, int]:
+    """Runs the bounded-wait failure path on purpose (a wait nothing
+    completes); returns (status, threads that gave up): (FMM_ERR_DEVICE, 64)
+    when it worked."""
+    g = ctypes.c_int()
+    st = lib().fmm_gpu_selftest_wait_expiry(ctypes.byref(g))
+    return st, g.value
+
+
 def take_device_error() -> int:
     return int(lib().fmm_gpu_take_device_error())
+
+
+def set_f64_batch_ctas(max_ctas: int) -> int:
+    """Caps the CTAs of the FP64 batch launch (0: two per SM); returns the
+    previous cap."""
+    return lib().fmm_gpu_set_f64_batch_ctas(int(max_ctas))
 
 
 def set_split_pair_rows(min_rows: int) -> int:

@@ -125,6 +125,17 @@ int* fmm_device_error_word(void)
     return g_err_ptr[dev];
 }
 
+/* FMM_ERR_DEVICE (and the word cleared) when a kernel recorded an expired
+ * wait, else FMM_OK; for synchronous calls, after their work has finished. */
+int fmm_device_error_status(void)
+{
+    int v = 0, zero = 0;
+    if (cudaMemcpyFromSymbol(&v, g_device_error, sizeof(int)) != cudaSuccess) return FMM_ERR_CUDA;
+    if (v == 0) return FMM_OK;
+    cudaMemcpyToSymbol(g_device_error, &zero, sizeof(int));
+    return FMM_ERR_DEVICE;
+}
+
 extern "C" int fmm_gpu_take_device_error(void)
 {
     int v = 0, zero = 0;
@@ -408,6 +419,7 @@ extern "C" int fmm_gpu_strassen_ab_gen(double alpha, const double* A, int64_t rs
     if (rc == FMM_OK) rc = fmm_gpu_dgemm(&fmm, 1, m, n, k, alpha, dA, m, dB, ka, beta, dC, m, nullptr);
     if (rc == FMM_OK) rc = operand_to_host(dC, m, n, C, rsc, csc, dT);
     if (rc == FMM_OK && cudaDeviceSynchronize() != cudaSuccess) rc = FMM_ERR_CUDA;
+    if (rc == FMM_OK) rc = fmm_device_error_status();
     cudaFree(dA);
     cudaFree(dB);
     cudaFree(dC);
@@ -512,6 +524,7 @@ extern "C" int fmm_gpu_split_strassen_ab_gen(double alpha, const double* A, int6
                                      nullptr);
     if (rc == FMM_OK) rc = operand_to_host(dC, m, n, C, rsc, csc, dT);
     if (rc == FMM_OK && cudaDeviceSynchronize() != cudaSuccess) rc = FMM_ERR_CUDA;
+    if (rc == FMM_OK) rc = fmm_device_error_status();
     cudaGetLastError();
     cudaFree(dA);
     cudaFree(dB);

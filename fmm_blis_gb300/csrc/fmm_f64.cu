@@ -26,6 +26,7 @@
 #include "fmm_internal.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <vector>
 
@@ -534,6 +535,15 @@ size_t fmm_f64_batch_ws_bytes(int count)
  * of their items, largest first. Each result is identical to the problem
  * issued alone through fmm_f64_launch: every tile shape accumulates the
  * packed sums, the k loop and the products in the same order. */
+namespace {
+std::atomic<int> g_f64_batch_ctas{0};   /* 0: two CTAs per SM */
+}  // namespace
+
+extern "C" int fmm_gpu_set_f64_batch_ctas(int max_ctas)
+{
+    return g_f64_batch_ctas.exchange(max_ctas > 0 ? max_ctas : 0);
+}
+
 int fmm_f64_batch_launch(int count, const F64BatchItem* items, void* ws, size_t ws_bytes, cudaStream_t st)
 {
     if (count <= 0) return FMM_OK;
@@ -581,7 +591,9 @@ int fmm_f64_batch_launch(int count, const F64BatchItem* items, void* ws, size_t 
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int64_t grid = std::min<int64_t>(items_total, 2 * (int64_t)sms);
+    int64_t grid = std::min<int64_t>(items_total, 2 * (int64_t)sms);
+    const int cap = g_f64_batch_ctas.load();
+    if (cap > 0) grid = std::min<int64_t>(grid, cap);   /* items are drawn from a counter: any grid finishes them */
     fmm_f64_batch_kernel<<<(unsigned)grid, (kF64Bm / kF64Tm) * (kF64Bn / kF64Tn), 0, st>>>(
         dtab, (int)tab.size(), items_total, counter);
     fmm_count_launch(1);

@@ -62,6 +62,7 @@ int fmm_alg_get(const fmm_t* flat, AlgView* out);  /* upload/cache */
 int fmm_alg_describe(const fmm_t* flat, std::vector<int>* table, AlgView* out);
 void fmm_count_launch(uint64_t n);
 int* fmm_device_error_word(void);                 /* device pointer */
+int fmm_device_error_status(void);                /* FMM_ERR_DEVICE if a wait expired (clears it), else FMM_OK */
 
 /* FP64 form (fmm_f64.cu) */
 int fmm_f64_launch(const AlgView& alg, int64_t m, int64_t n, int64_t k,

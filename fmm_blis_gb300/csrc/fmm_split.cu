@@ -2382,13 +2382,14 @@ int fmm_split_host(const AlgView& alg, int64_t m, int64_t n, int64_t k, double a
             if (!ok(cudaEventRecord(sp->gate[1], cs)) || !ok(cudaStreamSynchronize(cs)) ||
                 !ok(cudaStreamSynchronize(st)))
                 return FMM_ERR_CUDA;
-            return cudaGetLastError() == cudaSuccess ? FMM_OK : FMM_ERR_CUDA;
+            return cudaGetLastError() == cudaSuccess ? fmm_device_error_status() : FMM_ERR_CUDA;
         }
     }
     if (!ok(cudaMemcpy2DAsync(C, sizeof(double) * ldc, dC, row, row, n, cudaMemcpyDeviceToHost, st)) ||
         !ok(cudaStreamSynchronize(st)))
         return FMM_ERR_CUDA;
-    return cudaGetLastError() == cudaSuccess ? FMM_OK : FMM_ERR_CUDA;
+    /* a kernel whose bounded wait expired left C incomplete: report it */
+    return cudaGetLastError() == cudaSuccess ? fmm_device_error_status() : FMM_ERR_CUDA;
 }
 
 void fmm_split_host_release()
@@ -2799,4 +2800,49 @@ extern "C" int fmm_gpu_batch_dgemm(int count, const fmm_batch_problem* probs, vo
     }
     if (jobs.empty()) return FMM_OK;
     return fmm_split_batch((int)jobs.size(), jobs.data(), workspace, workspace_bytes, st);
+}
+
+/* ---------------------------------------------------------------------------
+ * Self-test of the failure path every kernel wait relies on: one CTA waits,
+ * with the library's bounded mbarrier wait (sm103::mbar_wait, the one the GEMM
+ * kernels use), on a barrier that nothing arrives at. After the wait limit it
+ * must record `code` in the device error word, raise the CTA's abort flag so
+ * the other waiting threads give up too, and return; the kernel then ends
+ * normally and the context stays usable.
+ * ------------------------------------------------------------------------- */
+namespace {
+__global__ void __launch_bounds__(64) selftest_wait_kernel(int* err, int code, int* gave_up)
+{
+    __shared__ uint64_t bar;
+    __shared__ volatile int abort_flag;
+    if (threadIdx.x == 0) {
+        sm103::mbar_init(&bar, 1);     /* one arrival expected; none comes */
+        abort_flag = 0;
+        sm103::fence_mbar_init();
+    }
+    __syncthreads();
+    const bool ok = sm103::mbar_wait(&bar, 0, &abort_flag, err, code);
+    if (!ok) atomicAdd(gave_up, 1);
+}
+}  // namespace
+
+extern "C" int fmm_gpu_selftest_wait_expiry(int* threads_gave_up)
+{
+    int* err = fmm_device_error_word();
+    if (err == nullptr) return FMM_ERR_CUDA;
+    int* d_gave = nullptr;
+    if (cudaMalloc(&d_gave, sizeof(int)) != cudaSuccess) return FMM_ERR_ALLOC;
+    int rc = FMM_OK;
+    if (cudaMemset(d_gave, 0, sizeof(int)) != cudaSuccess) rc = FMM_ERR_CUDA;
+    if (rc == FMM_OK) {
+        selftest_wait_kernel<<<1, 64>>>(err, 99, d_gave);
+        fmm_count_launch(1);
+        if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) rc = FMM_ERR_CUDA;
+    }
+    int gave = 0;
+    if (rc == FMM_OK && cudaMemcpy(&gave, d_gave, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) rc = FMM_ERR_CUDA;
+    cudaFree(d_gave);
+    if (threads_gave_up) *threads_gave_up = gave;
+    if (rc != FMM_OK) return rc;
+    return fmm_device_error_status();
 }

@@ -1,6 +1,6 @@
 """Serving loop for GEMM requests on one GPU: continuous batching with
-admission by HBM footprint, batched launches that overlap on a pool of
-streams, and per-size-bucket CUDA graphs for small requests.
+admission by HBM footprint, per-form queues, batched launches that overlap on
+a pool of streams, and per-size-bucket CUDA graphs for small requests.
 
 The reference has no serving layer (its only caller is one synchronous
 bli_strassen_ab_ex call, test/test_strassen_oapi.c:166); this is the served
@@ -10,15 +10,27 @@ form of the same FMM GEMM built on the library's batched C-ABI call
 Loop (Server.tick):
   1. completions: a batch whose event has fired releases its requests'
      device memory (operands stay on the device until the request is done)
-     and their footprint;
-  2. admission: waiting requests, first come first served, are admitted while
-     their footprint -- A, B, C and the FMM workspace of their plan -- fits the
-     HBM budget; a request that does not fit blocks the ones behind it (no
-     overtaking, so large requests are not starved);
-  3. launch: the requests admitted in this tick run as one batch (one
-     persistent launch for the FP64 problems, waves of persistent launches for
-     the split ones) on the next stream of the pool, so the batches of
-     successive ticks overlap on the device while earlier ones run.
+     and their footprint; cancelled requests are dropped here;
+  2. admission, one queue per form, first come first served within a queue:
+     a request is admitted while its footprint -- A, B, C and the FMM
+     workspace of its plan -- fits the HBM budget; FP64-tagged requests may
+     hold at most fp64_hbm_share of the budget, so a backlog of FP64 work
+     (about 50 times slower per flop than the split form on this GPU) never
+     takes the memory split requests need. Within a queue a request that
+     does not fit blocks the ones behind it (no overtaking, so large requests
+     are not starved);
+  3. launch: the split requests admitted in this tick run as one batch on
+     the next stream of the pool, so the batches of successive ticks overlap
+     on the device; the FP64 requests run as one batch on their own stream
+     with the persistent FP64 launch capped at fp64_ctas CTAs
+     (fmm_gpu_set_f64_batch_ctas), which leaves the other SMs to the split
+     form's kernels while a long FP64 batch runs.
+
+Faults are handled on the host: a workspace allocation that fails puts the
+batch's requests back at the front of their queue (operands are regenerated
+from the request's seed when it is launched again) and the loop goes on;
+cancel(rid) withdraws a waiting request, or drops an admitted one's result
+when its batch completes.
 
 A request's result depends only on the request: its plan comes from the
 deterministic Tuner and the batched call gives every problem exactly its
@@ -60,6 +72,7 @@ class Request:
     path: str = ""                    # "batch" or "graph"
     C: object = None                  # result (device tensor, column-major), kept after completion
     footprint: int = 0
+    cancelled: bool = False
     _A: object = field(default=None, repr=False)
     _B: object = field(default=None, repr=False)
 
@@ -112,7 +125,8 @@ class _GraphSlot:
 class Server:
     def __init__(self, hbm_budget: int | None = None, streams: int = 4, tuner: _tune.Tuner | None = None,
                  max_batch: int = 64, graph_max_dim: int = 1024, graph_slots: int = 2, use_graphs: bool = True,
-                 keep_results: bool = True, device: int = 0):
+                 keep_results: bool = True, device: int = 0, fp64_hbm_share: float = 0.25,
+                 fp64_ctas: int | None = None, alloc_hook=None):
         import torch
 
         import fmm_blis_gb300 as fmm
@@ -122,22 +136,38 @@ class Server:
             free, _total = torch.cuda.mem_get_info(self.dev)
             hbm_budget = int(free * 0.8)
         self.budget = hbm_budget
+        self.fp64_budget = int(hbm_budget * fp64_hbm_share)
         self.used = 0
+        self.used_fp64 = 0
         self.peak_used = 0
         self.tuner = tuner or _tune.Tuner()
         self.streams = [torch.cuda.Stream(device=self.dev) for _ in range(streams)]
+        self.fp64_stream = torch.cuda.Stream(device=self.dev)
+        sms = torch.cuda.get_device_properties(self.dev).multi_processor_count
+        # the FP64 batch kernel holds one SM per CTA against the split GEMM (their shared memory does not fit
+        # together): an eighth of the SMs by default
+        self.fp64_ctas = fp64_ctas if fp64_ctas is not None else max(1, sms // 8)
         self._next_stream = itertools.cycle(range(streams))
         self.max_batch = max_batch
         self.keep_results = keep_results
         self.graph_max_dim = graph_max_dim if use_graphs else 0
         self.graph_slots = graph_slots
-        self.pending: collections.deque[Request] = collections.deque()
+        self.queues: dict[str, collections.deque[Request]] = {"split": collections.deque(),
+                                                              "fp64": collections.deque()}
         self.inflight: list[tuple[object, list[Request], object]] = []   # (event, requests, workspace)
         self.completed: list[Request] = []
+        self.cancelled: list[Request] = []
+        self.alloc_hook = alloc_hook          # called before each workspace allocation; may raise (fault injection)
+        self.alloc_failures = 0
         self._algs: dict = {}
         self._slots: dict = {}
         self._rid = itertools.count()
         self.launched_batches = 0
+
+    @property
+    def pending(self):
+        """all waiting requests, split queue first"""
+        return list(self.queues["split"]) + list(self.queues["fp64"])
 
     # ------------------------------------------------------------ helpers
     def _alg(self, name: str):
@@ -169,73 +199,144 @@ class Server:
             r.arrival = time.perf_counter()
         r.plan = self.tuner.plan(r.m, r.n, r.k, r.form, r.target_rel_err)
         r.footprint = 8 * (r.m * r.k + r.k * r.n + r.m * r.n) + self._workspace_bytes(r)
-        if r.footprint > self.budget:
-            raise ValueError(f"request {r.rid} needs {r.footprint} bytes, more than the HBM budget {self.budget}")
-        self.pending.append(r)
+        cap = self.fp64_budget if r.plan.form == "fp64" else self.budget
+        if r.footprint > cap:
+            raise ValueError(f"request {r.rid} needs {r.footprint} bytes, more than its HBM budget {cap}")
+        self.queues[r.plan.form].append(r)
         return r
 
+    def cancel(self, rid: int) -> bool:
+        """Withdraws request rid: a waiting one leaves its queue at once, an
+        admitted one is dropped (memory released, result discarded) when its
+        batch completes. False if it is unknown or already done."""
+        for q in self.queues.values():
+            for r in q:
+                if r.rid == rid:
+                    q.remove(r)
+                    r.cancelled = True
+                    self.cancelled.append(r)
+                    return True
+        for _ev, reqs, _ws in self.inflight:
+            for r in reqs:
+                if r.rid == rid and not r.cancelled:
+                    r.cancelled = True
+                    return True
+        return False
+
     def idle(self) -> bool:
-        return not self.pending and not self.inflight
+        return not any(self.queues.values()) and not self.inflight
+
+    def _admit(self, form: str) -> list[Request]:
+        q, batch = self.queues[form], []
+        while q and len(batch) < self.max_batch:
+            r = q[0]
+            if self.used + r.footprint > self.budget:
+                break
+            if form == "fp64" and self.used_fp64 + r.footprint > self.fp64_budget:
+                break
+            q.popleft()
+            self.used += r.footprint
+            if form == "fp64":
+                self.used_fp64 += r.footprint
+            self.peak_used = max(self.peak_used, self.used)
+            r.admitted = time.perf_counter()
+            batch.append(r)
+        return batch
+
+    def _release(self, r: Request):
+        self.used -= r.footprint
+        if r.plan.form == "fp64":
+            self.used_fp64 -= r.footprint
+        r._A = r._B = None
+
+    def _workspace(self, nbytes: int):
+        if self.alloc_hook is not None:
+            self.alloc_hook(nbytes)
+        return self.torch.empty(max(nbytes, 256), dtype=self.torch.uint8, device=self.dev)
 
     def tick(self) -> int:
         """One scheduling round; returns the number of requests launched."""
-        torch = self.torch
         # 1. completions
         still = []
         now = time.perf_counter()
         for ev, reqs, ws in self.inflight:
             if ev.query():
                 for r in reqs:
+                    self._release(r)
+                    if r.cancelled:
+                        r.C = None
+                        self.cancelled.append(r)
+                        continue
                     r.done = now
-                    r._A = r._B = None
                     if not self.keep_results:
                         r.C = None
-                    self.used -= r.footprint
                     self.completed.append(r)
             else:
                 still.append((ev, reqs, ws))
         self.inflight = still
-        # 2. admission, first come first served
-        batch: list[Request] = []
-        while self.pending and len(batch) < self.max_batch:
-            r = self.pending[0]
-            if self.used + r.footprint > self.budget:
-                break
-            self.pending.popleft()
-            self.used += r.footprint
-            self.peak_used = max(self.peak_used, self.used)
-            r.admitted = time.perf_counter()
-            batch.append(r)
-        if not batch:
-            return 0
-        # 3. launch on the next stream of the pool
-        st = self.streams[next(self._next_stream)]
+        # 2. admission per form, 3. launch
+        launched = 0
+        for form in ("split", "fp64"):
+            batch = self._admit(form)
+            if not batch:
+                continue
+            st = self.fp64_stream if form == "fp64" else self.streams[next(self._next_stream)]
+            try:
+                ev, ws = self._launch(batch, st, form)
+            except (MemoryError, RuntimeError) as e:
+                if not isinstance(e, MemoryError) and "out of memory" not in str(e).lower():
+                    raise
+                # nothing of the batch ran: back to the front of the queue, in order
+                for r in reversed(batch):
+                    self._release(r)
+                    r.C = None
+                    r.admitted = None
+                    self.queues[form].appendleft(r)
+                self.alloc_failures += 1
+                continue
+            self.inflight.append((ev, batch, ws))
+            self.launched_batches += 1
+            launched += len(batch)
+        return launched
+
+    def _launch(self, batch, st, form):
+        """operands, workspace (the one allocation that may fail: nothing has
+        been launched but operand generation when it does), graph requests,
+        then one batched call for the rest"""
+        torch = self.torch
         with torch.cuda.stream(st):
-            direct = []
+            direct, graphs = [], []
             for r in batch:
-                g = torch.Generator(device=self.dev).manual_seed(r.seed)
                 bucket = self._graph_bucket(r)
                 if bucket is not None:
-                    self._run_graph(r, bucket, g, st)
+                    graphs.append((r, bucket))
                     continue
+                g = torch.Generator(device=self.dev).manual_seed(r.seed)
                 r._A = _colmajor_rand(torch, r.m, r.k, g, self.dev)
                 r._B = _colmajor_rand(torch, r.k, r.n, g, self.dev)
                 r.C = _colmajor_rand(torch, r.m, r.n, g, self.dev)
                 r.path = "batch"
                 direct.append(r)
-            ws = None
+            ws, arr = None, None
             if direct:
                 probs = [{"A": r._A, "B": r._B, "C": r.C, "fmm": self._alg(r.plan.alg), "levels": r.plan.levels,
                           "slices": r.plan.slices, "fmt": r.plan.fmt} for r in direct]
                 arr = self.fmm.make_batch(probs)
-                need = self.fmm.batch_workspace_size(arr)
-                ws = torch.empty(max(need, 256), dtype=torch.uint8, device=self.dev)
-                self.fmm.batch_dgemm(arr, workspace=ws, stream=st)
+                ws = self._workspace(self.fmm.batch_workspace_size(arr))
+            for r, bucket in graphs:
+                self._run_graph(r, bucket, torch.Generator(device=self.dev).manual_seed(r.seed), st)
+            if direct:
+                if form == "fp64":
+                    prev = self.fmm.set_f64_batch_ctas(self.fp64_ctas)
+                    try:
+                        self.fmm.batch_dgemm(arr, workspace=ws, stream=st)
+                    finally:
+                        self.fmm.set_f64_batch_ctas(prev)
+                else:
+                    self.fmm.batch_dgemm(arr, workspace=ws, stream=st)
             ev = torch.cuda.Event()
             ev.record(st)
-        self.inflight.append((ev, batch, ws))
-        self.launched_batches += 1
-        return len(batch)
+        return ev, ws
 
     def _run_graph(self, r: Request, bucket, gen, st):
         """operands into a zero-padded slot of the bucket, one graph launch,

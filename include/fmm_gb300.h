@@ -322,6 +322,14 @@ int fmm_gpu_split_dgemm_noalloc(const fmm_t* fmm, int levels,
 void fmm_gpu_set_kernel_timing(int enable);
 int fmm_gpu_read_kernel_timing(double* total_ms, uint64_t* launches, uint64_t* products);
 
+/* Upper bound on the CTAs of the persistent FP64 batch launch of
+ * fmm_gpu_batch_dgemm (0, the default: two per SM). Its work items are drawn
+ * from a counter, so any grid finishes them; a small cap leaves the other SMs
+ * free for work on other streams (a server keeps split-form requests flowing
+ * beside long FP64 batches this way). Results do not depend on it. Returns
+ * the previous value. No counterpart in the reference. */
+int fmm_gpu_set_f64_batch_ctas(int max_ctas);
+
 /* Smallest per-product row count m_e = ceil(m / m~^levels) from which the
  * split form's GEMM runs on CTA pairs (clusters of two SMs, 256 x 256 tiles,
  * tcgen05.mma cta_group::2) instead of one SM per 128 x 256 tile; applies to
@@ -345,6 +353,15 @@ uint64_t fmm_gpu_launch_count(void);
 /* Last device-side error word (0 = none) recorded by a kernel whose bounded
  * wait expired; reading it synchronizes the device. Clears it. */
 int fmm_gpu_take_device_error(void);
+
+/* Self-test of the kernels' failure path: one CTA of 64 threads waits, with
+ * the bounded mbarrier wait the GEMM kernels use, on a barrier nothing
+ * arrives at. The wait gives up after its limit (2 s), records an error code
+ * in the device error word, makes the other threads give up too, and the
+ * kernel ends; the call then reads the word as the synchronous entry points
+ * do. Returns FMM_ERR_DEVICE (word cleared) when the failure path worked,
+ * *threads_gave_up = 64. No counterpart in the reference. */
+int fmm_gpu_selftest_wait_expiry(int* threads_gave_up);
 
 #ifdef __cplusplus
 }

@@ -87,7 +87,8 @@ def test_admission_respects_hbm_budget(fmm, torch_cuda):
     reqs = [serve.Request(900, 800, 700 + 10 * i, form="split", seed=i, arrival=0.0) for i in range(12)]
     probe = serve.Server(streams=2, use_graphs=False)
     one = probe.submit(serve.Request(900, 800, 820, form="split", seed=99)).footprint
-    probe.pending.clear()
+    for q in probe.queues.values():
+        q.clear()
     probe.close()
     srv = serve.Server(hbm_budget=int(2.5 * one), streams=2, use_graphs=False)
     srv.run(reqs)
@@ -121,3 +122,69 @@ def test_split_plans_meet_their_target(fmm, torch_cuda):
     finally:
         for f in algs.values():
             fmm.free_fmm(f)
+
+
+def test_workspace_allocation_failure_is_retried(fmm, torch_cuda):
+    """A workspace allocation that fails (injected on the host) puts the
+    batch back in its queue; the loop goes on and every request completes
+    with the bits it gets without the fault."""
+    torch = torch_cuda
+    tuner = small_tuner()
+    calls = {"n": 0}
+
+    def fail_first_two(nbytes):
+        calls["n"] += 1
+        if calls["n"] <= 2:
+            raise MemoryError(f"injected: workspace of {nbytes} bytes")
+
+    reqs = [serve.Request(600 + 37 * i, 500 + 11 * i, 700 - 13 * i, form="split" if i % 4 else "fp64",
+                          seed=500 + i, arrival=0.0) for i in range(8)]
+    srv = serve.Server(streams=2, tuner=tuner, use_graphs=False, alloc_hook=fail_first_two)
+    srv.run(reqs)
+    srv.close()
+    assert srv.alloc_failures == 2
+    assert len(srv.completed) == len(reqs)
+    algs = {}
+    try:
+        for r in reqs:
+            assert np.array_equal(direct(fmm, torch, r, algs), host(r.C)), (r.m, r.n, r.k, r.form)
+    finally:
+        for f in algs.values():
+            fmm.free_fmm(f)
+    assert fmm.take_device_error() == 0
+
+
+def test_cancelled_requests_leave_the_rest_unchanged(fmm, torch_cuda):
+    torch = torch_cuda
+    tuner = small_tuner()
+    srv = serve.Server(streams=2, tuner=tuner)
+    reqs = [srv.submit(serve.Request(300 + 50 * i, 280, 310, form="split", seed=700 + i)) for i in range(6)]
+    assert srv.cancel(reqs[2].rid)                 # waiting: leaves its queue
+    assert srv.tick() == 5
+    assert srv.cancel(reqs[4].rid)                 # admitted: dropped when its batch completes
+    assert not srv.cancel(10**6)
+    srv.run([])
+    srv.close()
+    assert sorted(r.rid for r in srv.cancelled) == sorted([reqs[2].rid, reqs[4].rid])
+    assert sorted(r.rid for r in srv.completed) == sorted(r.rid for i, r in enumerate(reqs) if i not in (2, 4))
+    assert srv.used == 0 and srv.used_fp64 == 0
+    algs = {}
+    try:
+        for r in srv.completed:
+            assert np.array_equal(direct(fmm, torch, r, algs), host(r.C))
+    finally:
+        for f in algs.values():
+            fmm.free_fmm(f)
+
+
+def test_split_requests_pass_a_long_fp64_batch(fmm, torch_cuda):
+    """Per-form queues and the FP64 batch's CTA cap: split requests that arrive
+    behind a long FP64 request are admitted and finish while it still runs."""
+    srv = serve.Server(streams=2, use_graphs=False)
+    big = serve.Request(4096, 4096, 4096, form="fp64", seed=1, arrival=0.0)
+    small = [serve.Request(700, 650, 720, form="split", seed=10 + i, arrival=0.001 * (i + 1)) for i in range(10)]
+    srv.run([big] + small)
+    srv.close()
+    assert big.done is not None and all(r.done is not None for r in small)
+    assert max(r.done for r in small) < big.done
+    assert fmm.take_device_error() == 0
