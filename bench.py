@@ -343,8 +343,11 @@ def run_accuracy(args, fmm, dev, rank):
     relative Frobenius; the plain FP64 FMM's error beside them."""
     import torch
 
+    from fmm_blis_gb300 import tune
+
     algs = {"222": (fmm.new_fmm(COEFFS / "222.txt"), 2),
             "333": (fmm.new_fmm(COEFFS / "333.txt"), 1)}
+    tuner = tune.Tuner()
     rows = []
     for n in (8192, 16384):
         for dist, phi in (("uniform", None), ("hard_phi1", 1.0), ("hard_phi4", 4.0)):
@@ -354,6 +357,18 @@ def run_accuracy(args, fmm, dev, rank):
             fmm.dgemm(A, B, ref, None, 0)
             torch.cuda.synchronize()
             rmax, rfro = float(ref.abs().max()), float(torch.linalg.norm(ref))
+            # the tuner's input-aware plan for a 1e-10 target, and what it gives
+            p = tuner.plan_for(fmm, A, B, 1e-10)
+            fp = None if p.alg == "classical" else fmm.new_fmm(COEFFS / f"{p.alg}.txt")
+            Ct = torch.zeros_like(ref)
+            fmm.split_dgemm(A, B, Ct, fp, p.levels, p.slices, fmt=p.fmt)
+            torch.cuda.synchronize()
+            tuned = {"plan": {"alg": p.alg, "levels": p.levels, "slices": p.slices, "fmt": p.fmt},
+                     "shape_plan_slices": tuner.plan(n, n, n, "split", 1e-10).slices,
+                     "max_rel": float((Ct - ref).abs().max()) / rmax}
+            del Ct
+            if fp is not None:
+                fmm.free_fmm(fp)
             for name, (f, L) in algs.items():
                 Cf = torch.zeros_like(ref)
                 fmm.dgemm(A, B, Cf, f, L)
@@ -372,7 +387,7 @@ def run_accuracy(args, fmm, dev, rank):
                                               "ratio_to_fp64_fmm": float(d.abs().max()) / e64 if e64 > 0 else None}
                         del Cs, d
                 rows.append({"n": n, "inputs": dist, "alg": name, "levels": L, "fp64_fmm_max_err": e64,
-                             "fp64_fmm_max_rel": e64 / rmax, "split": errs})
+                             "fp64_fmm_max_rel": e64 / rmax, "split": errs, "tuner_1e-10": tuned})
             del A, B, ref
             torch.cuda.empty_cache()
     for f, _ in algs.values():
@@ -608,7 +623,7 @@ def run_fp64(args, fmm, f, dev, world, rank, barrier, max_over_ranks):
     executed = 2.0 * (-(-n // mt)) * (-(-n // nt)) * (-(-n // kt)) * R
     clk_sum = clk.summary()
     # the FP64 pipe's measured peak on this GPU: a compute-only DFMA kernel over every SM (and the FP64 MMA path beside it)
-    dfma_peak, dmma_peak = fmm.fp64_pipe_rates()
+    dfma_peak, dmma_peak, mixed_peak = fmm.fp64_pipe_rates()
     peak = dfma_peak
     achieved = executed / (ms / 1e3) / 1e12
     extra = {}
@@ -644,7 +659,7 @@ def run_fp64(args, fmm, f, dev, world, rank, barrier, max_over_ranks):
                          "frac": achieved / peak, "traffic": None, "kernel": "fmm_f64_kernel",
                          "peak_kind": "measured DFMA peak (compute-only kernel, fmm_gpu_fp64_pipe_rates)",
                          "executed_flops_per_step": executed},
-            "fp64_pipes": {"dfma_tflops": dfma_peak, "dmma_tflops": dmma_peak,
+            "fp64_pipes": {"dfma_tflops": dfma_peak, "dmma_tflops": dmma_peak, "dfma_and_dmma_tflops": mixed_peak,
                            "sms": torch.cuda.get_device_properties(dev).multi_processor_count},
             "cpu_baseline": None, "e2e": None, "gpu_launches": launches, "clocks": clk_sum, **extra}))
 
@@ -744,21 +759,21 @@ def main():
     if fmt == "fp8":
         peak_sus, peak_kind = 2 * peak_sus, f"2x {peak_kind} (FP8 nominal ratio)"
     achieved = kernel_flops / avg_launch_s / 1e12
-    traffic = None
-    tf = ROOT / "profiles" / "split_gemm_traffic.json"
-    # the committed capture is of the default workload only
-    if tf.exists() and (n, args.alg, levels, s, fmt) == (16384, "222", 2, 6, "bf16"):
-        try:
-            # ncu DRAM bytes of one step's GEMM launches, per launch
-            per_step = json.loads(tf.read_text()).get("bytes_per_step_16384_x2")
-            launches_per_step = gemm_n / max(args.steps, 1)
-            traffic = per_step / launches_per_step if per_step and launches_per_step else None
-        except ValueError:
-            traffic = None
+    # DRAM traffic per GEMM launch: the small-case capture (m=n=k=4096, ncu, one launch) per work item, times the
+    # items of this workload's launches. At 16384 the concurrent tiles' slice panels exceed L2 by more, so this
+    # scaled figure is a lower bound there.
+    traffic, traffic_src = None, None
+    tf = ROOT / "profiles" / "split_gemm_pair_kernel_traffic_222x2_4096.json"
+    if tf.exists() and fmt == "bf16" and me >= 1024:
+        cap = json.loads(tf.read_text())
+        items_per_launch = (gemm_products / max(gemm_n, 1)) * (-(-me // 256)) ** 2
+        traffic = (cap["dram_read"] + cap["dram_write"]) / cap["items"] * items_per_launch
+        traffic_src = (f"ncu capture at m=n=k=4096 ({cap['items']} items), scaled by work items to "
+                       f"{items_per_launch:.0f} items per launch; a lower bound at larger sizes")
     # single calls take 256 x 256 CTA-pair tiles once m_e >= 1024
     kernel = "split_gemm_pair_kernel" if me >= 1024 else "split_gemm_kernel"
     roofline = {"bound": "tensor", "achieved": achieved, "peak": peak_sus, "unit": "TFLOP/s",
-                "frac": achieved / peak_sus, "traffic": traffic,
+                "frac": achieved / peak_sus, "traffic": traffic, "traffic_source": traffic_src,
                 "kernel": kernel, "peak_kind": peak_kind,
                 "flops_per_launch": kernel_flops, "avg_launch_ms": avg_launch_s * 1e3, "launches_timed": gemm_n,
                 "products_per_launch": gemm_products / max(gemm_n, 1)}

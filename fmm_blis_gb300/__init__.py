@@ -138,7 +138,7 @@ def lib() -> ctypes.CDLL:
     L.fmm_gpu_set_f64_batch_ctas.restype = ci
     L.fmm_gpu_set_f64_batch_ctas.argtypes = [ci]
     L.fmm_gpu_fp64_pipe_rates.restype = ci
-    L.fmm_gpu_fp64_pipe_rates.argtypes = [ctypes.POINTER(dbl), ctypes.POINTER(dbl)]
+    L.fmm_gpu_fp64_pipe_rates.argtypes = [ctypes.POINTER(dbl), ctypes.POINTER(dbl), ctypes.POINTER(dbl)]
     L.fmm_gpu_split_dgemm_noalloc.restype = ci
     L.fmm_gpu_split_dgemm_noalloc.argtypes = [pf, ci, i64, i64, i64, dbl, vp, i64, vp, i64, dbl, vp, i64, ci, vp]
     L.fmm_gpu_set_kernel_timing.restype = None
@@ -219,11 +219,12 @@ def read_kernel_timing() -> tuple[float, int, int]:
     return ms.value, int(n.value), int(p.value)
 
 
-def fp64_pipe_rates() -> tuple[float, float]:
-    """(DFMA, FP64 MMA) peak TFLOP/s measured on the current GPU."""
-    a, b = ctypes.c_double(), ctypes.c_double()
-    _check(lib().fmm_gpu_fp64_pipe_rates(ctypes.byref(a), ctypes.byref(b)), "fmm_gpu_fp64_pipe_rates")
-    return a.value, b.value
+def fp64_pipe_rates() -> tuple[float, float, float]:
+    """(DFMA, FP64 MMA, both interleaved) peak TFLOP/s measured on the
+    current GPU."""
+    a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    _check(lib().fmm_gpu_fp64_pipe_rates(ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)), "fmm_gpu_fp64_pipe_rates")
+    return a.value, b.value, c.value
 
 
 def selftest_wait_expiry() -> tuple[int, int]:

@@ -611,47 +611,36 @@ namespace {
 
 constexpr int kRateChains = 8;
 
-__global__ void __launch_bounds__(256) dfma_rate_kernel(double* __restrict__ out, int iters)
-{
-    double a[kRateChains];
-#pragma unroll
-    for (int u = 0; u < kRateChains; ++u) a[u] = 1e-3 * (threadIdx.x + u);
-    const double b = 0.999999, c = 1e-9;
-    for (int it = 0; it < iters; ++it) {
-#pragma unroll
-        for (int u = 0; u < kRateChains; ++u) a[u] = fma(a[u], b, c);
-    }
-    double s = 0.0;
-#pragma unroll
-    for (int u = 0; u < kRateChains; ++u) s += a[u];
-    out[blockIdx.x * (int64_t)blockDim.x + threadIdx.x] = s;
-}
-
-__global__ void __launch_bounds__(256) dmma_rate_kernel(double* __restrict__ out, int iters)
+/* NF DFMA chains per thread and NM FP64 MMA chains per warp, interleaved */
+template <int NF, int NM>
+__global__ void __launch_bounds__(256) fp64_rate_kernel(double* __restrict__ out, int iters)
 {
     const int lane = threadIdx.x % 32;
-    const double a = 1e-3 * (lane + 1), b = 0.5;
-    double d[kRateChains][2];
+    double a[kRateChains], d[kRateChains][2];
 #pragma unroll
-    for (int u = 0; u < kRateChains; ++u) { d[u][0] = 0.0; d[u][1] = 0.0; }
+    for (int u = 0; u < kRateChains; ++u) { a[u] = 1e-3 * (threadIdx.x + u); d[u][0] = 0.0; d[u][1] = 0.0; }
+    const double x = 1e-3 * (lane + 1), y = 0.5, b = 0.999999, c = 1e-9;
     for (int it = 0; it < iters; ++it) {
 #pragma unroll
-        for (int u = 0; u < kRateChains; ++u)
-            asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0, %1}, {%2}, {%3}, {%0, %1};"
-                         : "+d"(d[u][0]), "+d"(d[u][1])
-                         : "d"(a), "d"(b));
+        for (int u = 0; u < kRateChains; ++u) {
+            if (u < NF) a[u] = fma(a[u], b, c);
+            if (u < NM)
+                asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0, %1}, {%2}, {%3}, {%0, %1};"
+                             : "+d"(d[u][0]), "+d"(d[u][1])
+                             : "d"(x), "d"(y));
+        }
     }
-    double s = 0.0;
+    double sum = 0.0;
 #pragma unroll
-    for (int u = 0; u < kRateChains; ++u) s += d[u][0] + d[u][1];
-    out[blockIdx.x * (int64_t)blockDim.x + threadIdx.x] = s;
+    for (int u = 0; u < kRateChains; ++u) sum += a[u] + d[u][0] + d[u][1];
+    out[blockIdx.x * (int64_t)blockDim.x + threadIdx.x] = sum;
 }
 
 }  // namespace
 
-extern "C" int fmm_gpu_fp64_pipe_rates(double* dfma_tflops, double* dmma_tflops)
+extern "C" int fmm_gpu_fp64_pipe_rates(double* dfma_tflops, double* dmma_tflops, double* mixed_tflops)
 {
-    if (dfma_tflops == nullptr || dmma_tflops == nullptr) return FMM_ERR_ARG;
+    if (dfma_tflops == nullptr || dmma_tflops == nullptr || mixed_tflops == nullptr) return FMM_ERR_ARG;
     int dev = 0, sms = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
@@ -663,12 +652,13 @@ extern "C" int fmm_gpu_fp64_pipe_rates(double* dfma_tflops, double* dmma_tflops)
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     int rc = FMM_OK;
-    float ms[2] = {0.f, 0.f};
-    for (int which = 0; which < 2 && rc == FMM_OK; ++which) {
+    float ms[3] = {0.f, 0.f, 0.f};
+    for (int which = 0; which < 3 && rc == FMM_OK; ++which) {
         for (int rep = 0; rep < 3; ++rep) {   /* the first launch warms up */
             cudaEventRecord(e0);
-            if (which == 0) dfma_rate_kernel<<<blocks, threads>>>(out, iters);
-            else dmma_rate_kernel<<<blocks, threads>>>(out, iters);
+            if (which == 0) fp64_rate_kernel<kRateChains, 0><<<blocks, threads>>>(out, iters);
+            else if (which == 1) fp64_rate_kernel<0, kRateChains><<<blocks, threads>>>(out, iters);
+            else fp64_rate_kernel<kRateChains / 2, kRateChains / 2><<<blocks, threads>>>(out, iters);
             cudaEventRecord(e1);
             fmm_count_launch(1);
             if (cudaEventSynchronize(e1) != cudaSuccess || cudaGetLastError() != cudaSuccess) { rc = FMM_ERR_CUDA; break; }
@@ -682,7 +672,9 @@ extern "C" int fmm_gpu_fp64_pipe_rates(double* dfma_tflops, double* dmma_tflops)
     cudaFree(out);
     if (rc != FMM_OK) return rc;
     const double threads_total = (double)blocks * threads;
-    *dfma_tflops = threads_total * iters * kRateChains * 2.0 / (ms[0] * 1e-3) / 1e12;
-    *dmma_tflops = threads_total / 32.0 * iters * kRateChains * (2.0 * 8 * 8 * 4) / (ms[1] * 1e-3) / 1e12;
+    const double fma_flops = threads_total * iters * 2.0, mma_flops = threads_total / 32.0 * iters * (2.0 * 8 * 8 * 4);
+    *dfma_tflops = fma_flops * kRateChains / (ms[0] * 1e-3) / 1e12;
+    *dmma_tflops = mma_flops * kRateChains / (ms[1] * 1e-3) / 1e12;
+    *mixed_tflops = (fma_flops + mma_flops) * (kRateChains / 2) / (ms[2] * 1e-3) / 1e12;
     return FMM_OK;
 }

@@ -340,12 +340,13 @@ int fmm_gpu_set_f64_batch_ctas(int max_ctas);
 int fmm_gpu_set_split_pair_rows(int min_rows);
 
 /* Measured peak rates (TFLOP/s) of the GPU's two FP64 paths: DFMA
- * (fma.rn.f64, which the plain form's micro-kernel uses) and the FP64
- * tensor-core MMA (mma.sync m8n8k4 f64), each from a compute-only kernel
- * with independent chains over every SM, timed with CUDA events (best of two
- * launches after a warm-up). A measurement utility for choosing the plain
- * form's engine; no counterpart in the reference. */
-int fmm_gpu_fp64_pipe_rates(double* dfma_tflops, double* dmma_tflops);
+ * (fma.rn.f64, which the plain form's micro-kernel uses), the FP64
+ * tensor-core MMA (mma.sync m8n8k4 f64), and both interleaved in one kernel
+ * (their sum; about the larger alone when they share one pipe). Each from a
+ * compute-only kernel with independent chains over every SM, timed with CUDA
+ * events (best of two launches after a warm-up). A measurement utility for
+ * choosing the plain form's engine; no counterpart in the reference. */
+int fmm_gpu_fp64_pipe_rates(double* dfma_tflops, double* dmma_tflops, double* mixed_tflops);
 
 /* Number of kernels the library launched since load (all entry points). */
 uint64_t fmm_gpu_launch_count(void);
