@@ -592,10 +592,11 @@ def run_serve(args, fmm, dev, world, rank, barrier, max_over_ranks):
 
 
 def run_fp64(args, fmm, f, dev, world, rank, barrier, max_over_ranks):
-    """The plain FP64 FMM drop-in as the timed step (one kernel launch per
-    step, C := C + A*B); the classical FP64 GEMM of this library at the same
-    shape is timed once beside it. The FP64 FMA pipe bounds this form: the
-    roofline peak is 2 FMA/clock/SM at the maximum SM clock."""
+    """The plain FP64 FMM as the timed step (one kernel launch per step,
+    C := C + A*B, device operands), `e2e` through the host-buffer drop-in
+    fmm_gpu_strassen_ab_ex; the classical FP64 GEMM of this library at the
+    same shape is timed once beside it. The FP64 FMA pipe bounds this form:
+    the roofline peak is the DFMA rate measured by fmm_gpu_fp64_pipe_rates."""
     import torch
 
     n, levels = args.n, args.levels
@@ -619,6 +620,39 @@ def run_fp64(args, fmm, f, dev, world, rank, barrier, max_over_ranks):
     launches = fmm.launch_count() - n_launch0
     ms = max_over_ranks(total / args.steps)
     value = world * flops / (ms / 1e3) / 1e12
+    # end to end through the host-buffer drop-in (fmm_gpu_strassen_ab_ex, bli_strassen_ab_ex's replacement) with
+    # pinned host operands: every call uploads A, B and C and reads C back
+    e2e = None
+    if rank == 0 and args.e2e_steps > 0:
+        hA = torch.empty((n, n), dtype=torch.float64, pin_memory=True).t()
+        hB = torch.empty((n, n), dtype=torch.float64, pin_memory=True).t()
+        hC = torch.empty((n, n), dtype=torch.float64, pin_memory=True).t()
+        hA.copy_(A)
+        hB.copy_(B)
+        hC.copy_(C0)
+        fl = f if levels == 1 else fmm.kron(f, f)
+        L = fmm.lib()
+
+        def host_step():
+            st = L.fmm_gpu_strassen_ab_ex(1.0, hA.data_ptr(), n, hB.data_ptr(), n, 1.0, hC.data_ptr(), n, n, n, n, fl)
+            assert st == 0, st
+
+        host_step()   # sizes the call's device buffers
+        with Clocks(torch.cuda.current_device()) as clk_e2e:
+            t0 = time.perf_counter()
+            for _ in range(args.e2e_steps):
+                host_step()
+            ms_e2e = (time.perf_counter() - t0) * 1e3 / args.e2e_steps
+        fmm.release_host_buffers()
+        link = copy_rates(torch, hA, A, hC, C)
+        op = n * n * 8
+        e2e = {"value": flops / ms_e2e / 1e9, "unit": "TFLOP/s", "h2d_bytes_per_step": 3 * op,
+               "d2h_bytes_per_step": op, "ms_per_step": ms_e2e,
+               "call": "fmm_gpu_strassen_ab_ex (host buffers; device buffers kept between calls)",
+               "link": {**link, "serial_copies_ms": 3 * op / link["h2d_gbs"] / 1e6 + op / link["d2h_gbs"] / 1e6},
+               "clocks": clk_e2e.summary()}
+        if levels != 1:
+            fmm.free_fmm(fl)
     mt, kt, nt, R = f.m_tilde ** levels, f.k_tilde ** levels, f.n_tilde ** levels, f.R ** levels
     executed = 2.0 * (-(-n // mt)) * (-(-n // nt)) * (-(-n // kt)) * R
     clk_sum = clk.summary()
@@ -661,7 +695,7 @@ def run_fp64(args, fmm, f, dev, world, rank, barrier, max_over_ranks):
                          "executed_flops_per_step": executed},
             "fp64_pipes": {"dfma_tflops": dfma_peak, "dmma_tflops": dmma_peak, "dfma_and_dmma_tflops": mixed_peak,
                            "sms": torch.cuda.get_device_properties(dev).multi_processor_count},
-            "cpu_baseline": None, "e2e": None, "gpu_launches": launches, "clocks": clk_sum, **extra}))
+            "cpu_baseline": None, "e2e": e2e, "gpu_launches": launches, "clocks": clk_sum, **extra}))
 
 
 def main():

@@ -273,32 +273,9 @@ extern "C" int fmm_gpu_strassen_ab_ex(double alpha, const double* A, int64_t lda
 {
     int rc = check_gemm_args(m, n, k, A, lda, B, ldb, C, ldc);
     if (rc != FMM_OK) return rc;
-    if (m == 0 || n == 0) return FMM_OK;
-    double *dA = nullptr, *dB = nullptr, *dC = nullptr;
-    const int64_t ka = k > 0 ? k : 1;
-    rc = FMM_OK;
-    if (cudaMalloc(&dA, sizeof(double) * (size_t)(m * ka)) != cudaSuccess ||
-        cudaMalloc(&dB, sizeof(double) * (size_t)(ka * n)) != cudaSuccess ||
-        cudaMalloc(&dC, sizeof(double) * (size_t)(m * n)) != cudaSuccess)
-        rc = FMM_ERR_ALLOC;
-    if (rc == FMM_OK && k > 0 &&
-        (cudaMemcpy2D(dA, sizeof(double) * m, A, sizeof(double) * lda, sizeof(double) * m, k,
-                      cudaMemcpyHostToDevice) != cudaSuccess ||
-         cudaMemcpy2D(dB, sizeof(double) * k, B, sizeof(double) * ldb, sizeof(double) * k, n,
-                      cudaMemcpyHostToDevice) != cudaSuccess))
-        rc = FMM_ERR_CUDA;
-    if (rc == FMM_OK && cudaMemcpy2D(dC, sizeof(double) * m, C, sizeof(double) * ldc, sizeof(double) * m, n,
-                                     cudaMemcpyHostToDevice) != cudaSuccess)
-        rc = FMM_ERR_CUDA;
-    if (rc == FMM_OK)
-        rc = fmm_gpu_dgemm(&fmm, 1, m, n, k, alpha, dA, m, dB, ka, beta, dC, m, nullptr);
-    if (rc == FMM_OK && cudaMemcpy2D(C, sizeof(double) * ldc, dC, sizeof(double) * m, sizeof(double) * m, n,
-                                     cudaMemcpyDeviceToHost) != cudaSuccess)
-        rc = FMM_ERR_CUDA;
-    cudaFree(dA);
-    cudaFree(dB);
-    cudaFree(dC);
-    return rc;
+    /* column-major operands: the layout path of fmm_gpu_strassen_ab_gen with row stride 1 */
+    return fmm_gpu_strassen_ab_gen(alpha, A, 1, std::max<int64_t>(lda, 1), B, 1, std::max<int64_t>(ldb, 1), beta, C,
+                                   1, std::max<int64_t>(ldc, 1), m, n, k, fmm);
 }
 
 namespace {
@@ -344,53 +321,102 @@ dim3 transpose_grid(int64_t rows, int64_t cols)
 }
 
 /* A host operand with element (i, j) at X[i*rs + j*cs] into the column-major
- * device array dX (rows x cols): rs == 1 is one pitched copy; cs == 1 (row
- * major, or a transposed column-major operand) is one pitched copy into
- * dtmp and a transpose on the device; any other strides are gathered on the
- * host. */
-int operand_to_device(const double* X, int64_t rows, int64_t cols, int64_t rs, int64_t cs, double* dX, double* dtmp)
+ * device array dX (rows x cols), asynchronously on st: rs == 1 is one pitched
+ * copy; cs == 1 (row major, or a transposed column-major operand) is one
+ * pitched copy into dtmp and a transpose on the device; any other strides
+ * are gathered on the host (a pageable source: the copy has taken it when
+ * cudaMemcpyAsync returns). */
+int operand_to_device(const double* X, int64_t rows, int64_t cols, int64_t rs, int64_t cs, double* dX, double* dtmp,
+                      cudaStream_t st)
 {
     if (rows == 0 || cols == 0) return FMM_OK;
     if (rs == 1) {
-        return cudaMemcpy2D(dX, sizeof(double) * rows, X, sizeof(double) * cs, sizeof(double) * rows, cols,
-                            cudaMemcpyHostToDevice) == cudaSuccess ? FMM_OK : FMM_ERR_CUDA;
+        return cudaMemcpy2DAsync(dX, sizeof(double) * rows, X, sizeof(double) * cs, sizeof(double) * rows, cols,
+                                 cudaMemcpyHostToDevice, st) == cudaSuccess ? FMM_OK : FMM_ERR_CUDA;
     }
     if (cs == 1) {
-        if (cudaMemcpy2D(dtmp, sizeof(double) * cols, X, sizeof(double) * rs, sizeof(double) * cols, rows,
-                         cudaMemcpyHostToDevice) != cudaSuccess)
+        if (cudaMemcpy2DAsync(dtmp, sizeof(double) * cols, X, sizeof(double) * rs, sizeof(double) * cols, rows,
+                              cudaMemcpyHostToDevice, st) != cudaSuccess)
             return FMM_ERR_CUDA;
-        transpose_to_colmajor<<<transpose_grid(rows, cols), dim3(32, 8)>>>(dtmp, dX, rows, cols);
+        transpose_to_colmajor<<<transpose_grid(rows, cols), dim3(32, 8), 0, st>>>(dtmp, dX, rows, cols);
         fmm_count_launch(1);
         return cudaGetLastError() == cudaSuccess ? FMM_OK : FMM_ERR_CUDA;
     }
     std::vector<double> h((size_t)(rows * cols));
     for (int64_t j = 0; j < cols; ++j)
         for (int64_t i = 0; i < rows; ++i) h[(size_t)(i + j * rows)] = X[i * rs + j * cs];
-    return cudaMemcpy(dX, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice) == cudaSuccess
+    return cudaMemcpyAsync(dX, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice, st) == cudaSuccess
                ? FMM_OK : FMM_ERR_CUDA;
 }
 
-/* the reverse for C: only the elements of the operand are written */
-int operand_to_host(const double* dX, int64_t rows, int64_t cols, double* X, int64_t rs, int64_t cs, double* dtmp)
+/* the reverse for C, on st: only the elements of the operand are written
+ * (the general-strides path waits for its copy before scattering) */
+int operand_to_host(const double* dX, int64_t rows, int64_t cols, double* X, int64_t rs, int64_t cs, double* dtmp,
+                    cudaStream_t st)
 {
     if (rows == 0 || cols == 0) return FMM_OK;
     if (rs == 1) {
-        return cudaMemcpy2D(X, sizeof(double) * cs, dX, sizeof(double) * rows, sizeof(double) * rows, cols,
-                            cudaMemcpyDeviceToHost) == cudaSuccess ? FMM_OK : FMM_ERR_CUDA;
+        return cudaMemcpy2DAsync(X, sizeof(double) * cs, dX, sizeof(double) * rows, sizeof(double) * rows, cols,
+                                 cudaMemcpyDeviceToHost, st) == cudaSuccess ? FMM_OK : FMM_ERR_CUDA;
     }
     if (cs == 1) {
-        transpose_from_colmajor<<<transpose_grid(rows, cols), dim3(32, 8)>>>(dX, dtmp, rows, cols);
+        transpose_from_colmajor<<<transpose_grid(rows, cols), dim3(32, 8), 0, st>>>(dX, dtmp, rows, cols);
         fmm_count_launch(1);
         if (cudaGetLastError() != cudaSuccess) return FMM_ERR_CUDA;
-        return cudaMemcpy2D(X, sizeof(double) * rs, dtmp, sizeof(double) * cols, sizeof(double) * cols, rows,
-                            cudaMemcpyDeviceToHost) == cudaSuccess ? FMM_OK : FMM_ERR_CUDA;
+        return cudaMemcpy2DAsync(X, sizeof(double) * rs, dtmp, sizeof(double) * cols, sizeof(double) * cols, rows,
+                                 cudaMemcpyDeviceToHost, st) == cudaSuccess ? FMM_OK : FMM_ERR_CUDA;
     }
     std::vector<double> h((size_t)(rows * cols));
-    if (cudaMemcpy(h.data(), dX, sizeof(double) * h.size(), cudaMemcpyDeviceToHost) != cudaSuccess)
+    if (cudaMemcpyAsync(h.data(), dX, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
         return FMM_ERR_CUDA;
     for (int64_t j = 0; j < cols; ++j)
         for (int64_t i = 0; i < rows; ++i) X[i * rs + j * cs] = h[(size_t)(i + j * rows)];
     return FMM_OK;
+}
+
+/* Device buffers of the host-buffer calls of any layout (fmm_gpu_strassen_ab_ex,
+ * fmm_gpu_strassen_ab_gen and the split form's non-column-major path), per
+ * device: grow-only, kept between calls so a call allocates nothing once
+ * warm, freed by fmm_gpu_release_host_buffers; and one non-blocking stream per
+ * device that the calls' copies and kernels run on. */
+struct GenBuffers {
+    void* p[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};   /* A, B, C, transpose scratch, split workspace */
+    size_t have[5] = {0, 0, 0, 0, 0};
+    cudaStream_t st = nullptr;
+};
+std::mutex g_gen_mu;
+GenBuffers g_gen[64];
+
+/* buffer x of at least `need` bytes (the stream is idle between calls) */
+int gen_buffer(GenBuffers& b, int x, size_t need, void** out)
+{
+    need = std::max<size_t>(need, 256);
+    if (b.have[x] < need) {
+        if (b.p[x]) cudaFree(b.p[x]);
+        b.p[x] = nullptr;
+        b.have[x] = 0;
+        if (cudaMalloc(&b.p[x], need) != cudaSuccess) return FMM_ERR_ALLOC;
+        b.have[x] = need;
+    }
+    *out = b.p[x];
+    return FMM_OK;
+}
+
+int gen_device(GenBuffers** out)
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return FMM_ERR_CUDA;
+    GenBuffers& b = g_gen[dev];
+    if (b.st == nullptr && cudaStreamCreateWithFlags(&b.st, cudaStreamNonBlocking) != cudaSuccess) return FMM_ERR_CUDA;
+    *out = &b;
+    return FMM_OK;
+}
+
+/* needs a transpose scratch: some operand is row-major (or transposed) */
+bool gen_needs_tmp(int64_t rsa, int64_t csa, int64_t rsb, int64_t csb, int64_t rsc, int64_t csc)
+{
+    return (rsa != 1 && csa == 1) || (rsb != 1 && csb == 1) || (rsc != 1 && csc == 1);
 }
 
 }  // namespace
@@ -404,26 +430,26 @@ extern "C" int fmm_gpu_strassen_ab_gen(double alpha, const double* A, int64_t rs
     if (m > 0 && n > 0 && C == nullptr) return FMM_ERR_ARG;
     if (m > 0 && n > 0 && k > 0 && (A == nullptr || B == nullptr)) return FMM_ERR_ARG;
     if (m == 0 || n == 0) return FMM_OK;
-    double *dA = nullptr, *dB = nullptr, *dC = nullptr, *dT = nullptr;
+    std::lock_guard<std::mutex> lk(g_gen_mu);
+    GenBuffers* b = nullptr;
+    int rc = gen_device(&b);
+    if (rc != FMM_OK) return rc;
     const int64_t ka = k > 0 ? k : 1;
-    const int64_t tmp = std::max(std::max(m * ka, ka * n), m * n);
-    int rc = FMM_OK;
-    if (cudaMalloc(&dA, sizeof(double) * (size_t)(m * ka)) != cudaSuccess ||
-        cudaMalloc(&dB, sizeof(double) * (size_t)(ka * n)) != cudaSuccess ||
-        cudaMalloc(&dC, sizeof(double) * (size_t)(m * n)) != cudaSuccess ||
-        cudaMalloc(&dT, sizeof(double) * (size_t)tmp) != cudaSuccess)
-        rc = FMM_ERR_ALLOC;
-    if (rc == FMM_OK && k > 0) rc = operand_to_device(A, m, k, rsa, csa, dA, dT);
-    if (rc == FMM_OK && k > 0) rc = operand_to_device(B, k, n, rsb, csb, dB, dT);
-    if (rc == FMM_OK) rc = operand_to_device(C, m, n, rsc, csc, dC, dT);
-    if (rc == FMM_OK) rc = fmm_gpu_dgemm(&fmm, 1, m, n, k, alpha, dA, m, dB, ka, beta, dC, m, nullptr);
-    if (rc == FMM_OK) rc = operand_to_host(dC, m, n, C, rsc, csc, dT);
-    if (rc == FMM_OK && cudaDeviceSynchronize() != cudaSuccess) rc = FMM_ERR_CUDA;
+    const size_t tmp = sizeof(double) * (size_t)std::max(std::max(m * ka, ka * n), m * n);
+    void *dA = nullptr, *dB = nullptr, *dC = nullptr, *dT = nullptr;
+    if ((rc = gen_buffer(*b, 0, sizeof(double) * (size_t)(m * ka), &dA)) != FMM_OK ||
+        (rc = gen_buffer(*b, 1, sizeof(double) * (size_t)(ka * n), &dB)) != FMM_OK ||
+        (rc = gen_buffer(*b, 2, sizeof(double) * (size_t)(m * n), &dC)) != FMM_OK ||
+        (gen_needs_tmp(rsa, csa, rsb, csb, rsc, csc) && (rc = gen_buffer(*b, 3, tmp, &dT)) != FMM_OK))
+        return rc;
+    if (k > 0) rc = operand_to_device(A, m, k, rsa, csa, (double*)dA, (double*)dT, b->st);
+    if (rc == FMM_OK && k > 0) rc = operand_to_device(B, k, n, rsb, csb, (double*)dB, (double*)dT, b->st);
+    if (rc == FMM_OK) rc = operand_to_device(C, m, n, rsc, csc, (double*)dC, (double*)dT, b->st);
+    if (rc == FMM_OK)
+        rc = fmm_gpu_dgemm(&fmm, 1, m, n, k, alpha, (double*)dA, m, (double*)dB, ka, beta, (double*)dC, m, b->st);
+    if (rc == FMM_OK) rc = operand_to_host((double*)dC, m, n, C, rsc, csc, (double*)dT, b->st);
+    if (cudaStreamSynchronize(b->st) != cudaSuccess && rc == FMM_OK) rc = FMM_ERR_CUDA;
     if (rc == FMM_OK) rc = fmm_device_error_status();
-    cudaFree(dA);
-    cudaFree(dB);
-    cudaFree(dC);
-    cudaFree(dT);
     return rc;
 }
 
@@ -483,7 +509,20 @@ extern "C" int fmm_gpu_split_strassen_ab_ex(double alpha, const double* A, int64
     return fmm_split_host(alg, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, slices, format);
 }
 
-extern "C" void fmm_gpu_release_host_buffers(void) { fmm_split_host_release(); }
+extern "C" void fmm_gpu_release_host_buffers(void)
+{
+    fmm_split_host_release();
+    std::lock_guard<std::mutex> lk(g_gen_mu);
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return;
+    GenBuffers& b = g_gen[dev];
+    if (b.st) cudaStreamSynchronize(b.st);
+    for (int x = 0; x < 5; ++x) {
+        if (b.p[x]) cudaFree(b.p[x]);
+        b.p[x] = nullptr;
+        b.have[x] = 0;
+    }
+}
 
 extern "C" int fmm_gpu_split_strassen_ab_gen(double alpha, const double* A, int64_t rsa, int64_t csa,
                                              const double* B, int64_t rsb, int64_t csb, double beta, double* C,
@@ -506,31 +545,28 @@ extern "C" int fmm_gpu_split_strassen_ab_gen(double alpha, const double* A, int6
     const fmm_t* pf = levels > 0 ? &fmm : nullptr;
     const size_t wsb = fmm_gpu_split_workspace_size_fmt(pf, levels, m, n, k, slices, format);
     if (wsb == 0) return FMM_ERR_ARG;
-    double *dA = nullptr, *dB = nullptr, *dC = nullptr, *dT = nullptr;
-    void* ws = nullptr;
+    std::lock_guard<std::mutex> lk(g_gen_mu);
+    GenBuffers* b = nullptr;
+    int rc = gen_device(&b);
+    if (rc != FMM_OK) return rc;
     const int64_t ka = k > 0 ? k : 1;
-    const int64_t tmp = std::max(std::max(m * ka, ka * n), m * n);
-    int rc = FMM_OK;
-    if (cudaMalloc(&dA, sizeof(double) * (size_t)(m * ka)) != cudaSuccess ||
-        cudaMalloc(&dB, sizeof(double) * (size_t)(ka * n)) != cudaSuccess ||
-        cudaMalloc(&dC, sizeof(double) * (size_t)(m * n)) != cudaSuccess ||
-        cudaMalloc(&dT, sizeof(double) * (size_t)tmp) != cudaSuccess || cudaMalloc(&ws, wsb) != cudaSuccess)
-        rc = FMM_ERR_ALLOC;
-    if (rc == FMM_OK && k > 0) rc = operand_to_device(A, m, k, rsa, csa, dA, dT);
-    if (rc == FMM_OK && k > 0) rc = operand_to_device(B, k, n, rsb, csb, dB, dT);
-    if (rc == FMM_OK) rc = operand_to_device(C, m, n, rsc, csc, dC, dT);
+    const size_t tmp = sizeof(double) * (size_t)std::max(std::max(m * ka, ka * n), m * n);
+    void *dA = nullptr, *dB = nullptr, *dC = nullptr, *dT = nullptr, *ws = nullptr;
+    if ((rc = gen_buffer(*b, 0, sizeof(double) * (size_t)(m * ka), &dA)) != FMM_OK ||
+        (rc = gen_buffer(*b, 1, sizeof(double) * (size_t)(ka * n), &dB)) != FMM_OK ||
+        (rc = gen_buffer(*b, 2, sizeof(double) * (size_t)(m * n), &dC)) != FMM_OK ||
+        (gen_needs_tmp(rsa, csa, rsb, csb, rsc, csc) && (rc = gen_buffer(*b, 3, tmp, &dT)) != FMM_OK) ||
+        (rc = gen_buffer(*b, 4, wsb, &ws)) != FMM_OK)
+        return rc;
+    if (k > 0) rc = operand_to_device(A, m, k, rsa, csa, (double*)dA, (double*)dT, b->st);
+    if (rc == FMM_OK && k > 0) rc = operand_to_device(B, k, n, rsb, csb, (double*)dB, (double*)dT, b->st);
+    if (rc == FMM_OK) rc = operand_to_device(C, m, n, rsc, csc, (double*)dC, (double*)dT, b->st);
     if (rc == FMM_OK)
-        rc = fmm_gpu_split_dgemm_fmt(pf, levels, m, n, k, alpha, dA, m, dB, ka, beta, dC, m, slices, format, ws, wsb,
-                                     nullptr);
-    if (rc == FMM_OK) rc = operand_to_host(dC, m, n, C, rsc, csc, dT);
-    if (rc == FMM_OK && cudaDeviceSynchronize() != cudaSuccess) rc = FMM_ERR_CUDA;
+        rc = fmm_gpu_split_dgemm_fmt(pf, levels, m, n, k, alpha, (double*)dA, m, (double*)dB, ka, beta, (double*)dC,
+                                     m, slices, format, ws, b->have[4], b->st);
+    if (rc == FMM_OK) rc = operand_to_host((double*)dC, m, n, C, rsc, csc, (double*)dT, b->st);
+    if (cudaStreamSynchronize(b->st) != cudaSuccess && rc == FMM_OK) rc = FMM_ERR_CUDA;
     if (rc == FMM_OK) rc = fmm_device_error_status();
-    cudaGetLastError();
-    cudaFree(dA);
-    cudaFree(dB);
-    cudaFree(dC);
-    cudaFree(dT);
-    cudaFree(ws);
     return rc;
 }
 
