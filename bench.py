@@ -430,7 +430,7 @@ def run_batch(args, fmm, dev, world, rank, barrier, max_over_ranks):
     flops = sum(2.0 * m * n * k for m, n, k in shapes)
     stream = torch.cuda.current_stream()
     results = {}
-    for form in ("split", "fp64"):
+    for form in ("split",) if args.no_fp64 else ("split", "fp64"):
         plans = [tuner.plan(m, n, k, form, args.target) for m, n, k in shapes]
         probs = [{"A": A, "B": B, "C": C, "fmm": alg(p.alg), "levels": p.levels, "slices": p.slices, "fmt": p.fmt}
                  for (A, B, C), p in zip(ops, plans)]
@@ -490,7 +490,7 @@ def run_batch(args, fmm, dev, world, rank, barrier, max_over_ranks):
                        "count": args.count, "total_gflop": flops / 1e9,
                        "l2": "operands of 512 problems (tens of GB) larger than L2; no flush",
                        "parallelism": f"replicas x{world}"},
-            "split_batch": sp, "fp64_batch": results["fp64"],
+            "split_batch": sp, "fp64_batch": results.get("fp64"),
             "split_max_rel_err_sample": max(errs), "gpu_launches": sp["launches_per_step"] * sp["steps"],
             "clocks": sp["clocks"]}))
 

@@ -264,15 +264,16 @@ __host__ __device__ __forceinline__ Tab tab_view(const int* tab)
 
 /* amax[b*m + i] = max over the columns of k-block b of |A[i, :]| (as the bit
  * pattern of a non-negative double, which orders like the value). */
-__global__ void amax_kernel(const double* __restrict__ A, int64_t lda, int64_t m, int64_t k,
-                            int kt, unsigned long long* __restrict__ amax, int cols_per_block)
+__device__ __forceinline__ void amax_body(const double* __restrict__ A, int64_t lda, int64_t m, int64_t k, int kt,
+                                          unsigned long long* __restrict__ amax, int cols_per_block, int64_t bx,
+                                          int by, int64_t bz)
 {
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    const int b = blockIdx.y;
+    const int64_t i = bx * (int64_t)blockDim.x + threadIdx.x;
+    const int b = by;
     if (i >= m) return;
     int64_t co, cl;
     fmm_part_geom(k, kt, b, &co, &cl);
-    const int64_t c0 = (int64_t)blockIdx.z * cols_per_block;
+    const int64_t c0 = bz * cols_per_block;
     if (c0 >= cl) return;
     const int64_t c1 = cl < c0 + cols_per_block ? cl : c0 + cols_per_block;
     const double* col = A + i + (co + c0) * lda;
@@ -296,12 +297,18 @@ __global__ void amax_kernel(const double* __restrict__ A, int64_t lda, int64_t m
     atomicMax(&amax[(int64_t)b * m + i], mx);
 }
 
+__global__ void amax_kernel(const double* __restrict__ A, int64_t lda, int64_t m, int64_t k,
+                            int kt, unsigned long long* __restrict__ amax, int cols_per_block)
+{
+    amax_body(A, lda, m, k, kt, amax, cols_per_block, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
 /* bmax[b*n + j] = max over the rows of k-block b of |B[:, j]| for the columns
  * j in [c0, c1); one warp per (j, b). */
-__global__ void bmax_kernel(const double* __restrict__ B, int64_t ldb, int64_t k, int64_t n,
-                            int kt, unsigned long long* __restrict__ bmax, int64_t c0, int64_t c1)
+__device__ __forceinline__ void bmax_body(const double* __restrict__ B, int64_t ldb, int64_t k, int64_t n, int kt,
+                                          unsigned long long* __restrict__ bmax, int64_t c0, int64_t c1, int64_t bx)
 {
-    const int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / 32;
+    const int64_t w = (bx * (int64_t)blockDim.x + threadIdx.x) / 32;
     const int lane = threadIdx.x % 32;
     const int64_t nc = c1 - c0;
     if (w >= nc * kt) return;
@@ -323,23 +330,28 @@ __global__ void bmax_kernel(const double* __restrict__ B, int64_t ldb, int64_t k
     if (lane == 0) bmax[(int64_t)b * n + j] = mx;
 }
 
+__global__ void bmax_kernel(const double* __restrict__ B, int64_t ldb, int64_t k, int64_t n,
+                            int kt, unsigned long long* __restrict__ bmax, int64_t c0, int64_t c1)
+{
+    bmax_body(B, ldb, k, n, kt, bmax, c0, c1, blockIdx.x);
+}
+
 /* Row exponents of S_r (index < m_pad) and column exponents of T_r (index
  * m_pad + j) for the products r = r0 + blockIdx.y of a group, into
  * e_row[q][m_pad] and f_col[q][n_pad]; a launch covers the indices
  * [first, end), so the row side (needs only amax) and the column side (needs
  * only bmax) can run on different streams. */
-__global__ void exps_kernel(const int* __restrict__ tab, int r0, int64_t m, int64_t n, int64_t k,
-                            int64_t m_pad, int64_t n_pad,
-                            const unsigned long long* __restrict__ amax,
-                            const unsigned long long* __restrict__ bmax,
-                            int* __restrict__ e_row, int* __restrict__ f_col, int64_t first, int64_t end)
+__device__ __forceinline__ void exps_body(const int* __restrict__ tab, int r0, int64_t m, int64_t n, int64_t k,
+                                          int64_t m_pad, int64_t n_pad, const unsigned long long* __restrict__ amax,
+                                          const unsigned long long* __restrict__ bmax, int* __restrict__ e_row,
+                                          int* __restrict__ f_col, int64_t first, int64_t end, int64_t bx, int by)
 {
     const Tab t = tab_view(tab);
-    const int r = r0 + (int)blockIdx.y;
-    e_row += (int64_t)blockIdx.y * m_pad;
-    f_col += (int64_t)blockIdx.y * n_pad;
+    const int r = r0 + by;
+    e_row += (int64_t)by * m_pad;
+    f_col += (int64_t)by * n_pad;
     const int64_t me = (m + t.mt - 1) / t.mt, ne = (n + t.nt - 1) / t.nt;
-    const int64_t idx = first + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t idx = first + bx * (int64_t)blockDim.x + threadIdx.x;
     if (idx >= end) return;
     if (idx < m_pad) {
         const int64_t i = idx;
@@ -377,6 +389,15 @@ __global__ void exps_kernel(const int* __restrict__ tab, int r0, int64_t m, int6
         f_col[j] = exp_above(bnd);
     }
     (void)k;
+}
+
+__global__ void exps_kernel(const int* __restrict__ tab, int r0, int64_t m, int64_t n, int64_t k,
+                            int64_t m_pad, int64_t n_pad,
+                            const unsigned long long* __restrict__ amax,
+                            const unsigned long long* __restrict__ bmax,
+                            int* __restrict__ e_row, int* __restrict__ f_col, int64_t first, int64_t end)
+{
+    exps_body(tab, r0, m, n, k, m_pad, n_pad, amax, bmax, e_row, f_col, first, end, blockIdx.x, blockIdx.y);
 }
 
 /* ----------------------------------------------------- pack kernels ---- */
@@ -431,18 +452,18 @@ __device__ __forceinline__ void scale_first(const PEnt& x, double (&s)[N])
  * memory, at most 64 registers) for batched waves, small enough to run on an
  * SM beside a resident GEMM CTA. */
 template <int S, int DB, int ROWS>
-__global__ void __launch_bounds__(ROWS * 4, ROWS == 64 ? 4 : 8)
-pack_a_kernel(const int* __restrict__ tab, int r0, int np, const double* __restrict__ A, int64_t lda,
-              int64_t m, int64_t k, int64_t m_pad, int64_t k_pad,
-              const int* __restrict__ e_row, uint8_t* __restrict__ sa)
+__device__ __forceinline__ void pack_a_body(const int* __restrict__ tab, int r0, int np, const double* __restrict__ A,
+                                            int64_t lda, int64_t m, int64_t k, int64_t m_pad, int64_t k_pad,
+                                            const int* __restrict__ e_row, uint8_t* __restrict__ sa, int64_t bx,
+                                            int64_t by)
 {
     __shared__ double Sf[64][ROWS + 1];
     __shared__ PEnt ent[kPackMaxEnt];
     const Tab t = tab_view(tab);
     const int64_t me = (m + t.mt - 1) / t.mt, ke = (k + t.kt - 1) / t.kt;
-    const int q = (int)(blockIdx.x % (unsigned)np);
+    const int q = (int)(bx % np);
     const int r = r0 + q;
-    const int64_t i0 = (int64_t)(blockIdx.x / (unsigned)np) * ROWS, p0 = (int64_t)blockIdx.y * 64;
+    const int64_t i0 = (bx / np) * ROWS, p0 = by * 64;
     e_row += (int64_t)q * m_pad;
     const int64_t slice0 = (int64_t)q * S * m_pad * k_pad;   /* element offset of this product */
     const int eb = t.u_off[r], ne_ = t.u_off[r + 1] - eb;
@@ -504,21 +525,30 @@ pack_a_kernel(const int* __restrict__ tab, int r0, int np, const double* __restr
     }
 }
 
+template <int S, int DB, int ROWS>
+__global__ void __launch_bounds__(ROWS * 4, ROWS == 64 ? 4 : 8)
+pack_a_kernel(const int* __restrict__ tab, int r0, int np, const double* __restrict__ A, int64_t lda,
+              int64_t m, int64_t k, int64_t m_pad, int64_t k_pad,
+              const int* __restrict__ e_row, uint8_t* __restrict__ sa)
+{
+    pack_a_body<S, DB, ROWS>(tab, r0, np, A, lda, m, k, m_pad, k_pad, e_row, sa, blockIdx.x, blockIdx.y);
+}
+
 /* B side, all products of a group: CTA (q, tile) forms the tile of COLS
  * columns x 64 k of T_r, r = r0 + q (column j of T_r is contiguous in k
  * already), and writes its digits into slices sb[q][t][n_pad][k_pad];
  * product index fastest, as on the A side. COLS = 32 (256 threads) for single
  * calls, 16 (128 threads, at most 64 registers) for batched waves. */
 template <int S, int DB, int COLS>
-__global__ void __launch_bounds__(COLS * 8, COLS == 32 ? 4 : 8)
-pack_b_kernel(const int* __restrict__ tab, int r0, int np, const double* __restrict__ B, int64_t ldb,
-              int64_t k, int64_t n, int64_t n_pad, int64_t k_pad,
-              const int* __restrict__ f_col, uint8_t* __restrict__ sb, int64_t j_first)
+__device__ __forceinline__ void pack_b_body(const int* __restrict__ tab, int r0, int np, const double* __restrict__ B,
+                                            int64_t ldb, int64_t k, int64_t n, int64_t n_pad, int64_t k_pad,
+                                            const int* __restrict__ f_col, uint8_t* __restrict__ sb, int64_t j_first,
+                                            int64_t bx, int64_t by)
 {
     __shared__ PEnt ent[kPackMaxEnt];
     const Tab t = tab_view(tab);
     const int64_t ne = (n + t.nt - 1) / t.nt, ke = (k + t.kt - 1) / t.kt;
-    const int q = (int)(blockIdx.x % (unsigned)np);
+    const int q = (int)(bx % np);
     const int r = r0 + q;
     f_col += (int64_t)q * n_pad;
     const int64_t slice0 = (int64_t)q * S * n_pad * k_pad;
@@ -532,8 +562,8 @@ pack_b_kernel(const int* __restrict__ tab, int r0, int np, const double* __restr
     }
     __syncthreads();
     const int kg = threadIdx.x % 8;
-    const int64_t gj = j_first + (int64_t)(blockIdx.x / (unsigned)np) * COLS + threadIdx.x / 8;
-    const int64_t p0 = (int64_t)blockIdx.y * 64 + kg * 8;
+    const int64_t gj = j_first + (bx / np) * COLS + threadIdx.x / 8;
+    const int64_t p0 = by * 64 + kg * 8;
     double v8[8];
 #pragma unroll
     for (int x = 0; x < 8; ++x) v8[x] = 0.0;
@@ -565,6 +595,15 @@ pack_b_kernel(const int* __restrict__ tab, int r0, int np, const double* __restr
 #pragma unroll
     for (int x = 0; x < 8; ++x) Y[x] = split_offset<S, DB>(v8[x], F);
     store_digits8<S, DB>(sb, slice0 + gj * k_pad + p0, n_pad * k_pad, Y);
+}
+
+template <int S, int DB, int COLS>
+__global__ void __launch_bounds__(COLS * 8, COLS == 32 ? 4 : 8)
+pack_b_kernel(const int* __restrict__ tab, int r0, int np, const double* __restrict__ B, int64_t ldb,
+              int64_t k, int64_t n, int64_t n_pad, int64_t k_pad,
+              const int* __restrict__ f_col, uint8_t* __restrict__ sb, int64_t j_first)
+{
+    pack_b_body<S, DB, COLS>(tab, r0, np, B, ldb, k, n, n_pad, k_pad, f_col, sb, j_first, blockIdx.x, blockIdx.y);
 }
 
 /* Which packs a launch_packs call issues: both sides, or one side only; the
@@ -1461,11 +1500,12 @@ __device__ __forceinline__ void scatter_all_element(uint64_t idx, uint32_t me, i
  * the group's W entries fit the shared-memory budget. */
 constexpr int kScatterAllSmem = 32 * 1024;   /* cs[] budget: P * threads * 8 */
 
-__global__ void __launch_bounds__(256)
-scatter_all_kernel(const int* __restrict__ tab, int r0, int nprod, int64_t m, int64_t n,
-                   int m_pad, int n_pad, int ebase, double alpha, const int64_t* __restrict__ Z,
-                   const int* __restrict__ e_row, const int* __restrict__ f_col, double* __restrict__ C,
-                   int64_t ldc, uint64_t idx_first, uint64_t idx_end)
+/* vb, vg: the block's index among the vg blocks that share the element range */
+__device__ __forceinline__ void scatter_all_body(const int* __restrict__ tab, int r0, int nprod, int64_t m, int64_t n,
+                                                 int m_pad, int n_pad, int ebase, double alpha,
+                                                 const int64_t* __restrict__ Z, const int* __restrict__ e_row,
+                                                 const int* __restrict__ f_col, double* __restrict__ C, int64_t ldc,
+                                                 uint64_t idx_first, uint64_t idx_end, uint64_t vb, uint64_t vg)
 {
     extern __shared__ double sm_all[];
     __shared__ int geo[4][64];           /* per sub-block p: ro, rl, co, cl */
@@ -1488,14 +1528,137 @@ scatter_all_kernel(const int* __restrict__ tab, int r0, int nprod, int64_t m, in
     __syncthreads();
     const uint32_t me = (uint32_t)((m + t.mt - 1) / t.mt), ne = (uint32_t)((n + t.nt - 1) / t.nt);
     /* me * ne < 2^32 (checked on the host), so the element index fits 32 bits */
-    const uint64_t idx = idx_first + (uint64_t)blockIdx.x * (uint64_t)T + (uint64_t)tid;
+    const uint64_t idx = idx_first + vb * (uint64_t)T + (uint64_t)tid;
     const uint64_t end = idx_end < (uint64_t)me * (uint64_t)ne ? idx_end : (uint64_t)me * (uint64_t)ne;
     /* grid-stride: a block's set-up above serves many elements */
-    for (uint64_t idx2 = idx; idx2 < end; idx2 += (uint64_t)gridDim.x * (uint64_t)T)
+    for (uint64_t idx2 = idx; idx2 < end; idx2 += vg * (uint64_t)T)
         scatter_all_element(idx2, me, P, T, tid, nprod, m_pad, n_pad, ebase, geo, cs, lam, pidx, off, Z, e_row,
                             f_col, C, ldc);
 }
 
+__global__ void __launch_bounds__(256)
+scatter_all_kernel(const int* __restrict__ tab, int r0, int nprod, int64_t m, int64_t n,
+                   int m_pad, int n_pad, int ebase, double alpha, const int64_t* __restrict__ Z,
+                   const int* __restrict__ e_row, const int* __restrict__ f_col, double* __restrict__ C,
+                   int64_t ldc, uint64_t idx_first, uint64_t idx_end)
+{
+    scatter_all_body(tab, r0, nprod, m, n, m_pad, n_pad, ebase, alpha, Z, e_row, f_col, C, ldc, idx_first, idx_end,
+                     blockIdx.x, gridDim.x);
+}
+
+
+/* ------------------------------------- batched waves: side work per wave ---- */
+
+/* A wave of a batch runs each side kernel (C scaling and maxima zeroing,
+ * maxima, exponents, packs, C updates) as one launch over all its problems
+ * instead of one launch per problem: the problems travel by value in a table
+ * (like the GEMM's), each owns a contiguous range of the launch's blocks, and
+ * a block finds its problem by binary search and runs the same per-block code
+ * (the *_body functions) the single-problem kernels run, so the results are
+ * the single calls' bits. */
+struct WaveProb {
+    const int* tab;
+    const double* A;
+    const double* B;
+    double* C;
+    unsigned long long* amax;
+    unsigned long long* bmax;
+    int* e_row;
+    int* f_col;
+    uint8_t* sa;
+    uint8_t* sb;
+    const int64_t* Z;
+    int64_t lda, ldb, ldc, m, n, k, m_pad, n_pad, k_pad;
+    int64_t b0;   /* the problem's first block in this launch */
+    int64_t nb;   /* its blocks */
+    int64_t gx;   /* blocks along the first coordinate of its per-problem grid */
+    double alpha, beta;
+    int R, kt, ebase;
+};
+struct WaveLaunch {
+    int nprob;
+    WaveProb p[kMaxLaunchProblems];
+};
+static_assert(sizeof(WaveLaunch) <= 32764, "WaveLaunch must fit the kernel parameter space");
+
+__device__ __forceinline__ int wave_find(const WaveLaunch& W, int64_t b)
+{
+    int lo = 0, hi = W.nprob - 1;   /* last problem with b0 <= b */
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) / 2;
+        if (W.p[mid].b0 <= b) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+/* C := beta*C (when beta != 1) and the maxima arrays zeroed, grid-stride over each problem's range */
+__global__ void __launch_bounds__(256) wave_prep_kernel(const __grid_constant__ WaveLaunch W)
+{
+    const WaveProb& P = W.p[wave_find(W, blockIdx.x)];
+    const int64_t vb = blockIdx.x - P.b0;
+    const int64_t za = (int64_t)P.kt * P.m, zb = (int64_t)P.kt * P.n;
+    const int64_t total = za + zb + (P.beta != 1.0 ? P.m * P.n : 0);
+    for (int64_t x = vb * blockDim.x + threadIdx.x; x < total; x += P.nb * (int64_t)blockDim.x) {
+        if (x < za) {
+            P.amax[x] = 0;
+        } else if (x < za + zb) {
+            P.bmax[x - za] = 0;
+        } else {
+            const int64_t e = x - za - zb;
+            double* c = P.C + e % P.m + (e / P.m) * P.ldc;
+            *c = P.beta == 0.0 ? 0.0 : P.beta * *c;
+        }
+    }
+}
+
+/* row maxima of A (gx blocks: 256 rows x one k part x 256 columns) then column maxima of B */
+__global__ void __launch_bounds__(256) wave_maxima_kernel(const __grid_constant__ WaveLaunch W)
+{
+    const WaveProb& P = W.p[wave_find(W, blockIdx.x)];
+    const int64_t vb = blockIdx.x - P.b0;
+    if (vb < P.gx) {
+        const int64_t rb = (P.m + 255) / 256;
+        amax_body(P.A, P.lda, P.m, P.k, P.kt, P.amax, 256, vb % rb, (int)((vb / rb) % P.kt), vb / rb / P.kt);
+    } else {
+        bmax_body(P.B, P.ldb, P.k, P.n, P.kt, P.bmax, 0, P.n, vb - P.gx);
+    }
+}
+
+__global__ void __launch_bounds__(256) wave_exps_kernel(const __grid_constant__ WaveLaunch W)
+{
+    const WaveProb& P = W.p[wave_find(W, blockIdx.x)];
+    const int64_t vb = blockIdx.x - P.b0;
+    exps_body(P.tab, 0, P.m, P.n, P.k, P.m_pad, P.n_pad, P.amax, P.bmax, P.e_row, P.f_col, 0, P.m_pad + P.n_pad,
+              vb % P.gx, (int)(vb / P.gx));
+}
+
+template <int S, int DB, int ROWS>
+__global__ void __launch_bounds__(ROWS * 4, ROWS == 64 ? 4 : 8) wave_pack_a_kernel(const __grid_constant__ WaveLaunch W)
+{
+    const WaveProb& P = W.p[wave_find(W, blockIdx.x)];
+    const int64_t vb = blockIdx.x - P.b0;
+    pack_a_body<S, DB, ROWS>(P.tab, 0, P.R, P.A, P.lda, P.m, P.k, P.m_pad, P.k_pad, P.e_row, P.sa, vb % P.gx,
+                             vb / P.gx);
+}
+
+template <int S, int DB, int COLS>
+__global__ void __launch_bounds__(COLS * 8, COLS == 32 ? 4 : 8) wave_pack_b_kernel(const __grid_constant__ WaveLaunch W)
+{
+    const WaveProb& P = W.p[wave_find(W, blockIdx.x)];
+    const int64_t vb = blockIdx.x - P.b0;
+    pack_b_body<S, DB, COLS>(P.tab, 0, P.R, P.B, P.ldb, P.k, P.n, P.n_pad, P.k_pad, P.f_col, P.sb, 0, vb % P.gx,
+                             vb / P.gx);
+}
+
+__global__ void __launch_bounds__(256) wave_scatter_kernel(const __grid_constant__ WaveLaunch W)
+{
+    const WaveProb& P = W.p[wave_find(W, blockIdx.x)];
+    const int64_t vb = blockIdx.x - P.b0;
+    const Tab t = tab_view(P.tab);
+    const uint64_t me = (uint64_t)((P.m + t.mt - 1) / t.mt), ne = (uint64_t)((P.n + t.nt - 1) / t.nt);
+    scatter_all_body(P.tab, 0, P.R, P.m, P.n, (int)P.m_pad, (int)P.n_pad, P.ebase, P.alpha, P.Z, P.e_row, P.f_col,
+                     P.C, P.ldc, 0, me * ne, (uint64_t)vb, (uint64_t)P.nb);
+}
 
 /* --------------------------------------------------------- host -------- */
 
@@ -2413,6 +2576,175 @@ void fmm_split_host_release()
  * caller's stream. A problem too large for its share of the workspace runs
  * alone, after everything before it, with the whole workspace and product
  * groups. Every problem's result equals its single-call result. */
+/* ------------------------------------------- batched waves: host side ---- */
+
+/* the fields every wave kernel reads, for a bound job (its whole algorithm as one group) */
+static WaveProb wave_prob(const SplitJob& j)
+{
+    WaveProb w;
+    memset(&w, 0, sizeof(w));
+    w.tab = j.alg.tab;
+    w.A = j.A; w.B = j.B; w.C = j.C;
+    w.amax = (unsigned long long*)(j.w + j.L.amax);
+    w.bmax = (unsigned long long*)(j.w + j.L.bmax);
+    w.e_row = (int*)(j.w + j.L.erow);
+    w.f_col = (int*)(j.w + j.L.fcol);
+    w.sa = j.w + j.L.sa;
+    w.sb = j.w + j.L.sb;
+    w.Z = (const int64_t*)(j.w + j.L.z);
+    w.lda = j.lda; w.ldb = j.ldb; w.ldc = j.ldc;
+    w.m = j.m; w.n = j.n; w.k = j.k;
+    w.m_pad = j.d.m_pad; w.n_pad = j.d.n_pad; w.k_pad = j.d.k_pad;
+    w.alpha = j.alpha; w.beta = j.beta;
+    w.R = j.alg.R; w.kt = j.alg.kt;
+    w.ebase = job_ebase(j);
+    return w;
+}
+
+/* a table over jobs `qs`, each given gx and its block count by `size`; returns the launch's blocks */
+template <class F>
+static int64_t wave_table(WaveLaunch& L, const std::vector<SplitJob*>& qs, F size)
+{
+    L.nprob = 0;
+    int64_t acc = 0;
+    for (SplitJob* j : qs) {
+        WaveProb& w = L.p[L.nprob++];
+        w = wave_prob(*j);
+        size(*j, w);
+        w.b0 = acc;
+        acc += w.nb;
+    }
+    return acc;
+}
+
+template <int S, int DB>
+static void wave_packs_t(WaveLaunch& L, const std::vector<SplitJob*>& qs, bool small, cudaStream_t st)
+{
+    const int rows = small ? 32 : 64, cols = small ? 16 : 32;
+    int64_t nb = wave_table(L, qs, [&](const SplitJob& j, WaveProb& w) {
+        w.gx = (int64_t)j.alg.R * (j.d.m_pad / rows);
+        w.nb = w.gx * (j.d.k_pad / 64);
+    });
+    if (small)
+        wave_pack_a_kernel<S, DB, 32><<<(unsigned)nb, 128, 0, st>>>(L);
+    else
+        wave_pack_a_kernel<S, DB, 64><<<(unsigned)nb, 256, 0, st>>>(L);
+    nb = wave_table(L, qs, [&](const SplitJob& j, WaveProb& w) {
+        w.gx = (int64_t)j.alg.R * ((j.d.n_pad + cols - 1) / cols);
+        w.nb = w.gx * (j.d.k_pad / 64);
+    });
+    if (small)
+        wave_pack_b_kernel<S, DB, 16><<<(unsigned)nb, 128, 0, st>>>(L);
+    else
+        wave_pack_b_kernel<S, DB, 32><<<(unsigned)nb, 256, 0, st>>>(L);
+    fmm_count_launch(2);
+}
+
+static void wave_packs(int fmt, int s, WaveLaunch& L, const std::vector<SplitJob*>& qs, bool small, cudaStream_t st)
+{
+#define FMM_WPACKS(S_, DB_) wave_packs_t<S_, DB_>(L, qs, small, st)
+    if (fmt == 0) {
+        switch (s) {
+        case 2: FMM_WPACKS(2, 8); break;
+        case 3: FMM_WPACKS(3, 8); break;
+        case 4: FMM_WPACKS(4, 8); break;
+        case 5: FMM_WPACKS(5, 8); break;
+        case 6: FMM_WPACKS(6, 8); break;
+        case 7: FMM_WPACKS(7, 8); break;
+        default: FMM_WPACKS(8, 8); break;
+        }
+    } else {
+        switch (s) {
+        case 2: FMM_WPACKS(2, 5); break;
+        case 3: FMM_WPACKS(3, 5); break;
+        case 4: FMM_WPACKS(4, 5); break;
+        case 5: FMM_WPACKS(5, 5); break;
+        case 6: FMM_WPACKS(6, 5); break;
+        case 7: FMM_WPACKS(7, 5); break;
+        case 8: FMM_WPACKS(8, 5); break;
+        case 9: FMM_WPACKS(9, 5); break;
+        case 10: FMM_WPACKS(10, 5); break;
+        case 11: FMM_WPACKS(11, 5); break;
+        default: FMM_WPACKS(12, 5); break;
+        }
+    }
+#undef FMM_WPACKS
+}
+
+/* The side work before a wave's GEMM, one launch per kernel over the bound
+ * jobs qs (all products of each as one group): C scaling and maxima zeroing,
+ * maxima, exponents, then the packs per (slice count, format). */
+static int wave_side_pack(const std::vector<SplitJob*>& qs, bool small, cudaStream_t st)
+{
+    if (qs.empty()) return FMM_OK;
+    WaveLaunch L;
+    int64_t nb = wave_table(L, qs, [](const SplitJob& j, WaveProb& w) {
+        const int64_t total = (int64_t)j.alg.kt * (j.m + j.n) + (j.beta != 1.0 ? j.m * j.n : 0);
+        w.gx = 1;
+        w.nb = std::min<int64_t>(std::max<int64_t>((total + 2047) / 2048, 1), 2048);
+    });
+    wave_prep_kernel<<<(unsigned)nb, 256, 0, st>>>(L);
+    nb = wave_table(L, qs, [](const SplitJob& j, WaveProb& w) {
+        w.gx = (j.m + 255) / 256 * j.alg.kt * ((j.d.ke + 255) / 256);
+        w.nb = w.gx + ((int64_t)j.alg.kt * j.n * 32 + 255) / 256;
+    });
+    wave_maxima_kernel<<<(unsigned)nb, 256, 0, st>>>(L);
+    nb = wave_table(L, qs, [](const SplitJob& j, WaveProb& w) {
+        w.gx = (j.d.m_pad + j.d.n_pad + 255) / 256;
+        w.nb = w.gx * j.alg.R;
+    });
+    wave_exps_kernel<<<(unsigned)nb, 256, 0, st>>>(L);
+    fmm_count_launch(3);
+    /* packs, one pair of launches per (format, slice count) present */
+    std::vector<std::pair<int, int>> kinds;
+    for (SplitJob* j : qs)
+        if (std::find(kinds.begin(), kinds.end(), std::make_pair(j->fmt, j->s)) == kinds.end())
+            kinds.emplace_back(j->fmt, j->s);
+    for (auto [fmt, sl] : kinds) {
+        std::vector<SplitJob*> sel;
+        for (SplitJob* j : qs)
+            if (j->fmt == fmt && j->s == sl) sel.push_back(j);
+        wave_packs(fmt, sl, L, sel, small, st);
+    }
+    return cudaGetLastError() == cudaSuccess ? FMM_OK : FMM_ERR_CUDA;
+}
+
+/* The C updates after a wave's GEMM: the element-major form in one launch for
+ * the jobs whose sub-block values and W entries fit its shared memory, the
+ * per-job form for the rest. */
+static int wave_side_scatter(const std::vector<SplitJob*>& qs, bool small, cudaStream_t st)
+{
+    std::vector<SplitJob*> all, other;
+    int T = small ? 128 : 256;
+    for (SplitJob* j : qs) {
+        int Tj;
+        size_t sm;
+        if (job_scatter_all(*j, 0, j->alg.R, &Tj, &sm) && Tj >= 32) {
+            all.push_back(j);
+            T = std::min(T, Tj);
+        } else {
+            other.push_back(j);
+        }
+    }
+    if (!all.empty()) {
+        size_t smem = 0;
+        for (SplitJob* j : all) {
+            const Tab ht = tab_view(j->alg.htab);
+            const int P = j->alg.mt * j->alg.nt, E = ht.w_off[j->alg.R] - ht.w_off[0];
+            smem = std::max(smem, (size_t)P * T * 8 + (size_t)E * 12 + (size_t)(j->alg.R + 1) * 4);
+        }
+        WaveLaunch L;
+        const int64_t nb = wave_table(L, all, [&](const SplitJob& j, WaveProb& w) {
+            w.gx = 1;
+            w.nb = scatter_blocks((uint64_t)(j.d.me * j.d.ne), T);
+        });
+        wave_scatter_kernel<<<(unsigned)nb, (unsigned)T, smem, st>>>(L);
+        fmm_count_launch(1);
+    }
+    for (SplitJob* j : other) job_scatter(*j, 0, j->alg.R, st, small);
+    return cudaGetLastError() == cudaSuccess ? FMM_OK : FMM_ERR_CUDA;
+}
+
 int fmm_split_batch(int count, const SplitJob* jobs_in, void* ws, size_t ws_bytes, cudaStream_t st)
 {
     std::lock_guard<std::mutex> use(g_side_use);
@@ -2451,15 +2783,17 @@ int fmm_split_batch(int count, const SplitJob* jobs_in, void* ws, size_t ws_byte
                 for (int y = 0; y < kWaveStreams; ++y)
                     if (!ok(cudaStreamWaitEvent(pack_st(x), sp->wave_sc[W.h][y], 0))) return FMM_ERR_CUDA;
         size_t off = 0;
+        std::vector<SplitJob*> qs;
         for (int q = W.i; q < W.e; ++q) {
             SplitJob& j = jobs[q];
-            cudaStream_t ss = pack_st(q - W.i);
             int rc = job_bind_group(j, base + off, full[q], j.alg.R);
             if (rc != FMM_OK) return rc;
             off += (full[q] + 255) / 256 * 256;
-            if ((rc = job_prologue(j, ss)) != FMM_OK) return rc;
-            if ((rc = job_pack(j, 0, j.alg.R, ss, nullptr, halves)) != FMM_OK) return rc;
+            qs.push_back(&j);
         }
+        /* the full-size tiles: measured, a wave's side kernels do not overlap the previous wave's GEMM (its
+         * CTAs hold the SMs), so the tiles that fit beside a GEMM CTA only make them slower */
+        if (int rc = wave_side_pack(qs, false, pack_st(0)); rc != FMM_OK) return rc;
         if (sp)
             for (int x = 0; x < kWaveStreams; ++x)
                 if (!ok(cudaEventRecord(sp->wave_pk[W.h][x], pack_st(x)))) return FMM_ERR_CUDA;
@@ -2505,7 +2839,9 @@ int fmm_split_batch(int count, const SplitJob* jobs_in, void* ws, size_t ws_byte
         if (sp)
             for (int y = 0; y < kWaveStreams; ++y)
                 if (!ok(cudaStreamWaitEvent(scat_st(y), sp->wave_gm[W.h], 0))) return FMM_ERR_CUDA;
-        for (int q = W.i; q < W.e; ++q) job_scatter(jobs[q], 0, jobs[q].alg.R, scat_st(q - W.i), halves);
+        std::vector<SplitJob*> qs;
+        for (int q = W.i; q < W.e; ++q) qs.push_back(&jobs[q]);
+        if (int rc = wave_side_scatter(qs, false, scat_st(0)); rc != FMM_OK) return rc;
         if (sp)
             for (int y = 0; y < kWaveStreams; ++y)
                 if (!ok(cudaEventRecord(sp->wave_sc[W.h][y], scat_st(y)))) return FMM_ERR_CUDA;

@@ -128,3 +128,40 @@ def test_batch_more_problems_than_one_launch(fmm, torch_cuda):
     for i, p in enumerate(probs):
         assert np.array_equal(to_host(p["C"]), single(fmm, p)), f"problem {i}"
     assert fmm.take_device_error() == 0
+
+
+def test_batch_wave_side_work_in_few_launches(fmm, torch_cuda):
+    """A wave's side work runs as one launch per kernel over all its problems
+    (per slice kind for the packs): BF16 and FP8 slices of several counts,
+    one and two levels, and a 444 two-level problem whose 256 C sub-blocks
+    take the per-problem C-update form. Every result equals its single call."""
+    import torch
+    algs = {a: fmm.new_fmm(COEFFS / f"{a}.txt") for a in ("222", "444")}
+    rng = np.random.default_rng(21)
+    kinds = [("bf16", 5), ("bf16", 6), ("fp8", 10)]
+    probs = []
+    try:
+        for i in range(30):
+            m, n, k = (int(x) for x in rng.integers(60, 500, 3))
+            fmt, s = kinds[i % 3]
+            f, levels = [(None, 0), (algs["222"], 1), (algs["222"], 2)][i % 3 if i % 5 else 1]
+            if i == 29:
+                f, levels, fmt, s, (m, n, k) = algs["444"], 2, "bf16", 6, (200, 180, 170)
+            C0 = rand(m, n, 4000 + i)
+            probs.append({"A": to_dev(rand(m, k, 5000 + i)), "B": to_dev(rand(k, n, 6000 + i)), "C0": C0,
+                          "C": to_dev(C0), "fmm": f, "levels": levels, "slices": s, "fmt": fmt,
+                          "alpha": float(rng.choice([1.0, 0.5])), "beta": float(rng.choice([1.0, 0.0, -2.0]))})
+        n0 = fmm.launch_count()
+        fmm.batch_dgemm(probs)
+        torch.cuda.synchronize()
+        launches = fmm.launch_count() - n0
+        assert launches <= 16, launches       # one wave: 3 + 2 x 3 kinds + GEMMs + C updates
+        for i, p in enumerate(probs):
+            dC = to_dev(p["C0"])
+            fmm.split_dgemm(p["A"], p["B"], dC, p["fmm"], p["levels"], p["slices"], alpha=p["alpha"], beta=p["beta"],
+                            fmt=p["fmt"])
+            assert np.array_equal(to_host(p["C"]), to_host(dC)), f"problem {i}"
+        assert fmm.take_device_error() == 0
+    finally:
+        for f in algs.values():
+            fmm.free_fmm(f)
