@@ -60,6 +60,8 @@ def parse():
     p.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison runs")
     p.add_argument("--no-cpu", action="store_true", help="skip the host-core baseline")
     p.add_argument("--e2e-steps", type=int, default=3)
+    p.add_argument("--f64-engine", choices=["dfma", "mma"], default=None,
+                   help="micro-kernel of the plain FP64 form (default: the library's)")
     p.add_argument("--serve-seconds", type=float, default=10.0,
                    help="default workload: seconds of the bounded served stream (Poisson 200/s); 0 skips it")
     p.add_argument("--form", choices=["split", "fp64"], default="split",
@@ -716,6 +718,8 @@ def main():
     else:
         torch.cuda.set_device(0)
     fbuild.build()
+    if args.f64_engine:
+        fmm.set_f64_engine(args.f64_engine)
     dev = torch.device("cuda", torch.cuda.current_device())
     n, levels, s = args.n, args.levels, args.slices
     f = fmm.new_fmm(COEFFS / f"{args.alg}.txt")

@@ -137,6 +137,8 @@ def lib() -> ctypes.CDLL:
     L.fmm_gpu_selftest_wait_expiry.argtypes = [ctypes.POINTER(ci)]
     L.fmm_gpu_set_f64_batch_ctas.restype = ci
     L.fmm_gpu_set_f64_batch_ctas.argtypes = [ci]
+    L.fmm_gpu_set_f64_engine.restype = ci
+    L.fmm_gpu_set_f64_engine.argtypes = [ci]
     L.fmm_gpu_fp64_pipe_rates.restype = ci
     L.fmm_gpu_fp64_pipe_rates.argtypes = [ctypes.POINTER(dbl), ctypes.POINTER(dbl), ctypes.POINTER(dbl)]
     L.fmm_gpu_split_dgemm_noalloc.restype = ci
@@ -217,6 +219,18 @@ def read_kernel_timing() -> tuple[float, int, int]:
     _check(lib().fmm_gpu_read_kernel_timing(ctypes.byref(ms), ctypes.byref(n), ctypes.byref(p)),
            "read_kernel_timing")
     return ms.value, int(n.value), int(p.value)
+
+
+F64_ENGINES = {"dfma": 0, "mma": 1}
+
+
+def set_f64_engine(engine: str) -> str:
+    """Micro-kernel of the plain FP64 form: "dfma" or "mma" (FP64 tensor-core
+    mma.sync); returns the previous one."""
+    prev = lib().fmm_gpu_set_f64_engine(F64_ENGINES[engine])
+    if prev < 0:
+        raise ValueError(engine)
+    return {v: k for k, v in F64_ENGINES.items()}[prev]
 
 
 def fp64_pipe_rates() -> tuple[float, float, float]:

@@ -34,6 +34,9 @@ namespace {
 
 constexpr int kMaxEntries = 256;  /* nonzero coefficients per product column */
 
+/* micro-kernel of the plain form (fmm_gpu_set_f64_engine): FMM_F64_DFMA or FMM_F64_MMA */
+std::atomic<int> g_f64_engine{FMM_F64_DFMA};
+
 struct Entry {
     const double* base;  /* sub-block origin in the source matrix */
     double coef;         /* small integer coefficient, already a double */
@@ -85,15 +88,42 @@ __device__ void stage_entries(const int* __restrict__ ent, int beg, int end, int
  * DFMA micro-kernel and the multi-C epilogue. Shared by the single-problem
  * kernel (one CTA per tile position) and the batched one (a work queue of
  * (problem, tile position) items). */
-template <int BM, int BN, int BK, int TM, int TN>
+/* Shared-memory layout of the combined operand tiles. DFMA engine: A as
+ * [k][m] and B as [k][n], pitch +1 (the micro-kernel reads a row of each).
+ * FP64 MMA engine: A as [k][m] with pitch BM + 8 and B transposed to [n][k]
+ * with pitch BK + 4, so both the fused packs' stores (consecutive m, or
+ * consecutive k) and the m8n8k4 fragment loads (A[gid][tig], B[tig][gid])
+ * hit distinct banks. */
+template <int BM, int BN, int BK, bool MMA>
+struct F64Smem {
+    static constexpr int PA = MMA ? BM + 8 : BM + 1;
+    static constexpr int PB = MMA ? BK + 4 : BN + 1;
+    static constexpr int A_ELEMS = BK * PA;
+    static constexpr int B_ELEMS = MMA ? BN * PB : BK * PB;
+    __device__ static __forceinline__ int a(int kk, int mm) { return kk * PA + mm; }
+    __device__ static __forceinline__ int b(int kk, int nn) { return MMA ? nn * PB + kk : kk * PB + nn; }
+};
+
+/* D += A * B on an 8 x 8 x 4 FP64 tile, one warp (mma.sync.m8n8k4.f64):
+ * a = A[gid][tig], b = B[tig][gid], d = D[gid][2 tig .. 2 tig + 1] with
+ * gid = lane / 4, tig = lane % 4. */
+__device__ __forceinline__ void mma_f64_8x8x4(double (&d)[2], double a, double b)
+{
+    asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0, %1}, {%2}, {%3}, {%0, %1};"
+                 : "+d"(d[0]), "+d"(d[1])
+                 : "d"(a), "d"(b));
+}
+
+template <int BM, int BN, int BK, int TM, int TN, bool MMA>
 __device__ __forceinline__ void f64_tile(const int* __restrict__ tab, int64_t m, int64_t n, int64_t k,
                                          double alpha, const double* __restrict__ A, int64_t lda,
                                          const double* __restrict__ B, int64_t ldb,
                                          double* __restrict__ C, int64_t ldc, int ti, int tj,
-                                         double (&As)[BK][BM + 1], double (&Bs)[BK][BN + 1],
+                                         double* As, double* Bs,
                                          Entry* ue, Entry* ve, int r_begin, int r_end,
                                          const double* __restrict__ Sp, const double* __restrict__ Tp)
 {
+    using SM = F64Smem<BM, BN, BK, MMA>;
     constexpr int NT = (BM / TM) * (BN / TN);
     constexpr int RT = BM / TM;  /* thread rows */
     constexpr int CT = BN / TN;  /* thread cols */
@@ -139,11 +169,26 @@ __device__ __forceinline__ void f64_tile(const int* __restrict__ tab, int64_t m,
         }
         __syncthreads();
 
-        double acc[TM][TN];
+        /* MMA engine: 8 warps in a WGM x (8 / WGM) grid, each an (MB*8) x (NB*8) block of fragments */
+        constexpr int WGM = BM >= 64 ? BM / 32 : 4;
+        constexpr int WM = BM / WGM, WN = BN / (8 / WGM);
+        constexpr int MB = MMA ? WM / 8 : 1, NB = MMA ? WN / 8 : 1;
+        static_assert(!MMA || (NT == 256 && WM % 8 == 0 && WN % 8 == 0 && BK % 4 == 0), "MMA warp tiling");
+        const int lane = tid % 32, wid = tid / 32, gid = lane / 4, tig = lane % 4;
+        const int wm = wid % WGM, wn = wid / WGM;
+        double acc[MMA ? 1 : TM][MMA ? 1 : TN];
+        double facc[MB][NB][2];
+        if (MMA) {
 #pragma unroll
-        for (int a = 0; a < TM; ++a)
+            for (int a = 0; a < MB; ++a)
 #pragma unroll
-            for (int b = 0; b < TN; ++b) acc[a][b] = 0.0;
+                for (int b = 0; b < NB; ++b) facc[a][b][0] = facc[a][b][1] = 0.0;
+        } else {
+#pragma unroll
+            for (int a = 0; a < (MMA ? 1 : TM); ++a)
+#pragma unroll
+                for (int b = 0; b < (MMA ? 1 : TN); ++b) acc[a][b] = 0.0;
+        }
 
         for (int64_t k0 = 0; k0 < ke; k0 += BK) {
             /* fused pack of the A-side combination: BM x BK. Each term's
@@ -176,7 +221,7 @@ __device__ __forceinline__ void f64_tile(const int* __restrict__ tab, int64_t m,
                     }
                 }
 #pragma unroll
-                for (int t = 0; t < NA; ++t) As[tid / BM + t * (NT / BM)][li] = s[t];
+                for (int t = 0; t < NA; ++t) As[SM::a(tid / BM + t * (NT / BM), li)] = s[t];
             }
             /* fused pack of the B-side combination: BK x BN */
             {
@@ -205,20 +250,35 @@ __device__ __forceinline__ void f64_tile(const int* __restrict__ tab, int64_t m,
                     }
                 }
 #pragma unroll
-                for (int t = 0; t < NB; ++t) Bs[lp][tid / BK + t * (NT / BK)] = s[t];
+                for (int t = 0; t < NB; ++t) Bs[SM::b(lp, tid / BK + t * (NT / BK))] = s[t];
             }
             __syncthreads();
+            if (MMA) {
+#pragma unroll 2
+                for (int kk = 0; kk < BK; kk += 4) {
+                    double a[MB], b[NB];
+#pragma unroll
+                    for (int x = 0; x < MB; ++x) a[x] = As[SM::a(kk + tig, wm * WM + x * 8 + gid)];
+#pragma unroll
+                    for (int y = 0; y < NB; ++y) b[y] = Bs[SM::b(kk + tig, wn * WN + y * 8 + gid)];
+#pragma unroll
+                    for (int x = 0; x < MB; ++x)
+#pragma unroll
+                        for (int y = 0; y < NB; ++y) mma_f64_8x8x4(facc[x][y], a[x], b[y]);
+                }
+            } else {
 #pragma unroll 4
-            for (int kk = 0; kk < BK; ++kk) {
-                double a[TM], b[TN];
+                for (int kk = 0; kk < BK; ++kk) {
+                    double a[MMA ? 1 : TM], b[MMA ? 1 : TN];
 #pragma unroll
-                for (int x = 0; x < TM; ++x) a[x] = As[kk][tr + x * RT];
+                    for (int x = 0; x < (MMA ? 1 : TM); ++x) a[x] = As[SM::a(kk, tr + x * RT)];
 #pragma unroll
-                for (int y = 0; y < TN; ++y) b[y] = Bs[kk][tc + y * CT];
+                    for (int y = 0; y < (MMA ? 1 : TN); ++y) b[y] = Bs[SM::b(kk, tc + y * CT)];
 #pragma unroll
-                for (int x = 0; x < TM; ++x)
+                    for (int x = 0; x < (MMA ? 1 : TM); ++x)
 #pragma unroll
-                    for (int y = 0; y < TN; ++y) acc[x][y] = fma(a[x], b[y], acc[x][y]);
+                        for (int y = 0; y < (MMA ? 1 : TN); ++y) acc[x][y] = fma(a[x], b[y], acc[x][y]);
+                }
             }
             __syncthreads();
         }
@@ -231,16 +291,34 @@ __device__ __forceinline__ void f64_tile(const int* __restrict__ tab, int64_t m,
             fmm_part_geom(m, mt, part / nt, &ro, &rl);
             fmm_part_geom(n, nt, part % nt, &co, &cl);
             double* cb = C + ro + co * ldc;
+            if (MMA) {
 #pragma unroll
-            for (int y = 0; y < TN; ++y) {
-                const int64_t gj = j0 + tc + y * CT;
-                if (gj >= cl) continue;
+                for (int y = 0; y < NB; ++y)
 #pragma unroll
-                for (int x = 0; x < TM; ++x) {
-                    const int64_t gi = i0 + tr + x * RT;
-                    if (gi < rl) {
-                        double* p = cb + gi + gj * ldc;
-                        *p = fma(lam, acc[x][y], *p);
+                    for (int h = 0; h < 2; ++h) {
+                        const int64_t gj = j0 + wn * WN + y * 8 + 2 * tig + h;
+                        if (gj >= cl) continue;
+#pragma unroll
+                        for (int x = 0; x < MB; ++x) {
+                            const int64_t gi = i0 + wm * WM + x * 8 + gid;
+                            if (gi < rl) {
+                                double* p = cb + gi + gj * ldc;
+                                *p = fma(lam, facc[x][y][h], *p);
+                            }
+                        }
+                    }
+            } else {
+#pragma unroll
+                for (int y = 0; y < (MMA ? 1 : TN); ++y) {
+                    const int64_t gj = j0 + tc + y * CT;
+                    if (gj >= cl) continue;
+#pragma unroll
+                    for (int x = 0; x < (MMA ? 1 : TM); ++x) {
+                        const int64_t gi = i0 + tr + x * RT;
+                        if (gi < rl) {
+                            double* p = cb + gi + gj * ldc;
+                            *p = fma(lam, acc[x][y], *p);
+                        }
                     }
                 }
             }
@@ -249,7 +327,7 @@ __device__ __forceinline__ void f64_tile(const int* __restrict__ tab, int64_t m,
     (void)me; (void)ne;
 }
 
-template <int BM, int BN, int BK, int TM, int TN>
+template <int BM, int BN, int BK, int TM, int TN, bool MMA>
 __global__ void __launch_bounds__((BM / TM) * (BN / TN))
 fmm_f64_kernel(const int* __restrict__ tab, int64_t m, int64_t n, int64_t k,
                double alpha, const double* __restrict__ A, int64_t lda,
@@ -257,12 +335,13 @@ fmm_f64_kernel(const int* __restrict__ tab, int64_t m, int64_t n, int64_t k,
                double* __restrict__ C, int64_t ldc, int tiles_m, int r_begin, int r_end,
                const double* __restrict__ Sp, const double* __restrict__ Tp)
 {
-    __shared__ double As[BK][BM + 1];
-    __shared__ double Bs[BK][BN + 1];
+    using SM = F64Smem<BM, BN, BK, MMA>;
+    __shared__ double As[SM::A_ELEMS];
+    __shared__ double Bs[SM::B_ELEMS];
     __shared__ Entry ue[kMaxEntries];
     __shared__ Entry ve[kMaxEntries];
-    f64_tile<BM, BN, BK, TM, TN>(tab, m, n, k, alpha, A, lda, B, ldb, C, ldc, (int)(blockIdx.x % tiles_m),
-                                 (int)(blockIdx.x / tiles_m), As, Bs, ue, ve, r_begin, r_end, Sp, Tp);
+    f64_tile<BM, BN, BK, TM, TN, MMA>(tab, m, n, k, alpha, A, lda, B, ldb, C, ldc, (int)(blockIdx.x % tiles_m),
+                                      (int)(blockIdx.x / tiles_m), As, Bs, ue, ve, r_begin, r_end, Sp, Tp);
 }
 
 /* ------------------------------------------------------------ batched -- */
@@ -306,13 +385,15 @@ __global__ void f64_table_write(const __grid_constant__ F64TableChunk c)
  * every sub-block of that tile position, then runs the tile exactly as the
  * single-problem kernel does, so each result is identical to the problem
  * issued alone. */
+template <bool MMA>
 __global__ void __launch_bounds__((kF64Bm / kF64Tm) * (kF64Bn / kF64Tn))
 fmm_f64_batch_kernel(const F64Prob* __restrict__ probs, int nprob, int64_t nitems,
                      unsigned long long* __restrict__ counter)
 {
     constexpr int RT = kF64Bm / kF64Tm, CT = kF64Bn / kF64Tn;
-    __shared__ double As[kF64Bk][kF64Bm + 1];
-    __shared__ double Bs[kF64Bk][kF64Bn + 1];
+    using SM = F64Smem<kF64Bm, kF64Bn, kF64Bk, MMA>;
+    __shared__ double As[SM::A_ELEMS];
+    __shared__ double Bs[SM::B_ELEMS];
     __shared__ Entry ue[kMaxEntries];
     __shared__ Entry ve[kMaxEntries];
     __shared__ long long next;
@@ -351,7 +432,7 @@ fmm_f64_batch_kernel(const F64Prob* __restrict__ probs, int nprob, int64_t nitem
             }
         }
         if (P.k == 0 || P.alpha == 0.0) continue;
-        f64_tile<kF64Bm, kF64Bn, kF64Bk, kF64Tm, kF64Tn>(P.tab, P.m, P.n, P.k, P.alpha, P.A, P.lda, P.B, P.ldb,
+        f64_tile<kF64Bm, kF64Bn, kF64Bk, kF64Tm, kF64Tn, MMA>(P.tab, P.m, P.n, P.k, P.alpha, P.A, P.lda, P.B, P.ldb,
                                                         P.C, P.ldc, ti, tj, As, Bs, ue, ve, 0, P.tab[3],
                                                         nullptr, nullptr);
     }
@@ -427,8 +508,12 @@ int launch_cfg(const AlgView& alg, int64_t m, int64_t n, int64_t k, double alpha
     const int64_t me = (m + alg.mt - 1) / alg.mt, ne = (n + alg.nt - 1) / alg.nt;
     const int64_t tm = (me + BM - 1) / BM, tn = (ne + BN - 1) / BN;
     if (tm * tn > 0x7fffffffLL) return FMM_ERR_UNSUPPORTED;
-    fmm_f64_kernel<BM, BN, BK, TM, TN><<<(unsigned)(tm * tn), (BM / TM) * (BN / TN), 0, st>>>(
-        alg.tab, m, n, k, alpha, A, lda, B, ldb, C, ldc, (int)tm, r_begin, r_end, Sp, Tp);
+    if (g_f64_engine.load(std::memory_order_relaxed) == FMM_F64_MMA)
+        fmm_f64_kernel<BM, BN, BK, TM, TN, true><<<(unsigned)(tm * tn), (BM / TM) * (BN / TN), 0, st>>>(
+            alg.tab, m, n, k, alpha, A, lda, B, ldb, C, ldc, (int)tm, r_begin, r_end, Sp, Tp);
+    else
+        fmm_f64_kernel<BM, BN, BK, TM, TN, false><<<(unsigned)(tm * tn), (BM / TM) * (BN / TN), 0, st>>>(
+            alg.tab, m, n, k, alpha, A, lda, B, ldb, C, ldc, (int)tm, r_begin, r_end, Sp, Tp);
     fmm_count_launch(1);
     return cudaGetLastError() == cudaSuccess ? FMM_OK : FMM_ERR_CUDA;
 }
@@ -594,8 +679,12 @@ int fmm_f64_batch_launch(int count, const F64BatchItem* items, void* ws, size_t 
     int64_t grid = std::min<int64_t>(items_total, 2 * (int64_t)sms);
     const int cap = g_f64_batch_ctas.load();
     if (cap > 0) grid = std::min<int64_t>(grid, cap);   /* items are drawn from a counter: any grid finishes them */
-    fmm_f64_batch_kernel<<<(unsigned)grid, (kF64Bm / kF64Tm) * (kF64Bn / kF64Tn), 0, st>>>(
-        dtab, (int)tab.size(), items_total, counter);
+    if (g_f64_engine.load(std::memory_order_relaxed) == FMM_F64_MMA)
+        fmm_f64_batch_kernel<true><<<(unsigned)grid, (kF64Bm / kF64Tm) * (kF64Bn / kF64Tn), 0, st>>>(
+            dtab, (int)tab.size(), items_total, counter);
+    else
+        fmm_f64_batch_kernel<false><<<(unsigned)grid, (kF64Bm / kF64Tm) * (kF64Bn / kF64Tn), 0, st>>>(
+            dtab, (int)tab.size(), items_total, counter);
     fmm_count_launch(1);
     return cudaGetLastError() == cudaSuccess ? FMM_OK : FMM_ERR_CUDA;
 }
@@ -677,4 +766,10 @@ extern "C" int fmm_gpu_fp64_pipe_rates(double* dfma_tflops, double* dmma_tflops,
     *dmma_tflops = mma_flops * kRateChains / (ms[1] * 1e-3) / 1e12;
     *mixed_tflops = (fma_flops + mma_flops) * (kRateChains / 2) / (ms[2] * 1e-3) / 1e12;
     return FMM_OK;
+}
+
+extern "C" int fmm_gpu_set_f64_engine(int engine)
+{
+    if (engine != FMM_F64_DFMA && engine != FMM_F64_MMA) return -1;
+    return g_f64_engine.exchange(engine);
 }

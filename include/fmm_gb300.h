@@ -339,6 +339,16 @@ int fmm_gpu_set_f64_batch_ctas(int max_ctas);
  * the previous value. No counterpart in the reference. */
 int fmm_gpu_set_split_pair_rows(int min_rows);
 
+/* Micro-kernel of the plain FP64 form, for single and batched calls alike:
+ * FMM_F64_DFMA (register-blocked fma.rn.f64) or FMM_F64_MMA (the FP64
+ * tensor-core path, mma.sync m8n8k4 f64, fragments from the same fused-pack
+ * tiles). Both accumulate every C element over k in increasing order; on
+ * GB300 they share one FP64 pipe (fmm_gpu_fp64_pipe_rates). Returns the
+ * previous engine, or -1 for an unknown one. No counterpart in the reference
+ * (whose micro-kernel is the haswell dgemm assembly kernel). */
+enum fmm_f64_engine { FMM_F64_DFMA = 0, FMM_F64_MMA = 1 };
+int fmm_gpu_set_f64_engine(int engine);
+
 /* Measured peak rates (TFLOP/s) of the GPU's two FP64 paths: DFMA
  * (fma.rn.f64, which the plain form's micro-kernel uses), the FP64
  * tensor-core MMA (mma.sync m8n8k4 f64), and both interleaved in one kernel
