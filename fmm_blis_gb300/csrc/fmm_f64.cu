@@ -700,23 +700,34 @@ namespace {
 
 constexpr int kRateChains = 8;
 
-/* NF DFMA chains per thread and NM FP64 MMA chains per warp, interleaved */
+/* NF DFMA chains per thread and NM FP64 MMA chains per warp, interleaved,
+ * every chain with its own operand registers. On GB300 this compute-only loop
+ * measures below what the DFMA GEMM kernel itself reaches (1.06 against
+ * 1.25 TFLOP/s for the classical FP64 GEMM at 16384^3), so its figures are a
+ * relative comparison of the two paths, not the pipe's peak. */
 template <int NF, int NM>
 __global__ void __launch_bounds__(256) fp64_rate_kernel(double* __restrict__ out, int iters)
 {
     const int lane = threadIdx.x % 32;
-    double a[kRateChains], d[kRateChains][2];
+    double a[kRateChains], bb[kRateChains], cc[kRateChains], d[kRateChains][2], x[kRateChains], y[kRateChains];
 #pragma unroll
-    for (int u = 0; u < kRateChains; ++u) { a[u] = 1e-3 * (threadIdx.x + u); d[u][0] = 0.0; d[u][1] = 0.0; }
-    const double x = 1e-3 * (lane + 1), y = 0.5, b = 0.999999, c = 1e-9;
+    for (int u = 0; u < kRateChains; ++u) {
+        a[u] = 1e-3 * (threadIdx.x + u);
+        bb[u] = 0.999999 - 1e-8 * u;
+        cc[u] = 1e-9 * (u + 1);
+        d[u][0] = 0.0;
+        d[u][1] = 0.0;
+        x[u] = 1e-3 * (lane + 1 + u);
+        y[u] = 0.5 - 1e-3 * u;
+    }
     for (int it = 0; it < iters; ++it) {
 #pragma unroll
         for (int u = 0; u < kRateChains; ++u) {
-            if (u < NF) a[u] = fma(a[u], b, c);
+            if (u < NF) a[u] = fma(a[u], bb[u], cc[u]);
             if (u < NM)
                 asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0, %1}, {%2}, {%3}, {%0, %1};"
                              : "+d"(d[u][0]), "+d"(d[u][1])
-                             : "d"(x), "d"(y));
+                             : "d"(x[u]), "d"(y[u]));
         }
     }
     double sum = 0.0;
@@ -734,7 +745,7 @@ extern "C" int fmm_gpu_fp64_pipe_rates(double* dfma_tflops, double* dmma_tflops,
     if (cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
         return FMM_ERR_CUDA;
-    const int blocks = 8 * sms, threads = 256, iters = 4096;
+    const int blocks = 8 * sms, threads = 256, iters = 16384;
     double* out = nullptr;
     if (cudaMalloc(&out, sizeof(double) * (size_t)blocks * threads) != cudaSuccess) return FMM_ERR_ALLOC;
     cudaEvent_t e0, e1;

@@ -349,13 +349,14 @@ int fmm_gpu_set_split_pair_rows(int min_rows);
 enum fmm_f64_engine { FMM_F64_DFMA = 0, FMM_F64_MMA = 1 };
 int fmm_gpu_set_f64_engine(int engine);
 
-/* Measured peak rates (TFLOP/s) of the GPU's two FP64 paths: DFMA
- * (fma.rn.f64, which the plain form's micro-kernel uses), the FP64
- * tensor-core MMA (mma.sync m8n8k4 f64), and both interleaved in one kernel
- * (their sum; about the larger alone when they share one pipe). Each from a
- * compute-only kernel with independent chains over every SM, timed with CUDA
- * events (best of two launches after a warm-up). A measurement utility for
- * choosing the plain form's engine; no counterpart in the reference. */
+/* Rates (TFLOP/s) of the GPU's two FP64 paths from compute-only kernels
+ * with independent chains over every SM, timed with CUDA events (best of two
+ * launches after a warm-up): DFMA (fma.rn.f64, which the plain form's
+ * micro-kernel uses), the FP64 tensor-core MMA (mma.sync m8n8k4 f64), and
+ * both interleaved in one kernel (their sum; about the larger alone when they
+ * share one pipe). On GB300 these loops stay below the rate the DFMA GEMM
+ * reaches, so they compare the paths rather than give the pipe's peak. A
+ * measurement utility; no counterpart in the reference. */
 int fmm_gpu_fp64_pipe_rates(double* dfma_tflops, double* dmma_tflops, double* mixed_tflops);
 
 /* Number of kernels the library launched since load (all entry points). */
