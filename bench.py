@@ -841,6 +841,11 @@ def main():
             for _ in range(args.e2e_steps):
                 host_step()
             ms_e2e = (time.perf_counter() - t0) * 1e3 / args.e2e_steps
+        # one more call with its timeline recorded (CUDA events inside the call), outside the timed steps
+        fmm.set_host_timeline(True)
+        host_step()
+        fmm.set_host_timeline(False)
+        timeline = fmm.read_host_timeline()
         fmm.release_host_buffers()
         # the host link on this machine, with the same pinned buffers: one operand up, C down (CUDA events)
         link = copy_rates(torch, hA, A, hC, C)
@@ -855,6 +860,7 @@ def main():
                         # the call cannot start the GEMM before A and B are up, nor finish before C's last
                         # column chunk (1/8 of C) is down
                         "overlap_floor_ms": up_ab + ms + op_bytes / 8 / link["d2h_gbs"] / 1e6},
+               "timeline_ms": timeline,
                "clocks": clk_e2e.summary()}
 
     extra = {}

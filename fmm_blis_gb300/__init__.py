@@ -139,6 +139,10 @@ def lib() -> ctypes.CDLL:
     L.fmm_gpu_set_f64_batch_ctas.argtypes = [ci]
     L.fmm_gpu_set_f64_engine.restype = ci
     L.fmm_gpu_set_f64_engine.argtypes = [ci]
+    L.fmm_gpu_set_host_timeline.restype = None
+    L.fmm_gpu_set_host_timeline.argtypes = [ci]
+    L.fmm_gpu_read_host_timeline.restype = ci
+    L.fmm_gpu_read_host_timeline.argtypes = [ctypes.POINTER(dbl), ci]
     L.fmm_gpu_fp64_pipe_rates.restype = ci
     L.fmm_gpu_fp64_pipe_rates.argtypes = [ctypes.POINTER(dbl), ctypes.POINTER(dbl), ctypes.POINTER(dbl)]
     L.fmm_gpu_split_dgemm_noalloc.restype = ci
@@ -479,6 +483,21 @@ def split_strassen_ab_ex(alpha: float, A, B, beta: float, C, fmm: FmmT | None = 
                                             fmm if fmm is not None else FmmT(), levels if fmm is not None else 0,
                                             slices, _fmt(fmt))
     _check(st, "fmm_gpu_split_strassen_ab_ex")
+
+
+HOST_TIMELINE = ("a_up", "b_up", "gemm_start", "gemm_end", "c_down", "host_wall")
+
+
+def set_host_timeline(enable: bool) -> None:
+    lib().fmm_gpu_set_host_timeline(1 if enable else 0)
+
+
+def read_host_timeline() -> dict:
+    """The last host-buffer split call's timeline in milliseconds (see
+    fmm_gpu_read_host_timeline)."""
+    buf = (ctypes.c_double * len(HOST_TIMELINE))()
+    c = lib().fmm_gpu_read_host_timeline(buf, len(HOST_TIMELINE))
+    return {k: buf[x] for x, k in enumerate(HOST_TIMELINE[:c])}
 
 
 def release_host_buffers() -> None:

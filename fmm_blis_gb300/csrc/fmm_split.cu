@@ -72,6 +72,7 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <chrono>
 #include <atomic>
 #include <cstring>
 #include <deque>
@@ -1925,6 +1926,15 @@ static int job_bind_group(SplitJob& j, void* ws, size_t ws_bytes, int G)
  * call, the B-side maxima and pack beside the A-side ones. Created once per
  * device; forked from and joined back to the caller's stream with events,
  * which a stream capture follows. One call at a time uses a pool (g_side_use). */
+/* Timeline of the last host-buffer call (fmm_gpu_set_host_timeline): device
+ * times, from the first copy's start, of A on the device, B on the device,
+ * the first GEMM launch's start, the last GEMM launch's end, C's last column
+ * chunk back on the host; plus the call's host wall time. */
+constexpr int kTimelinePoints = 5;
+std::atomic<bool> g_timeline{false};
+std::mutex g_timeline_mu;
+double g_timeline_ms[kTimelinePoints + 1] = {0, 0, 0, 0, 0, 0};
+
 constexpr int kWaveStreams = 8;                  /* batched waves: pack streams, then scatter streams */
 constexpr int kSideStreams = 2 * kWaveStreams;
 
@@ -1938,6 +1948,7 @@ struct SidePool {
     cudaEvent_t wave_sc[2][kWaveStreams];   /* a workspace half's C updates done */
     cudaEvent_t gate[3];   /* host-buffer calls: A, B and C on the device */
     cudaEvent_t chunk[16]; /* host-buffer calls: B chunks in, C chunks out */
+    cudaEvent_t tl[kTimelinePoints + 1];  /* host-buffer calls: the call's timeline (timing events) */
     cudaStream_t hi;       /* greatest priority: GEMMs that side work runs beside */
 };
 
@@ -1958,6 +1969,7 @@ SidePool* side_pool()
     bool ok = cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming) == cudaSuccess &&
               cudaStreamCreateWithPriority(&p->hi, cudaStreamNonBlocking, greatest) == cudaSuccess;
     for (int i = 0; i < 3 && ok; ++i) ok = cudaEventCreateWithFlags(&p->gate[i], cudaEventDisableTiming) == cudaSuccess;
+    for (int i = 0; i <= kTimelinePoints && ok; ++i) ok = cudaEventCreate(&p->tl[i]) == cudaSuccess;
     for (int i = 0; i < 16 && ok; ++i) ok = cudaEventCreateWithFlags(&p->chunk[i], cudaEventDisableTiming) == cudaSuccess;
     for (int h = 0; h < 2 && ok; ++h) {
         ok = cudaEventCreateWithFlags(&p->wave_gm[h], cudaEventDisableTiming) == cudaSuccess;
@@ -2454,6 +2466,9 @@ int fmm_split_host(const AlgView& alg, int64_t m, int64_t n, int64_t k, double a
     uint8_t* ws = base + bA + bB + bC;
     const size_t row = sizeof(double) * (size_t)m;
     auto ok = [](cudaError_t e) { return e == cudaSuccess; };
+    const bool tline = g_timeline.load() && !trivial;
+    const auto host_t0 = std::chrono::steady_clock::now();
+    auto mark = [&](int x, cudaStream_t on) { if (tline) cudaEventRecord(sp->tl[x], on); };
     if (trivial) {
         /* C := beta*C */
         if (beta != 0.0 && !ok(cudaMemcpy2DAsync(dC, row, C, sizeof(double) * ldc, row, n, cudaMemcpyHostToDevice, st)))
@@ -2469,9 +2484,11 @@ int fmm_split_host(const AlgView& alg, int64_t m, int64_t n, int64_t k, double a
         cudaStream_t sb = sp->s[0];
         /* A, then the A side's maxima (and, with one product group, its
          * exponents and slices) */
+        mark(0, cs);
         if (!ok(cudaMemcpy2DAsync(dA, row, A, sizeof(double) * lda, row, k, cudaMemcpyHostToDevice, cs)) ||
             !ok(cudaEventRecord(sp->gate[0], cs)) || !ok(cudaStreamWaitEvent(st, sp->gate[0], 0)))
             return FMM_ERR_CUDA;
+        mark(1, cs);
         if ((rc = job_maxima_a(j, st)) != FMM_OK) return rc;
         if (one_group) job_pack_a(j, 0, alg.R, st);
         /* B in kChunks chunks of T_r columns [j0, j1): chunk x holds the B
@@ -2500,6 +2517,7 @@ int fmm_split_host(const AlgView& alg, int64_t m, int64_t n, int64_t k, double a
             }
             if (one_group) job_pack_b_cols(j, 0, alg.R, j0, j1, sb);
         }
+        mark(2, cs);
         for (int r0 = 0; r0 < alg.R; r0 += G) {
             const int np = std::min(G, alg.R - r0);
             if (one_group) {
@@ -2507,7 +2525,9 @@ int fmm_split_host(const AlgView& alg, int64_t m, int64_t n, int64_t k, double a
             } else if ((rc = job_pack(j, r0, np, st, sp)) != FMM_OK) {
                 return rc;
             }
+            if (r0 == 0) mark(3, st);
             if ((rc = job_gemm(j, np, st)) != FMM_OK) return rc;
+            if (r0 + np >= alg.R) mark(4, st);
             if (r0 == 0) {
                 /* C under the first GEMM, then C := beta*C before the first scatter */
                 if (beta != 0.0 &&
@@ -2542,9 +2562,20 @@ int fmm_split_host(const AlgView& alg, int64_t m, int64_t n, int64_t k, double a
                         return FMM_ERR_CUDA;
                 }
             }
+            mark(5, cs);
             if (!ok(cudaEventRecord(sp->gate[1], cs)) || !ok(cudaStreamSynchronize(cs)) ||
                 !ok(cudaStreamSynchronize(st)))
                 return FMM_ERR_CUDA;
+            if (tline) {
+                std::lock_guard<std::mutex> lk(g_timeline_mu);
+                for (int x = 1; x <= kTimelinePoints; ++x) {
+                    float t = 0.f;
+                    cudaEventElapsedTime(&t, sp->tl[0], sp->tl[x]);
+                    g_timeline_ms[x - 1] = t;
+                }
+                g_timeline_ms[kTimelinePoints] =
+                    std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - host_t0).count();
+            }
             return cudaGetLastError() == cudaSuccess ? fmm_device_error_status() : FMM_ERR_CUDA;
         }
     }
@@ -3181,4 +3212,15 @@ extern "C" int fmm_gpu_selftest_wait_expiry(int* threads_gave_up)
     if (threads_gave_up) *threads_gave_up = gave;
     if (rc != FMM_OK) return rc;
     return fmm_device_error_status();
+}
+
+extern "C" void fmm_gpu_set_host_timeline(int enable) { g_timeline.store(enable != 0); }
+
+extern "C" int fmm_gpu_read_host_timeline(double* ms, int count)
+{
+    if (ms == nullptr || count < 0) return FMM_ERR_ARG;
+    std::lock_guard<std::mutex> lk(g_timeline_mu);
+    const int c = std::min(count, kTimelinePoints + 1);
+    for (int x = 0; x < c; ++x) ms[x] = g_timeline_ms[x];
+    return c;
 }

@@ -252,6 +252,17 @@ int fmm_gpu_split_strassen_ab_gen(double alpha, const double* A, int64_t rs_a, i
 /* Frees the current device's buffers kept by fmm_gpu_split_strassen_ab_ex. */
 void fmm_gpu_release_host_buffers(void);
 
+/* Timeline of fmm_gpu_split_strassen_ab_ex calls, while enabled: CUDA events
+ * recorded inside the call. fmm_gpu_read_host_timeline fills ms[0..5] for the
+ * last call: device milliseconds from the start of A's upload to A on the
+ * device, B on the device, the first GEMM launch's start, the last GEMM
+ * launch's end and C's last column chunk back on the host, then the call's
+ * host wall time. Returns how many values it wrote. Recorded when the call
+ * takes its overlapped path (all products' C updates in the element-major
+ * form). No counterpart in the reference. */
+void fmm_gpu_set_host_timeline(int enable);
+int fmm_gpu_read_host_timeline(double* ms, int count);
+
 /* ------------------------------------------------------- GPU, batched -- */
 
 /* One GEMM of a batch: C := beta*C + alpha*A*B with `levels` levels of `fmm`

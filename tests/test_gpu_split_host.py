@@ -114,3 +114,23 @@ def test_host_call_any_layout(fmm, torch_cuda, fmt, s):
     mask = np.ones_like(big, dtype=bool)
     mask[::2, ::3] = False
     assert np.all(big[mask] == 9.0)                    # only C's own elements written
+
+
+def test_host_call_timeline(fmm):
+    """The host-buffer call's timeline (CUDA events inside the call): A and
+    B arrive before the GEMM starts, the GEMM ends before C's last chunk is
+    back, and the device span fits inside the call's host wall time."""
+    import torch
+    assert torch.cuda.is_available()
+    m, n, k = 1500, 1300, 1100
+    A, B, C = rand(m, k, 71), rand(k, n, 72), rand(m, n, 73)
+    f = fmm.strassen_fmm()
+    fmm.set_host_timeline(True)
+    try:
+        fmm.split_strassen_ab_ex(1.0, A, B, 1.0, C.copy(order="F"), f, 1, 6)
+    finally:
+        fmm.set_host_timeline(False)
+    t = fmm.read_host_timeline()
+    assert set(t) == {"a_up", "b_up", "gemm_start", "gemm_end", "c_down", "host_wall"}
+    assert 0.0 < t["a_up"] <= t["b_up"] <= t["gemm_start"] + 1e-3
+    assert t["gemm_start"] < t["gemm_end"] <= t["c_down"] <= t["host_wall"]
