@@ -331,11 +331,11 @@ int operand_to_device(const double* X, int64_t rows, int64_t cols, int64_t rs, i
 {
     if (rows == 0 || cols == 0) return FMM_OK;
     if (rs == 1) {
-        return cudaMemcpy2DAsync(dX, sizeof(double) * rows, X, sizeof(double) * cs, sizeof(double) * rows, cols,
+        return fmm_copy2d_async(dX, sizeof(double) * rows, X, sizeof(double) * cs, sizeof(double) * rows, cols,
                                  cudaMemcpyHostToDevice, st) == cudaSuccess ? FMM_OK : FMM_ERR_CUDA;
     }
     if (cs == 1) {
-        if (cudaMemcpy2DAsync(dtmp, sizeof(double) * cols, X, sizeof(double) * rs, sizeof(double) * cols, rows,
+        if (fmm_copy2d_async(dtmp, sizeof(double) * cols, X, sizeof(double) * rs, sizeof(double) * cols, rows,
                               cudaMemcpyHostToDevice, st) != cudaSuccess)
             return FMM_ERR_CUDA;
         transpose_to_colmajor<<<transpose_grid(rows, cols), dim3(32, 8), 0, st>>>(dtmp, dX, rows, cols);
@@ -356,14 +356,14 @@ int operand_to_host(const double* dX, int64_t rows, int64_t cols, double* X, int
 {
     if (rows == 0 || cols == 0) return FMM_OK;
     if (rs == 1) {
-        return cudaMemcpy2DAsync(X, sizeof(double) * cs, dX, sizeof(double) * rows, sizeof(double) * rows, cols,
+        return fmm_copy2d_async(X, sizeof(double) * cs, dX, sizeof(double) * rows, sizeof(double) * rows, cols,
                                  cudaMemcpyDeviceToHost, st) == cudaSuccess ? FMM_OK : FMM_ERR_CUDA;
     }
     if (cs == 1) {
         transpose_from_colmajor<<<transpose_grid(rows, cols), dim3(32, 8), 0, st>>>(dX, dtmp, rows, cols);
         fmm_count_launch(1);
         if (cudaGetLastError() != cudaSuccess) return FMM_ERR_CUDA;
-        return cudaMemcpy2DAsync(X, sizeof(double) * rs, dtmp, sizeof(double) * cols, sizeof(double) * cols, rows,
+        return fmm_copy2d_async(X, sizeof(double) * rs, dtmp, sizeof(double) * cols, sizeof(double) * cols, rows,
                                  cudaMemcpyDeviceToHost, st) == cudaSuccess ? FMM_OK : FMM_ERR_CUDA;
     }
     std::vector<double> h((size_t)(rows * cols));

@@ -98,6 +98,16 @@ int fmm_split_launch(const AlgView& alg, int64_t m, int64_t n, int64_t k,
                      const double* B, int64_t ldb, double beta, double* C, int64_t ldc,
                      int slices, int fmt, void* ws, size_t ws_bytes, cudaStream_t st);
 
+/* Pitched copy of `height` rows of `width` bytes between host and device.
+ * When both pitches equal the width the rows are one contiguous block and go
+ * as a single linear copy (cudaMemcpyAsync); otherwise as a pitched copy. */
+inline cudaError_t fmm_copy2d_async(void* dst, size_t dpitch, const void* src, size_t spitch, size_t width,
+                                    size_t height, cudaMemcpyKind kind, cudaStream_t st)
+{
+    if (dpitch == width && spitch == width) return cudaMemcpyAsync(dst, src, width * height, kind, st);
+    return cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, height, kind, st);
+}
+
 /* C := beta*C (fmm_f64.cu) */
 int fmm_scale_c(int64_t m, int64_t n, double beta, double* C, int64_t ldc, cudaStream_t st);
 

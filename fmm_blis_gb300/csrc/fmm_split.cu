@@ -488,12 +488,18 @@ __device__ __forceinline__ void pack_a_body(const int* __restrict__ tab, int r0,
 #pragma unroll
         for (int y = 0; y < 8; ++y) v8[y] = 0.0;
         if (row_ok) {
-            /* term e + 1's loads go out before term e's FMAs */
+            /* term e + 1's loads go out before term e's FMAs; per term, one
+             * row test and one k limit, then a pointer step of 4 columns per
+             * element (no per-element index arithmetic) */
+            const int64_t st4 = 4 * lda;
             auto load8 = [&](const PEnt& x, double (&d)[8]) {
+                const bool rok = gi < x.rows;
+                const int64_t kl = (ke < x.cols ? ke : x.cols) - (p0 + kq + 32 * h);   /* valid while 4y < kl */
+                const double* pt = x.base + gi + (p0 + kq + 32 * h) * lda;
 #pragma unroll
                 for (int y = 0; y < 8; ++y) {
-                    const int64_t gp = p0 + kq + 4 * (8 * h + y);
-                    d[y] = (gp < ke && gi < x.rows && gp < x.cols) ? x.base[gi + gp * lda] : 0.0;
+                    d[y] = (rok && 4 * y < kl) ? __ldg(pt) : 0.0;
+                    pt += st4;
                 }
             };
             double nx[8];
@@ -569,13 +575,15 @@ __device__ __forceinline__ void pack_b_body(const int* __restrict__ tab, int r0,
 #pragma unroll
     for (int x = 0; x < 8; ++x) v8[x] = 0.0;
     if (ne_ > 0 && gj < ne) {
-        /* term e + 1's loads go out before term e's FMAs */
+        /* term e + 1's loads go out before term e's FMAs; per term, one
+         * column test and one k limit, then 8 contiguous values at fixed
+         * offsets from one pointer */
         auto load8 = [&](const PEnt& x, double (&d)[8]) {
+            const int64_t kl = (ke < x.rows ? ke : x.rows) - p0;   /* valid while y < kl */
+            const bool cok = gj < x.cols;
+            const double* pt = x.base + gj * ldb + p0;
 #pragma unroll
-            for (int y = 0; y < 8; ++y) {
-                const int64_t gp = p0 + y;
-                d[y] = (gp < ke && gp < x.rows && gj < x.cols) ? x.base[gp + gj * ldb] : 0.0;
-            }
+            for (int y = 0; y < 8; ++y) d[y] = (cok && y < kl) ? __ldg(pt + y) : 0.0;
         };
         double nx[8];
         load8(ent[0], v8);
@@ -2471,7 +2479,7 @@ int fmm_split_host(const AlgView& alg, int64_t m, int64_t n, int64_t k, double a
     auto mark = [&](int x, cudaStream_t on) { if (tline) cudaEventRecord(sp->tl[x], on); };
     if (trivial) {
         /* C := beta*C */
-        if (beta != 0.0 && !ok(cudaMemcpy2DAsync(dC, row, C, sizeof(double) * ldc, row, n, cudaMemcpyHostToDevice, st)))
+        if (beta != 0.0 && !ok(fmm_copy2d_async(dC, row, C, sizeof(double) * ldc, row, n, cudaMemcpyHostToDevice, st)))
             return FMM_ERR_CUDA;
         if (int rc = fmm_scale_c(m, n, beta, dC, m, st); rc != FMM_OK) return rc;
     } else {
@@ -2485,7 +2493,7 @@ int fmm_split_host(const AlgView& alg, int64_t m, int64_t n, int64_t k, double a
         /* A, then the A side's maxima (and, with one product group, its
          * exponents and slices) */
         mark(0, cs);
-        if (!ok(cudaMemcpy2DAsync(dA, row, A, sizeof(double) * lda, row, k, cudaMemcpyHostToDevice, cs)) ||
+        if (!ok(fmm_copy2d_async(dA, row, A, sizeof(double) * lda, row, k, cudaMemcpyHostToDevice, cs)) ||
             !ok(cudaEventRecord(sp->gate[0], cs)) || !ok(cudaStreamWaitEvent(st, sp->gate[0], 0)))
             return FMM_ERR_CUDA;
         mark(1, cs);
@@ -2504,7 +2512,7 @@ int fmm_split_host(const AlgView& alg, int64_t m, int64_t n, int64_t k, double a
                 int64_t co, cl;
                 fmm_part_geom(n, nt, c, &co, &cl);
                 const int64_t a = co + std::min(j0, cl), b = co + std::min(j1, cl);
-                if (b > a && !ok(cudaMemcpy2DAsync(dB + a * k, sizeof(double) * k, B + a * ldb, sizeof(double) * ldb,
+                if (b > a && !ok(fmm_copy2d_async(dB + a * k, sizeof(double) * k, B + a * ldb, sizeof(double) * ldb,
                                                    sizeof(double) * k, b - a, cudaMemcpyHostToDevice, cs)))
                     return FMM_ERR_CUDA;
             }
@@ -2531,7 +2539,7 @@ int fmm_split_host(const AlgView& alg, int64_t m, int64_t n, int64_t k, double a
             if (r0 == 0) {
                 /* C under the first GEMM, then C := beta*C before the first scatter */
                 if (beta != 0.0 &&
-                    (!ok(cudaMemcpy2DAsync(dC, row, C, sizeof(double) * ldc, row, n, cudaMemcpyHostToDevice, cs)) ||
+                    (!ok(fmm_copy2d_async(dC, row, C, sizeof(double) * ldc, row, n, cudaMemcpyHostToDevice, cs)) ||
                      !ok(cudaEventRecord(sp->gate[2], cs)) || !ok(cudaStreamWaitEvent(st, sp->gate[2], 0))))
                     return FMM_ERR_CUDA;
                 if ((rc = fmm_scale_c(m, n, beta, dC, m, st)) != FMM_OK) return rc;
@@ -2557,7 +2565,7 @@ int fmm_split_host(const AlgView& alg, int64_t m, int64_t n, int64_t k, double a
                     int64_t co, cl;
                     fmm_part_geom(n, nt, c, &co, &cl);
                     const int64_t a = co + std::min(j0, cl), b = co + std::min(j1, cl);
-                    if (b > a && !ok(cudaMemcpy2DAsync(C + a * ldc, sizeof(double) * ldc, dC + a * m, row, row, b - a,
+                    if (b > a && !ok(fmm_copy2d_async(C + a * ldc, sizeof(double) * ldc, dC + a * m, row, row, b - a,
                                                        cudaMemcpyDeviceToHost, cs)))
                         return FMM_ERR_CUDA;
                 }
@@ -2579,7 +2587,7 @@ int fmm_split_host(const AlgView& alg, int64_t m, int64_t n, int64_t k, double a
             return cudaGetLastError() == cudaSuccess ? fmm_device_error_status() : FMM_ERR_CUDA;
         }
     }
-    if (!ok(cudaMemcpy2DAsync(C, sizeof(double) * ldc, dC, row, row, n, cudaMemcpyDeviceToHost, st)) ||
+    if (!ok(fmm_copy2d_async(C, sizeof(double) * ldc, dC, row, row, n, cudaMemcpyDeviceToHost, st)) ||
         !ok(cudaStreamSynchronize(st)))
         return FMM_ERR_CUDA;
     /* a kernel whose bounded wait expired left C incomplete: report it */
