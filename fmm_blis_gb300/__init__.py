@@ -139,6 +139,8 @@ def lib() -> ctypes.CDLL:
     L.fmm_gpu_set_f64_batch_ctas.argtypes = [ci]
     L.fmm_gpu_set_f64_engine.restype = ci
     L.fmm_gpu_set_f64_engine.argtypes = [ci]
+    L.fmm_gpu_f64_sup_splits.restype = ci
+    L.fmm_gpu_f64_sup_splits.argtypes = [i64, i64, i64]
     L.fmm_gpu_set_host_timeline.restype = None
     L.fmm_gpu_set_host_timeline.argtypes = [ci]
     L.fmm_gpu_read_host_timeline.restype = ci
@@ -226,6 +228,12 @@ def read_kernel_timing() -> tuple[float, int, int]:
 
 
 F64_ENGINES = {"dfma": 0, "mma": 1}
+
+
+def f64_sup_splits(m: int, n: int, k: int) -> int:
+    """k chunks the plain FP64 form's small/skinny classical path uses for an
+    m x n x k classical problem (0: the regular kernel); host-only."""
+    return int(lib().fmm_gpu_f64_sup_splits(m, n, k))
 
 
 def set_f64_engine(engine: str) -> str:

@@ -25,10 +25,35 @@
  */
 #include "fmm_internal.h"
 
+#include <cooperative_groups.h>
+
 #include <algorithm>
 #include <atomic>
 #include <cstring>
 #include <vector>
+
+namespace cg = cooperative_groups;
+
+/* k chunks of the small/skinny classical path for an m x n x k FP64
+ * problem, 0 when the regular kernel runs it: at most 128 output tiles of
+ * 32 x 32, chunks of at least 256 k, at most 8 chunks (a portable cluster)
+ * and at most 256 CTAs. A function of the shape only, so single and batched
+ * calls take the same path. */
+extern "C" int fmm_gpu_f64_sup_splits(int64_t m, int64_t n, int64_t k)
+{
+    if (m <= 0 || n <= 0 || k <= 0) return 0;
+    const int64_t tiles = ((m + 31) / 32) * ((n + 31) / 32);
+    if (tiles > 128) return 0;
+    const int64_t ks = std::min<int64_t>({8, 256 / tiles, k / 256});
+    return ks >= 2 ? (int)ks : 0;
+}
+
+/* chunk length: k / ks rounded up to whole 32-k steps; every chunk is
+ * non-empty because each holds at least 256 k */
+int64_t fmm_f64_sup_chunk(int64_t k, int ks)
+{
+    return ((k + ks - 1) / ks + 31) / 32 * 32;
+}
 
 namespace {
 
@@ -500,6 +525,126 @@ __global__ void scale_c_kernel(int64_t m, int64_t n, double beta, double* C, int
     }
 }
 
+/* ------------------------------------------- small/skinny classical ---- */
+
+/* The classical FP64 GEMM of a small output (at most 128 tiles of 32 x 32)
+ * with a long k (the BLIS "sup" shapes, blis/kernels/haswell/3/sup): the
+ * regular kernel would run one CTA per tile down the whole of k on a few
+ * SMs. Here a cluster of ks CTAs (one per k chunk of kc elements) computes
+ * each tile: every CTA accumulates its chunk in k order with the DFMA
+ * micro-kernel, leaves its partial tile in shared memory, and after a cluster
+ * barrier each CTA sums a share of the tile's elements over the ks partials
+ * through distributed shared memory, always in chunk order
+ * (((p_0 + p_1) + p_2) + ...), and applies C := fma(alpha, sum, C). The
+ * result depends only on (m, n, k): the batched call runs these problems
+ * through the same kernel. */
+constexpr int kSupB = 32, kSupBk = 32, kSupT = 2, kSupThreads = (kSupB / kSupT) * (kSupB / kSupT);
+constexpr int kSupMaxTiles = 128, kSupMaxSplits = 8, kSupMinChunk = 256;
+
+__global__ void __launch_bounds__(kSupThreads)
+fmm_f64_sup_kernel(int64_t m, int64_t n, int64_t k, double alpha, const double* __restrict__ A, int64_t lda,
+                   const double* __restrict__ B, int64_t ldb, double* __restrict__ C, int64_t ldc, int tiles_m,
+                   int ks, int64_t kc)
+{
+    constexpr int RT = kSupB / kSupT;   /* thread rows (and columns) */
+    __shared__ double As[kSupBk][kSupB + 1];
+    __shared__ double Bs[kSupBk][kSupB + 1];
+    __shared__ double Ps[kSupB * kSupB];          /* this CTA's partial tile, element i + 32 j */
+    cg::cluster_group cl = cg::this_cluster();
+    const int rank = (int)cl.block_rank();        /* the k chunk */
+    const int tile = (int)(blockIdx.x / (unsigned)ks);
+    const int64_t i0 = (int64_t)(tile % tiles_m) * kSupB, j0 = (int64_t)(tile / tiles_m) * kSupB;
+    const int64_t kb = (int64_t)rank * kc, kend = kb + kc < k ? kb + kc : k;
+    const int tid = threadIdx.x, tr = tid % RT, tc = tid / RT;
+    double acc[kSupT][kSupT];
+#pragma unroll
+    for (int x = 0; x < kSupT; ++x)
+#pragma unroll
+        for (int y = 0; y < kSupT; ++y) acc[x][y] = 0.0;
+    for (int64_t k0 = kb; k0 < kend; k0 += kSupBk) {
+        /* A: 32 rows x 32 k, B: 32 k x 32 columns, zero past the edges */
+#pragma unroll
+        for (int t = 0; t < kSupB * kSupBk / kSupThreads; ++t) {
+            const int e = tid + t * kSupThreads;
+            const int li = e % kSupB, lk = e / kSupB;
+            const int64_t gi = i0 + li, gk = k0 + lk;
+            As[lk][li] = (gi < m && gk < kend) ? __ldg(A + gi + gk * lda) : 0.0;
+            const int lk2 = e % kSupBk, lj = e / kSupBk;
+            const int64_t gk2 = k0 + lk2, gj = j0 + lj;
+            Bs[lk2][lj] = (gk2 < kend && gj < n) ? __ldg(B + gk2 + gj * ldb) : 0.0;
+        }
+        __syncthreads();
+#pragma unroll 8
+        for (int kk = 0; kk < kSupBk; ++kk) {
+            double a[kSupT], b[kSupT];
+#pragma unroll
+            for (int x = 0; x < kSupT; ++x) a[x] = As[kk][tr + x * RT];
+#pragma unroll
+            for (int y = 0; y < kSupT; ++y) b[y] = Bs[kk][tc + y * RT];
+#pragma unroll
+            for (int x = 0; x < kSupT; ++x)
+#pragma unroll
+                for (int y = 0; y < kSupT; ++y) acc[x][y] = fma(a[x], b[y], acc[x][y]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int x = 0; x < kSupT; ++x)
+#pragma unroll
+        for (int y = 0; y < kSupT; ++y) Ps[(tr + x * RT) + kSupB * (tc + y * RT)] = acc[x][y];
+    cl.sync();   /* every partial tile of the cluster is in place */
+    /* the tile's 1024 elements in groups of 256, group g summed by CTA g % ks */
+    for (int g = rank; g < kSupB * kSupB / kSupThreads; g += ks) {
+        const int e = g * kSupThreads + tid;
+        double s = *cl.map_shared_rank(Ps + e, 0);
+        for (int q = 1; q < ks; ++q) s = s + *cl.map_shared_rank(Ps + e, q);
+        const int64_t gi = i0 + e % kSupB, gj = j0 + e / kSupB;
+        if (gi < m && gj < n) {
+            double* p = C + gi + gj * ldc;
+            *p = fma(alpha, s, *p);
+        }
+    }
+    cl.sync();   /* no CTA leaves while another still reads its partial */
+}
+
+/* the trivial 1 x 1 x 1 algorithm with all three coefficients +1: the
+ * classical GEMM C += alpha * A * B */
+bool plain_classical(const AlgView& alg)
+{
+    if (alg.R != 1 || alg.mt != 1 || alg.kt != 1 || alg.nt != 1 || alg.htab == nullptr) return false;
+    const int* t = alg.htab;
+    const int* u_off = t + FMM_ALG_HDR;
+    const int* v_off = u_off + 2;
+    const int* w_off = v_off + 2;
+    const int* u_ent = w_off + 2;
+    const int* v_ent = u_ent + 2 * u_off[1];
+    const int* w_ent = v_ent + 2 * v_off[1];
+    return u_off[1] == 1 && v_off[1] == 1 && w_off[1] == 1 && u_ent[1] == 1 && v_ent[1] == 1 && w_ent[1] == 1;
+}
+
+int sup_launch(int64_t m, int64_t n, int64_t k, double alpha, const double* A, int64_t lda, const double* B,
+               int64_t ldb, double* C, int64_t ldc, int ks, cudaStream_t st)
+{
+    const int64_t tm = (m + kSupB - 1) / kSupB, tn = (n + kSupB - 1) / kSupB;
+    const int64_t kc = fmm_f64_sup_chunk(k, ks);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(tm * tn * ks));
+    cfg.blockDim = dim3(kSupThreads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)ks;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, fmm_f64_sup_kernel, m, n, k, alpha, A, lda, B, ldb, C, ldc,
+                                             (int)tm, ks, kc);
+    fmm_count_launch(1);
+    return e == cudaSuccess && cudaGetLastError() == cudaSuccess ? FMM_OK : FMM_ERR_CUDA;
+}
+
 template <int BM, int BN, int BK, int TM, int TN>
 int launch_cfg(const AlgView& alg, int64_t m, int64_t n, int64_t k, double alpha,
                const double* A, int64_t lda, const double* B, int64_t ldb, double* C,
@@ -562,6 +707,10 @@ int fmm_f64_launch(const AlgView& alg, int64_t m, int64_t n, int64_t k, double a
     if (m == 0 || n == 0 || k == 0 || alpha == 0.0) return FMM_OK;
     if (alg.max_nnz_u > kMaxEntries || alg.max_nnz_v > kMaxEntries) return FMM_ERR_UNSUPPORTED;
 
+    if (plain_classical(alg)) {
+        const int ks = fmm_gpu_f64_sup_splits(m, n, k);
+        if (ks >= 2) return sup_launch(m, n, k, alpha, A, lda, B, ldb, C, ldc, ks, st);
+    }
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -640,6 +789,18 @@ int fmm_f64_batch_launch(int count, const F64BatchItem* items, void* ws, size_t 
         const F64BatchItem& it = items[i];
         if (it.alg.max_nnz_u > kMaxEntries || it.alg.max_nnz_v > kMaxEntries) return FMM_ERR_UNSUPPORTED;
         if (it.m == 0 || it.n == 0) continue;   /* nothing to do at all */
+        if (it.k > 0 && it.alpha != 0.0 && plain_classical(it.alg)) {
+            /* small/skinny classical problems take the same kernel as their
+             * single calls (C := beta*C first, as there) */
+            const int ks = fmm_gpu_f64_sup_splits(it.m, it.n, it.k);
+            if (ks >= 2) {
+                int rc = fmm_scale_c(it.m, it.n, it.beta, it.C, it.ldc, st);
+                if (rc == FMM_OK) rc = sup_launch(it.m, it.n, it.k, it.alpha, it.A, it.lda, it.B, it.ldb, it.C,
+                                                  it.ldc, ks, st);
+                if (rc != FMM_OK) return rc;
+                continue;
+            }
+        }
         const int64_t ke = (it.k + it.alg.kt - 1) / it.alg.kt;
         cost[i] = (it.k == 0 || it.alpha == 0.0) ? 1.0 : (double)it.alg.R * (double)(ke + 1);
         order.push_back(i);

@@ -360,6 +360,17 @@ int fmm_gpu_set_split_pair_rows(int min_rows);
 enum fmm_f64_engine { FMM_F64_DFMA = 0, FMM_F64_MMA = 1 };
 int fmm_gpu_set_f64_engine(int engine);
 
+/* The small/skinny classical path of the plain FP64 form, the counterpart of
+ * BLIS's "sup" kernels for small and skinny shapes (blis/kernels/haswell/3/
+ * sup): a classical FP64 GEMM (levels 0) whose output has at most 128 tiles
+ * of 32 x 32 and whose k is long runs as clusters of CTAs that split k into
+ * 2..8 chunks of at least 256 and add the chunks' partial tiles through
+ * distributed shared memory in chunk order, instead of one CTA per tile down
+ * all of k. Returns the number of chunks for an m x n x k problem (0: the
+ * regular kernel). It depends on the shape only, so single and batched calls
+ * of a problem give the same bits; it needs no GPU. */
+int fmm_gpu_f64_sup_splits(int64_t m, int64_t n, int64_t k);
+
 /* Rates (TFLOP/s) of the GPU's two FP64 paths from compute-only kernels
  * with independent chains over every SM, timed with CUDA events (best of two
  * launches after a warm-up): DFMA (fma.rn.f64, which the plain form's
