@@ -16,7 +16,10 @@ Cost model (calibrated on GB300 at m = n = k = 16384, SM clock 1.8-2.07 GHz):
     algorithms, one HBM write and read of every product's operand
     combinations (formed once ahead of the tiles). (16384^3: classical
     7.03 s measured, 7.14 s modelled; 444 two levels 5.24 / 4.96 s;
-    333 two levels 5.86 / 5.55 s.)
+    333 two levels 5.86 / 5.55 s.) Grids too small to fill the SMs use
+    32 x 32 tiles; classical problems with a small output and a long k take
+    the small/skinny path (clusters of CTAs splitting k; 128 x 128 x 16384:
+    1.05 ms measured, 1.01 ms modelled).
   Split form: the persistent tcgen05 GEMM runs (problem, product, 128 x 256
     tile) items on 152 CTAs, each item s(s+1)/2 slice pairs x k_pad/64 blocks
     of 512 MMA clocks at about 61% of 2.07 GHz under the power cap
@@ -59,6 +62,8 @@ COEFF_DIR = Path(__file__).resolve().parent / "coeffs"   # the algorithms shippe
 SMS = 152
 CLOCK_HZ = 2.07e9
 FP64_EFF = 0.98
+FP64_SMALL_EFF = 0.8      # 32 x 32 tiles (two CTAs per SM)
+FP64_SUP_EFF = 0.5        # one small/skinny cluster CTA per SM: 128 x 128 x 16384 in 1.05 ms
 SPLIT_EFF = 0.61
 PACK_S_PER_ELEM_SLICE = 1.16e-12
 SCATTER_S_PER_ENTRY_ELEM = 2.44e-12
@@ -70,6 +75,13 @@ ERR_SAFETY = 4.0
 FP8_PAIR_COST = 0.55
 DIGIT_BITS = {"bf16": 8, "fp8": 5}
 SLICE_RANGE = {"bf16": (3, 8), "fp8": (3, 12)}
+
+
+def _sup_splits(m: int, n: int, k: int) -> int:
+    """k chunks of the library's small/skinny classical FP64 path (0: the
+    regular kernel); a host-only query of the shape rule."""
+    from . import f64_sup_splits
+    return f64_sup_splits(m, n, k)
 
 
 def _cdiv(a: int, b: int) -> int:
@@ -135,7 +147,15 @@ def fp64_time(a: AlgShape, m: int, n: int, k: int) -> float:
     tiles = _cdiv(me, 64) * _cdiv(ne, 64)
     per_sm = _cdiv(tiles, SMS)
     gemm = per_sm * 2048.0 * ke * a.R / CLOCK_HZ / FP64_EFF
+    # grids too small to fill the SMs take 32 x 32 tiles, two CTAs per SM
+    gemm = min(gemm, _cdiv(_cdiv(me, 32) * _cdiv(ne, 32), 2 * SMS) * 1024.0 * ke * a.R / CLOCK_HZ / FP64_SMALL_EFF)
     if a.R == 1:
+        ks = _sup_splits(m, n, k)
+        if ks:
+            # small/skinny classical path: clusters of ks CTAs, one per k chunk
+            kc = _round_up(_cdiv(k, ks), 32)
+            ctas = _cdiv(m, 32) * _cdiv(n, 32) * ks
+            return _cdiv(ctas, 2 * SMS) * 512.0 * kc / CLOCK_HZ / FP64_SUP_EFF + 2 * LAUNCH_S
         return gemm + 2 * LAUNCH_S
     # FMM: each product's operand combinations are formed once ahead of the
     # tiles (written, then read back: HBM), so the tiles see single-term operands

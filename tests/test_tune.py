@@ -89,3 +89,18 @@ def test_slice_format_choice():
     assert only8.fmt == "fp8" and only8.est_rel_err * tune.ERR_SAFETY <= 1e-10
     a = {(x.name, x.levels): x for x in tune.alg_shapes()}
     assert tune.split_time(a[("222", 2)], 16384, 16384, 16384, 10, "fp8") == pytest.approx(0.157, rel=0.15)
+
+
+def test_small_skinny_classical_model():
+    """Classical FP64 problems with a small output and a long k are modelled
+    on the small/skinny cluster path (k split over CTAs): measured on GB300
+    128 x 128 x 16384 in 1.05 ms and 256 x 256 x 8192 in 1.06 ms (against 4.44
+    and 2.23 ms with one CTA per 32 x 32 tile down all of k)."""
+    a = {(x.name, x.levels): x for x in tune.alg_shapes()}
+    cls = a[("classical", 0)]
+    assert tune.fp64_time(cls, 128, 128, 16384) == pytest.approx(1.05e-3, rel=0.2)
+    assert tune.fp64_time(cls, 256, 256, 8192) == pytest.approx(1.06e-3, rel=0.2)
+    # the same output with a short k stays on the regular kernel
+    assert tune._sup_splits(128, 128, 300) == 0
+    p = tune.Tuner().plan(128, 128, 16384, "fp64")
+    assert (p.alg, p.levels) == ("classical", 0)
