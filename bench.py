@@ -497,6 +497,34 @@ def run_batch(args, fmm, dev, world, rank, barrier, max_over_ranks):
             "clocks": sp["clocks"]}))
 
 
+def host_operand(torch, fmm, n):
+    """An n x n column-major float64 CPU tensor in the library's pinned host
+    memory on huge pages (fmm.host_empty), as a caller of the host-buffer
+    entry points would allocate its operands."""
+    return torch.from_numpy(fmm.host_empty(n, n))
+
+
+def huge_page_share(arrays):
+    """Share of the arrays' bytes that the kernel backs with transparent huge
+    pages (AnonHugePages of the overlapping /proc/self/smaps regions); None
+    where smaps is unreadable."""
+    spans = [(a.data_ptr(), a.data_ptr() + a.numel() * a.element_size()) for a in arrays]
+    total = sum(hi - lo for lo, hi in spans)
+    huge, cur = 0, False
+    try:
+        with open("/proc/self/smaps") as f:
+            for line in f:
+                head = line.split(None, 1)[0]
+                if "-" in head and ":" not in head:
+                    lo, hi = (int(x, 16) for x in head.split("-"))
+                    cur = any(lo < b and hi > a for a, b in spans)
+                elif cur and head == "AnonHugePages:":
+                    huge += int(line.split()[1]) * 1024
+    except OSError:
+        return None
+    return min(1.0, huge / total) if total else None
+
+
 def copy_rates(torch, h_src, d_dst, h_dst, d_src, reps=3):
     """Host-link throughput with the caller's pinned buffers: best of `reps`
     host-to-device copies of h_src into d_dst and device-to-host copies of
@@ -623,12 +651,10 @@ def run_fp64(args, fmm, f, dev, world, rank, barrier, max_over_ranks):
     ms = max_over_ranks(total / args.steps)
     value = world * flops / (ms / 1e3) / 1e12
     # end to end through the host-buffer drop-in (fmm_gpu_strassen_ab_ex, bli_strassen_ab_ex's replacement) with
-    # pinned host operands: every call uploads A, B and C and reads C back
+    # pinned host operands (fmm_gpu_host_alloc): every call uploads A, B and C and reads C back
     e2e = None
     if rank == 0 and args.e2e_steps > 0:
-        hA = torch.empty((n, n), dtype=torch.float64, pin_memory=True).t()
-        hB = torch.empty((n, n), dtype=torch.float64, pin_memory=True).t()
-        hC = torch.empty((n, n), dtype=torch.float64, pin_memory=True).t()
+        hA, hB, hC = (host_operand(torch, fmm, n) for _ in range(3))
         hA.copy_(A)
         hB.copy_(B)
         hC.copy_(C0)
@@ -651,6 +677,7 @@ def run_fp64(args, fmm, f, dev, world, rank, barrier, max_over_ranks):
         e2e = {"value": flops / ms_e2e / 1e9, "unit": "TFLOP/s", "h2d_bytes_per_step": 3 * op,
                "d2h_bytes_per_step": op, "ms_per_step": ms_e2e,
                "call": "fmm_gpu_strassen_ab_ex (host buffers; device buffers kept between calls)",
+               "host_buffers": "fmm_gpu_host_alloc (pinned, huge pages)",
                "link": {**link, "serial_copies_ms": 3 * op / link["h2d_gbs"] / 1e6 + op / link["d2h_gbs"] / 1e6},
                "clocks": clk_e2e.summary()}
         if levels != 1:
@@ -821,12 +848,10 @@ def main():
                 "products_per_launch": gemm_products / max(gemm_n, 1)}
 
     # end to end through the host-buffer C-ABI call (fmm_gpu_split_strassen_ab_ex)
-    # with pinned host operands: every step uploads A, B and C and reads C back
+    # with pinned host operands (fmm_gpu_host_alloc): every step uploads A, B and C and reads C back
     e2e = None
     if rank == 0 and args.e2e_steps > 0:
-        hA = torch.empty((n, n), dtype=torch.float64, pin_memory=True).t()
-        hB = torch.empty((n, n), dtype=torch.float64, pin_memory=True).t()
-        hC = torch.empty((n, n), dtype=torch.float64, pin_memory=True).t()
+        hA, hB, hC = (host_operand(torch, fmm, n) for _ in range(3))
         hA.copy_(A)
         hB.copy_(B)
         hC.copy_(C0)
@@ -854,12 +879,14 @@ def main():
         e2e = {"value": flops / ms_e2e / 1e9, "unit": "TFLOP/s", "h2d_bytes_per_step": 3 * n * n * 8,
                "d2h_bytes_per_step": n * n * 8, "ms_per_step": ms_e2e,
                "call": "fmm_gpu_split_strassen_ab_ex (host buffers, copies overlapped with the device work)",
+               "host_buffers": "fmm_gpu_host_alloc (pinned, huge pages)",
                "link": {**link,
                         "serial_copies_ms": 3 * op_bytes / link["h2d_gbs"] / 1e6 + op_bytes / link["d2h_gbs"] / 1e6,
                         "upload_A_B_ms": up_ab,
                         # the call cannot start the GEMM before A and B are up, nor finish before C's last
                         # column chunk (1/8 of C) is down
                         "overlap_floor_ms": up_ab + ms + op_bytes / 8 / link["d2h_gbs"] / 1e6},
+               "host_huge_page_share": huge_page_share([hA, hB, hC]),
                "timeline_ms": timeline,
                "clocks": clk_e2e.summary()}
 

@@ -117,6 +117,10 @@ def lib() -> ctypes.CDLL:
                                                 FmmT, ci, ci, ci]
     L.fmm_gpu_release_host_buffers.restype = None
     L.fmm_gpu_release_host_buffers.argtypes = []
+    L.fmm_gpu_host_alloc.restype = ci
+    L.fmm_gpu_host_alloc.argtypes = [ctypes.c_size_t, ctypes.POINTER(ctypes.c_void_p)]
+    L.fmm_gpu_host_free.restype = ci
+    L.fmm_gpu_host_free.argtypes = [ctypes.c_void_p]
     L.fmm_gpu_strassen_ab.restype = ci
     L.fmm_gpu_strassen_ab.argtypes = [dbl, vp, i64, vp, i64, dbl, vp, i64, i64, i64, i64]
     L.fmm_gpu_split_workspace_size.restype = ctypes.c_size_t
@@ -511,6 +515,24 @@ def read_host_timeline() -> dict:
 def release_host_buffers() -> None:
     """Frees the device buffers kept by split_strassen_ab_ex on this device."""
     lib().fmm_gpu_release_host_buffers()
+
+
+def host_empty(rows: int, cols: int):
+    """A zeroed Fortran-order float64 numpy array of rows x cols in pinned
+    host memory on huge pages (fmm_gpu_host_alloc), for the operands of the
+    host-buffer calls; freed when the array (and every view of it, e.g.
+    torch.from_numpy) is gone. Needs a GPU."""
+    import weakref
+
+    import numpy as np
+
+    nbytes = max(rows * cols * 8, 8)
+    p = ctypes.c_void_p()
+    _check(lib().fmm_gpu_host_alloc(nbytes, ctypes.byref(p)), "fmm_gpu_host_alloc")
+    buf = (ctypes.c_double * max(rows * cols, 1)).from_address(p.value)
+    arr = np.ctypeslib.as_array(buf)[: rows * cols].reshape((rows, cols), order="F")
+    weakref.finalize(arr, lib().fmm_gpu_host_free, p.value)
+    return arr
 
 
 def bli_strassen_ab_ex(alpha: float, A, B, beta: float, C, fmm: FmmT) -> None:

