@@ -176,53 +176,82 @@ def host_operands(n, seed=7):
             for _ in range(3)]
 
 
-def cpu_reference(alg, levels, n, target_s, arrays=None):
-    """The reference FMM algorithm (oracle, FP64) on the host cores: a bounded
-    sample of the products of the flattened algorithm at the full shape.
-    Returns (eff TFLOP/s extrapolated to all products, dict)."""
+def cpu_reference_plan(alg, levels, n, target_s, arrays):
+    """How many products of the flattened algorithm make a host-core sample of
+    about target_s seconds at the full shape (one product timed first)."""
     import oracle
     from oracle import coeffs as oc
 
     flat = oc.power(oc.read(COEFFS / f"{alg}.txt"), levels)
     R = flat[3]
     oracle.set_threads(os.cpu_count() or 1)
-    A, B, C = arrays if arrays is not None else host_operands(n)
+    A, B, C = arrays
     t0 = time.perf_counter()
     oracle.fmm_dgemm(flat, A, B, C, r_begin=0, r_end=1)
     t1 = time.perf_counter() - t0
-    P = max(1, min(R, int(target_s / max(t1, 1e-3))))
+    return flat, max(1, min(R, int(target_s / max(t1, 1e-3)))), R
+
+
+def cpu_reference_sample(flat, P, arrays):
+    """Seconds for products 0..P-1 of the reference FMM algorithm (oracle,
+    FP64) on the host cores at the full shape."""
+    import oracle
+
+    A, B, C = arrays
     t0 = time.perf_counter()
     oracle.fmm_dgemm(flat, A, B, C, r_begin=0, r_end=P)
-    tp = time.perf_counter() - t0
+    return time.perf_counter() - t0
+
+
+def cpu_reference(alg, levels, n, target_s, arrays=None):
+    """The reference FMM algorithm (oracle, FP64) on the host cores: a bounded
+    sample of the products of the flattened algorithm at the full shape.
+    Returns (eff TFLOP/s of the sample: its share P/R of 2n^3 over its time,
+    dict)."""
+    import oracle
+
+    arrays = arrays if arrays is not None else host_operands(n)
+    flat, P, R = cpu_reference_plan(alg, levels, n, target_s, arrays)
+    tp = cpu_reference_sample(flat, P, arrays)
     eff = 2.0 * n ** 3 * (P / R) / tp / 1e12
     info = {"cores": oracle.num_threads(), "products": P, "of": R, "seconds": tp}
     return eff, info
 
 
 def run_reference(args):
+    """The reference arm: each step is a bounded sample of the workload on the
+    host cores (products 0..P-1 of the R products of the FMM step at the full
+    shape, P sized to a few seconds), timed; value = the sample's effective
+    flops (its share P/R of 2mnk) over its time, ms_per_step = that time."""
+    import oracle
+
     world, rank, _ = dist_setup()
     if rank != 0:
         return
     steps, warm = args.steps, args.warmup
     per_step = max(2.0, 60.0 / max(steps + warm, 1))
-    vals = []
-    info = None
     arrays = host_operands(args.n)
+    flat, P, R = cpu_reference_plan(args.alg, args.levels, args.n, per_step, arrays)
+    secs = []
     for i in range(warm + steps):
-        v, info = cpu_reference(args.alg, args.levels, args.n, per_step, arrays)
+        t = cpu_reference_sample(flat, P, arrays)
         if i >= warm:
-            vals.append(v)
-    value = statistics.median(vals)
-    sample = (f"FP64 FMM {args.alg} x{args.levels} levels at m=n=k={args.n}: products 0..{info['products']} "
-              f"of {info['of']} per step ({info['seconds']:.1f} s), extrapolated to all products")
+            secs.append(t)
+    t_step = statistics.median(secs)
+    sample_flops = 2.0 * args.n ** 3 * P / R
+    value = sample_flops / t_step / 1e12
+    cores = oracle.num_threads()
+    sample = (f"FP64 FMM {args.alg} x{args.levels} levels at m=n=k={args.n}: products 0..{P - 1} of {R} per step "
+              f"({t_step:.2f} s; {P}/{R} of the step's 2mnk)")
     out = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": args.gpus,
-        "steps": steps, "warmup": warm, "ms_per_step": 2.0 * args.n ** 3 / (value * 1e12) * 1e3,
+        "steps": steps, "warmup": warm, "ms_per_step": t_step * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"FMM {args.alg} x{args.levels} levels, m=n=k={args.n} (reference algorithm, FP64, host cores)",
-                   "m": args.n, "n": args.n, "k": args.n, "alg": args.alg, "levels": args.levels},
-        "cpu_baseline": {"value": value, "unit": "TFLOP/s", "cores": info["cores"], "kind": "port",
-                         "sample": sample},
+        "config": {"workload": f"FMM {args.alg} x{args.levels} levels, m=n=k={args.n} (reference algorithm, FP64, host "
+                               f"cores), a sample of {P} of its {R} products per step",
+                   "m": args.n, "n": args.n, "k": args.n, "alg": args.alg, "levels": args.levels,
+                   "sample_products": P, "products": R},
+        "cpu_baseline": {"value": value, "unit": "TFLOP/s", "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out))
@@ -926,8 +955,8 @@ def main():
         eff, info = cpu_reference(args.alg, levels, n, 15.0,
                                   [np.asfortranarray(X.cpu().numpy()) for X in (A, B, C0)])
         cpu = {"value": eff, "unit": "TFLOP/s", "cores": info["cores"], "kind": "port",
-               "sample": (f"oracle FP64 FMM {args.alg} x{levels} at m=n=k={n}: products 0..{info['products']} "
-                          f"of {info['of']} ({info['seconds']:.1f} s), extrapolated")}
+               "sample": (f"oracle FP64 FMM {args.alg} x{levels} at m=n=k={n}: products 0..{info['products'] - 1} "
+                          f"of {info['of']} ({info['seconds']:.1f} s; value = their share of 2mnk over that time)")}
 
     served = None
     if rank == 0 and args.serve_seconds > 0:

@@ -586,6 +586,11 @@ extern "C" int fmm_gpu_host_alloc(size_t bytes, void** ptr)
     if (align == hp) madvise(p, len, MADV_HUGEPAGE);
 #endif
     memset(p, 0, len);
+    /* where the first touch fell back to small pages (no free huge page at
+     * fault time), ask the kernel to collapse the range now (Linux 6.1+;
+     * MADV_COLLAPSE, 25, compacts memory to find huge pages; an older kernel
+     * refuses it and the small pages stay) */
+    if (align == hp) madvise(p, len, 25);
     if (cudaHostRegister(p, len, cudaHostRegisterDefault) != cudaSuccess) {
         cudaGetLastError();
         munmap(base, map_len);
