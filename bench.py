@@ -912,9 +912,10 @@ def main():
                "link": {**link,
                         "serial_copies_ms": 3 * op_bytes / link["h2d_gbs"] / 1e6 + op_bytes / link["d2h_gbs"] / 1e6,
                         "upload_A_B_ms": up_ab,
-                        # the call cannot start the GEMM before A and B are up, nor finish before C's last
-                        # column chunk (1/8 of C) is down
-                        "overlap_floor_ms": up_ab + ms + op_bytes / 8 / link["d2h_gbs"] / 1e6},
+                        # the call's GEMM starts once A and the first half of B's columns are up, and the call
+                        # ends once C's last column chunk (1/8 of C) is down after the GEMM
+                        "before_gemm_ms": 1.5 * op_bytes / link["h2d_gbs"] / 1e6,
+                        "after_gemm_ms": op_bytes / 8 / link["d2h_gbs"] / 1e6},
                "host_huge_page_share": huge_page_share([hA, hB, hC]),
                "timeline_ms": timeline,
                "clocks": clk_e2e.summary()}

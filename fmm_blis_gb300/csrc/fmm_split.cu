@@ -1956,6 +1956,7 @@ struct SidePool {
     cudaEvent_t wave_sc[2][kWaveStreams];   /* a workspace half's C updates done */
     cudaEvent_t gate[3];   /* host-buffer calls: A, B and C on the device */
     cudaEvent_t chunk[16]; /* host-buffer calls: B chunks in, C chunks out */
+    cudaEvent_t half[4];   /* host-buffer calls: B slices of a column half packed, its GEMM done */
     cudaEvent_t tl[kTimelinePoints + 1];  /* host-buffer calls: the call's timeline (timing events) */
     cudaStream_t hi;       /* greatest priority: GEMMs that side work runs beside */
 };
@@ -1979,6 +1980,7 @@ SidePool* side_pool()
     for (int i = 0; i < 3 && ok; ++i) ok = cudaEventCreateWithFlags(&p->gate[i], cudaEventDisableTiming) == cudaSuccess;
     for (int i = 0; i <= kTimelinePoints && ok; ++i) ok = cudaEventCreate(&p->tl[i]) == cudaSuccess;
     for (int i = 0; i < 16 && ok; ++i) ok = cudaEventCreateWithFlags(&p->chunk[i], cudaEventDisableTiming) == cudaSuccess;
+    for (int i = 0; i < 4 && ok; ++i) ok = cudaEventCreateWithFlags(&p->half[i], cudaEventDisableTiming) == cudaSuccess;
     for (int h = 0; h < 2 && ok; ++h) {
         ok = cudaEventCreateWithFlags(&p->wave_gm[h], cudaEventDisableTiming) == cudaSuccess;
         for (int i = 0; i < kWaveStreams && ok; ++i)
@@ -2216,6 +2218,42 @@ static int job_gemm(const SplitJob& j, int np, cudaStream_t st)
     return FMM_OK;
 }
 
+/* job_gemm restricted to the tile columns [jt0, jt1) of every product: the
+ * B slice map starts jt0 * 256 rows further and Z jt0 * 256 columns
+ * further, with the same row strides, so each (product, tile) item computes
+ * exactly what the full launch computes for it. */
+static int job_gemm_cols(const SplitJob& j, int np, int64_t jt0, int64_t jt1, cudaStream_t st)
+{
+    const bool pair = job_pair(j);
+    const int64_t tn = jt1 - jt0;
+    if (tn <= 0) return FMM_OK;
+    const int64_t tiles_m = j.d.m_pad / (pair ? kPairTileM : kTileM);
+    const int64_t tiles = tiles_m * tn;
+    const int64_t units = pair ? 76 : 152;
+    int K = (int)std::min<int64_t>(np, std::max<int64_t>(1, (24 * units + tiles - 1) / tiles));
+    const int nl = (np + K - 1) / K;
+    K = (np + nl - 1) / nl;
+    const size_t esz = j.fmt ? 1 : 2;
+    GemmLaunch gl;
+    for (int r = 0; r < np; r += K) {
+        const int cnt = std::min(K, np - r);
+        memset(&gl, 0, sizeof(gl));
+        gl.nprob = 1;
+        gl.sched = (unsigned int*)(j.w + j.L.sched);
+        GemmProblem& gp = gl.prob[0];
+        if (int rc = job_fill(j, gp, cnt, 0, pair, r); rc != FMM_OK) return rc;
+        const int64_t c0 = jt0 * kTileN;
+        const uint8_t* sb = j.w + j.L.sb + ((size_t)r * j.s * j.d.n_pad + (size_t)c0) * j.d.k_pad * esz;
+        if (make_slice_map(&gp.tmB, sb, j.d.k_pad, (int64_t)cnt * j.s * j.d.n_pad - c0, pair ? kTileN / 2 : kTileN,
+                           j.fmt) != FMM_OK)
+            return FMM_ERR_CUDA;
+        gp.Z += c0 * j.d.m_pad;
+        gp.tiles_n = (int)tn;
+        if (int rc = launch_gemm(gl, (int64_t)cnt * tiles, cnt, st, pair); rc != FMM_OK) return rc;
+    }
+    return FMM_OK;
+}
+
 /* blocks of the grid-stride element-major scatter: one per T elements, at
  * most 16 per SM (each then serves several elements) */
 static unsigned scatter_blocks(uint64_t elems, int T)
@@ -2238,11 +2276,18 @@ static bool job_scatter_all(const SplitJob& j, int r0, int np, int* T_out, size_
 
 /* the C updates of products [r0, r0 + np) for the product-grid columns
  * [j0, j1) (all rows), element-major form only */
-static void job_scatter_cols(const SplitJob& j, int r0, int np, int64_t j0, int64_t j1, cudaStream_t st)
+static void job_scatter_cols(const SplitJob& j, int r0, int np, int64_t j0, int64_t j1, cudaStream_t st,
+                             bool small = false)
 {
     int T;
     size_t smem;
     job_scatter_all(j, r0, np, &T, &smem);
+    if (small && T > 128) {   /* 128-thread blocks fit on an SM beside a resident GEMM CTA */
+        const Tab ht = tab_view(j.alg.htab);
+        const int P = j.alg.mt * j.alg.nt, E = ht.w_off[r0 + np] - ht.w_off[r0];
+        T = 128;
+        smem = (size_t)P * T * 8 + (size_t)E * 12 + (size_t)(np + 1) * 4;
+    }
     const uint64_t first = (uint64_t)j0 * (uint64_t)j.d.me, end = (uint64_t)j1 * (uint64_t)j.d.me;
     if (end <= first) return;
     scatter_all_kernel<<<scatter_blocks(end - first, T), (unsigned)T, smem, st>>>(
@@ -2499,15 +2544,34 @@ int fmm_split_host(const AlgView& alg, int64_t m, int64_t n, int64_t k, double a
         mark(1, cs);
         if ((rc = job_maxima_a(j, st)) != FMM_OK) return rc;
         if (one_group) job_pack_a(j, 0, alg.R, st);
-        /* B in kChunks chunks of T_r columns [j0, j1): chunk x holds the B
-         * columns co_c + [j0, j1) of every column part c, and the B side of
-         * those columns (maxima; with one group, exponents and slices) runs
-         * on s[0] as soon as the chunk has arrived */
+        /* B in chunks of T_r columns [j0, j1): chunk x holds the B columns
+         * co_c + [j0, j1) of every column part c, and the B side of those
+         * columns (maxima; with one group, exponents and slices) runs on s[0]
+         * as soon as the chunk has arrived. With one product group and the
+         * element-major C update, the GEMM runs in two halves of tile
+         * columns: the first half starts once the B slices of its columns
+         * are formed, and its C columns are updated and read back while the
+         * second half is computed. */
         const int64_t ne = j.d.ne, n_pad = j.d.n_pad;
-        const int64_t W = (ne + kChunks * 32 - 1) / (kChunks * 32) * 32;
+        const int64_t tiles_n = n_pad / kTileN, th = (tiles_n + 1) / 2, js = th * kTileN;
+        int Tchk;
+        size_t smchk;
+        const bool halves = one_group && tiles_n >= 2 && job_scatter_all(j, 0, alg.R, &Tchk, &smchk);
+        std::vector<std::pair<int64_t, int64_t>> bch;
+        if (halves) {
+            /* four chunks per half, multiples of 32 columns */
+            for (int h = 0; h < 2; ++h) {
+                const int64_t a = h ? js : 0, b = h ? n_pad : js;
+                const int64_t w = round_up((b - a + 3) / 4, 32);
+                for (int64_t c0 = a; c0 < b; c0 += w) bch.emplace_back(c0, std::min(c0 + w, b));
+            }
+        } else {
+            const int64_t W = (ne + kChunks * 32 - 1) / (kChunks * 32) * 32;
+            for (int64_t j0 = 0; j0 < n_pad; j0 += W) bch.emplace_back(j0, std::min(j0 + W, n_pad));
+        }
         int x = 0;
-        for (int64_t j0 = 0; j0 < n_pad; j0 += W, ++x) {
-            const int64_t j1 = std::min(j0 + W, n_pad);
+        for (const auto& ch : bch) {
+            const int64_t j0 = ch.first, j1 = ch.second;
             for (int c = 0; c < nt; ++c) {
                 int64_t co, cl;
                 fmm_part_geom(n, nt, c, &co, &cl);
@@ -2524,6 +2588,64 @@ int fmm_split_host(const AlgView& alg, int64_t m, int64_t n, int64_t k, double a
                 job_maxima_b(j, sb, co + std::min(j0, cl), co + std::min(j1, cl));
             }
             if (one_group) job_pack_b_cols(j, 0, alg.R, j0, j1, sb);
+            if (halves && (j1 == js || j1 == n_pad) && !ok(cudaEventRecord(sp->half[j1 == js ? 0 : 1], sb)))
+                return FMM_ERR_CUDA;
+            ++x;
+        }
+        if (halves) {
+            cudaStream_t ss = sp->s[3];
+            mark(2, cs);
+            /* C up behind B, then C := beta*C, on s[3] */
+            if (beta != 0.0 &&
+                (!ok(fmm_copy2d_async(dC, row, C, sizeof(double) * ldc, row, n, cudaMemcpyHostToDevice, cs)) ||
+                 !ok(cudaEventRecord(sp->gate[2], cs)) || !ok(cudaStreamWaitEvent(ss, sp->gate[2], 0))))
+                return FMM_ERR_CUDA;
+            if ((rc = fmm_scale_c(m, n, beta, dC, m, ss)) != FMM_OK) return rc;
+            for (int h = 0; h < 2; ++h) {
+                if (!ok(cudaStreamWaitEvent(st, sp->half[h], 0))) return FMM_ERR_CUDA;
+                if (h == 0) mark(3, st);
+                if ((rc = job_gemm_cols(j, alg.R, h ? th : 0, h ? tiles_n : th, st)) != FMM_OK) return rc;
+                if (!ok(cudaEventRecord(sp->half[2 + h], st))) return FMM_ERR_CUDA;
+            }
+            mark(4, st);
+            /* per half, the C updates of its product-grid columns in four
+             * column chunks on s[3] (beside the second half's GEMM: 128-thread
+             * blocks), each chunk's C columns read back on s[1] */
+            x = 0;
+            for (int h = 0; h < 2; ++h) {
+                if (!ok(cudaStreamWaitEvent(ss, sp->half[2 + h], 0))) return FMM_ERR_CUDA;
+                const int64_t a0 = h ? js : 0, b0 = h ? ne : std::min(js, ne);
+                const int64_t w = std::max<int64_t>((b0 - a0 + 3) / 4, 1);
+                for (int64_t j0 = a0; j0 < b0; j0 += w, ++x) {
+                    const int64_t j1 = std::min(j0 + w, b0);
+                    job_scatter_cols(j, 0, alg.R, j0, j1, ss, h == 0);
+                    if (!ok(cudaEventRecord(sp->chunk[kChunks + x], ss)) ||
+                        !ok(cudaStreamWaitEvent(cs, sp->chunk[kChunks + x], 0)))
+                        return FMM_ERR_CUDA;
+                    for (int c = 0; c < nt; ++c) {
+                        int64_t co, cl;
+                        fmm_part_geom(n, nt, c, &co, &cl);
+                        const int64_t a = co + std::min(j0, cl), b = co + std::min(j1, cl);
+                        if (b > a && !ok(fmm_copy2d_async(C + a * ldc, sizeof(double) * ldc, dC + a * m, row, row,
+                                                           b - a, cudaMemcpyDeviceToHost, cs)))
+                            return FMM_ERR_CUDA;
+                    }
+                }
+            }
+            mark(5, cs);
+            if (!ok(cudaStreamSynchronize(cs)) || !ok(cudaStreamSynchronize(st)) || !ok(cudaStreamSynchronize(ss)))
+                return FMM_ERR_CUDA;
+            if (tline) {
+                std::lock_guard<std::mutex> lk(g_timeline_mu);
+                for (int y = 1; y <= kTimelinePoints; ++y) {
+                    float t = 0.f;
+                    cudaEventElapsedTime(&t, sp->tl[0], sp->tl[y]);
+                    g_timeline_ms[y - 1] = t;
+                }
+                g_timeline_ms[kTimelinePoints] =
+                    std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - host_t0).count();
+            }
+            return cudaGetLastError() == cudaSuccess ? fmm_device_error_status() : FMM_ERR_CUDA;
         }
         mark(2, cs);
         for (int r0 = 0; r0 < alg.R; r0 += G) {

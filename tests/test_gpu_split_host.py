@@ -163,3 +163,29 @@ def test_host_alloc_buffers(fmm, torch_cuda):
     del hA, hB, hC, tC, big
     gc.collect()
     assert fmm.take_device_error() == 0
+
+
+@pytest.mark.parametrize("levels,shape,alpha,beta", [(1, (517, 1033, 700), 1.5, 0.5), (2, (1037, 1033, 411), 1.0, 0.0),
+                                                     (0, (300, 2311, 257), -1.0, 2.0)])
+def test_host_call_gemm_halves(fmm, torch_cuda, levels, shape, alpha, beta):
+    """Product grids of at least two 256-column tiles run the GEMM in two
+    halves of tile columns, the first half's C columns updated and read back
+    during the second (uneven halves: 517 / 3 and 259 / 2 columns of the
+    product grid; leading dimensions larger than the row counts): the device
+    call's bits."""
+    m, n, k = shape
+    A, B, C = rand(m, k, 551), rand(k, n, 552), rand(m, n, 553)
+    f = fmm.strassen_fmm() if levels else None
+    want = device_call(fmm, f, levels, A, B, C, 6, "bf16", alpha, beta)
+    Ab = np.zeros((m + 3, k), order="F"); Ab[:m] = A
+    Cb = np.full((m + 7, n), 5.0, order="F"); Cb[:m] = C
+    L = fmm.lib()
+    st = L.fmm_gpu_split_strassen_ab_ex(alpha, Ab.ctypes.data, m + 3, B.ctypes.data, k, beta, Cb.ctypes.data, m + 7,
+                                        m, n, k, f if f is not None else fmm.FmmT(), levels, 6, 0)
+    assert st == 0
+    assert np.array_equal(Cb[:m], want)
+    assert np.all(Cb[m:] == 5.0)
+    got = C.copy(order="F")
+    fmm.split_strassen_ab_ex(alpha, A, B, beta, got, f, levels, 6)
+    assert np.array_equal(got, want)
+    assert fmm.take_device_error() == 0
