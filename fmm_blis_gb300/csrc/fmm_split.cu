@@ -267,11 +267,11 @@ __host__ __device__ __forceinline__ Tab tab_view(const int* tab)
  * pattern of a non-negative double, which orders like the value). */
 __device__ __forceinline__ void amax_body(const double* __restrict__ A, int64_t lda, int64_t m, int64_t k, int kt,
                                           unsigned long long* __restrict__ amax, int cols_per_block, int64_t bx,
-                                          int by, int64_t bz)
+                                          int by, int64_t bz, int64_t i_first = 0, int64_t i_end = -1)
 {
-    const int64_t i = bx * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t i = i_first + bx * (int64_t)blockDim.x + threadIdx.x;
     const int b = by;
-    if (i >= m) return;
+    if (i >= (i_end < 0 ? m : i_end)) return;
     int64_t co, cl;
     fmm_part_geom(k, kt, b, &co, &cl);
     const int64_t c0 = bz * cols_per_block;
@@ -298,10 +298,12 @@ __device__ __forceinline__ void amax_body(const double* __restrict__ A, int64_t 
     atomicMax(&amax[(int64_t)b * m + i], mx);
 }
 
+/* the rows [i_first, i_end) of A */
 __global__ void amax_kernel(const double* __restrict__ A, int64_t lda, int64_t m, int64_t k,
-                            int kt, unsigned long long* __restrict__ amax, int cols_per_block)
+                            int kt, unsigned long long* __restrict__ amax, int cols_per_block, int64_t i_first,
+                            int64_t i_end)
 {
-    amax_body(A, lda, m, k, kt, amax, cols_per_block, blockIdx.x, blockIdx.y, blockIdx.z);
+    amax_body(A, lda, m, k, kt, amax, cols_per_block, blockIdx.x, blockIdx.y, blockIdx.z, i_first, i_end);
 }
 
 /* bmax[b*n + j] = max over the rows of k-block b of |B[:, j]| for the columns
@@ -456,7 +458,7 @@ template <int S, int DB, int ROWS>
 __device__ __forceinline__ void pack_a_body(const int* __restrict__ tab, int r0, int np, const double* __restrict__ A,
                                             int64_t lda, int64_t m, int64_t k, int64_t m_pad, int64_t k_pad,
                                             const int* __restrict__ e_row, uint8_t* __restrict__ sa, int64_t bx,
-                                            int64_t by)
+                                            int64_t by, int64_t i_first = 0)
 {
     __shared__ double Sf[64][ROWS + 1];
     __shared__ PEnt ent[kPackMaxEnt];
@@ -464,7 +466,7 @@ __device__ __forceinline__ void pack_a_body(const int* __restrict__ tab, int r0,
     const int64_t me = (m + t.mt - 1) / t.mt, ke = (k + t.kt - 1) / t.kt;
     const int q = (int)(bx % np);
     const int r = r0 + q;
-    const int64_t i0 = (bx / np) * ROWS, p0 = by * 64;
+    const int64_t i0 = i_first + (bx / np) * ROWS, p0 = by * 64;
     e_row += (int64_t)q * m_pad;
     const int64_t slice0 = (int64_t)q * S * m_pad * k_pad;   /* element offset of this product */
     const int eb = t.u_off[r], ne_ = t.u_off[r + 1] - eb;
@@ -536,9 +538,9 @@ template <int S, int DB, int ROWS>
 __global__ void __launch_bounds__(ROWS * 4, ROWS == 64 ? 4 : 8)
 pack_a_kernel(const int* __restrict__ tab, int r0, int np, const double* __restrict__ A, int64_t lda,
               int64_t m, int64_t k, int64_t m_pad, int64_t k_pad,
-              const int* __restrict__ e_row, uint8_t* __restrict__ sa)
+              const int* __restrict__ e_row, uint8_t* __restrict__ sa, int64_t i_first)
 {
-    pack_a_body<S, DB, ROWS>(tab, r0, np, A, lda, m, k, m_pad, k_pad, e_row, sa, blockIdx.x, blockIdx.y);
+    pack_a_body<S, DB, ROWS>(tab, r0, np, A, lda, m, k, m_pad, k_pad, e_row, sa, blockIdx.x, blockIdx.y, i_first);
 }
 
 /* B side, all products of a group: CTA (q, tile) forms the tile of COLS
@@ -616,9 +618,11 @@ pack_b_kernel(const int* __restrict__ tab, int r0, int np, const double* __restr
 }
 
 /* Which packs a launch_packs call issues: both sides, or one side only; the
+ * A side over the S_r rows [ia0, ia1) (multiples of 64, or ia1 = m_pad), the
  * B side over the T_r columns [jb0, jb1) (multiples of 32, or jb1 = n_pad). */
 struct PackSel {
     bool a = true, b = true;
+    int64_t ia0 = 0, ia1 = -1;
     int64_t jb0 = 0, jb1 = -1;
     bool small = false;   /* the 128-thread tiles that fit beside a resident GEMM CTA */
 };
@@ -629,11 +633,13 @@ void launch_packs_t(const int* tab, int r, int np, const double* A, int64_t lda,
                     const int* e_row, const int* f_col, uint8_t* sa, uint8_t* sb, cudaStream_t st,
                     cudaStream_t st_b, const PackSel& sel)
 {
-    const dim3 ka((unsigned)(np * (m_pad / (sel.small ? 32 : 64))), (unsigned)(k_pad / 64));
-    if (sel.a && sel.small)
-        pack_a_kernel<S, DB, 32><<<ka, 128, 0, st>>>(tab, r, np, A, lda, m, k, m_pad, k_pad, e_row, sa);
-    else if (sel.a)
-        pack_a_kernel<S, DB, 64><<<ka, 256, 0, st>>>(tab, r, np, A, lda, m, k, m_pad, k_pad, e_row, sa);
+    const int64_t i1 = sel.ia1 < 0 ? m_pad : sel.ia1;
+    const int rows = sel.small ? 32 : 64;
+    const dim3 ka((unsigned)(np * ((i1 - sel.ia0 + rows - 1) / rows)), (unsigned)(k_pad / 64));
+    if (sel.a && i1 > sel.ia0 && sel.small)
+        pack_a_kernel<S, DB, 32><<<ka, 128, 0, st>>>(tab, r, np, A, lda, m, k, m_pad, k_pad, e_row, sa, sel.ia0);
+    else if (sel.a && i1 > sel.ia0)
+        pack_a_kernel<S, DB, 64><<<ka, 256, 0, st>>>(tab, r, np, A, lda, m, k, m_pad, k_pad, e_row, sa, sel.ia0);
     const int64_t j1 = sel.jb1 < 0 ? n_pad : sel.jb1;
     if (!sel.b || j1 <= sel.jb0) return;
     const int cols = sel.small ? 16 : 32;
@@ -1448,14 +1454,15 @@ scatter_kernel(const int* __restrict__ tab, int r0, int nprod, int64_t m, int64_
 }
 
 /* one element (i, j) of the product grid for scatter_all_kernel */
-__device__ __forceinline__ void scatter_all_element(uint64_t idx, uint32_t me, int P, int T, int tid, int nprod,
+__device__ __forceinline__ void scatter_all_element(uint64_t idx, uint32_t rows, uint32_t i_lo, int P, int T, int tid,
+                                                    int nprod,
                                                     int m_pad, int n_pad, int ebase, const int (&geo)[4][64],
                                                     double* cs, const double* lam, const int* pidx, const int* off,
                                                     const int64_t* __restrict__ Z, const int* __restrict__ e_row,
                                                     const int* __restrict__ f_col, double* __restrict__ C,
                                                     int64_t ldc)
 {
-    const int i = (int)((uint32_t)idx % me), j = (int)((uint32_t)idx / me);
+    const int i = (int)(i_lo + (uint32_t)idx % rows), j = (int)((uint32_t)idx / rows);
     uint64_t live = 0;
     for (int p = 0; p < P; ++p) {
         if (i < geo[1][p] && j < geo[3][p]) {
@@ -1514,7 +1521,8 @@ __device__ __forceinline__ void scatter_all_body(const int* __restrict__ tab, in
                                                  int m_pad, int n_pad, int ebase, double alpha,
                                                  const int64_t* __restrict__ Z, const int* __restrict__ e_row,
                                                  const int* __restrict__ f_col, double* __restrict__ C, int64_t ldc,
-                                                 uint64_t idx_first, uint64_t idx_end, uint64_t vb, uint64_t vg)
+                                                 uint64_t idx_first, uint64_t idx_end, uint64_t vb, uint64_t vg,
+                                                 uint32_t i_lo = 0, uint32_t i_rows = 0)
 {
     extern __shared__ double sm_all[];
     __shared__ int geo[4][64];           /* per sub-block p: ro, rl, co, cl */
@@ -1536,23 +1544,26 @@ __device__ __forceinline__ void scatter_all_body(const int* __restrict__ tab, in
     }
     __syncthreads();
     const uint32_t me = (uint32_t)((m + t.mt - 1) / t.mt), ne = (uint32_t)((n + t.nt - 1) / t.nt);
-    /* me * ne < 2^32 (checked on the host), so the element index fits 32 bits */
+    /* the product-grid rows [i_lo, i_lo + rows) of every column, element
+     * index (i - i_lo) + j * rows (all rows when i_rows is 0); rows * ne <
+     * 2^32 (checked on the host), so the element index fits 32 bits */
+    const uint32_t rows = i_rows ? i_rows : me;
     const uint64_t idx = idx_first + vb * (uint64_t)T + (uint64_t)tid;
-    const uint64_t end = idx_end < (uint64_t)me * (uint64_t)ne ? idx_end : (uint64_t)me * (uint64_t)ne;
+    const uint64_t end = idx_end < (uint64_t)rows * (uint64_t)ne ? idx_end : (uint64_t)rows * (uint64_t)ne;
     /* grid-stride: a block's set-up above serves many elements */
     for (uint64_t idx2 = idx; idx2 < end; idx2 += vg * (uint64_t)T)
-        scatter_all_element(idx2, me, P, T, tid, nprod, m_pad, n_pad, ebase, geo, cs, lam, pidx, off, Z, e_row,
-                            f_col, C, ldc);
+        scatter_all_element(idx2, rows, i_lo, P, T, tid, nprod, m_pad, n_pad, ebase, geo, cs, lam, pidx, off, Z,
+                            e_row, f_col, C, ldc);
 }
 
 __global__ void __launch_bounds__(256)
 scatter_all_kernel(const int* __restrict__ tab, int r0, int nprod, int64_t m, int64_t n,
                    int m_pad, int n_pad, int ebase, double alpha, const int64_t* __restrict__ Z,
                    const int* __restrict__ e_row, const int* __restrict__ f_col, double* __restrict__ C,
-                   int64_t ldc, uint64_t idx_first, uint64_t idx_end)
+                   int64_t ldc, uint64_t idx_first, uint64_t idx_end, uint32_t i_lo, uint32_t i_rows)
 {
     scatter_all_body(tab, r0, nprod, m, n, m_pad, n_pad, ebase, alpha, Z, e_row, f_col, C, ldc, idx_first, idx_end,
-                     blockIdx.x, gridDim.x);
+                     blockIdx.x, gridDim.x, i_lo, i_rows);
 }
 
 
@@ -1955,8 +1966,8 @@ struct SidePool {
     cudaEvent_t wave_gm[2];                 /* a workspace half's GEMM done */
     cudaEvent_t wave_sc[2][kWaveStreams];   /* a workspace half's C updates done */
     cudaEvent_t gate[3];   /* host-buffer calls: A, B and C on the device */
-    cudaEvent_t chunk[16]; /* host-buffer calls: B chunks in, C chunks out */
-    cudaEvent_t half[4];   /* host-buffer calls: B slices of a column half packed, its GEMM done */
+    cudaEvent_t chunk[32]; /* host-buffer calls: B chunks in (0..7), C chunks out (8..31) */
+    cudaEvent_t blk[10];   /* host-buffer calls, blocked schedule: A halves up, A and B halves packed, GEMM blocks done */
     cudaEvent_t tl[kTimelinePoints + 1];  /* host-buffer calls: the call's timeline (timing events) */
     cudaStream_t hi;       /* greatest priority: GEMMs that side work runs beside */
 };
@@ -1979,8 +1990,8 @@ SidePool* side_pool()
               cudaStreamCreateWithPriority(&p->hi, cudaStreamNonBlocking, greatest) == cudaSuccess;
     for (int i = 0; i < 3 && ok; ++i) ok = cudaEventCreateWithFlags(&p->gate[i], cudaEventDisableTiming) == cudaSuccess;
     for (int i = 0; i <= kTimelinePoints && ok; ++i) ok = cudaEventCreate(&p->tl[i]) == cudaSuccess;
-    for (int i = 0; i < 16 && ok; ++i) ok = cudaEventCreateWithFlags(&p->chunk[i], cudaEventDisableTiming) == cudaSuccess;
-    for (int i = 0; i < 4 && ok; ++i) ok = cudaEventCreateWithFlags(&p->half[i], cudaEventDisableTiming) == cudaSuccess;
+    for (int i = 0; i < 32 && ok; ++i) ok = cudaEventCreateWithFlags(&p->chunk[i], cudaEventDisableTiming) == cudaSuccess;
+    for (int i = 0; i < 10 && ok; ++i) ok = cudaEventCreateWithFlags(&p->blk[i], cudaEventDisableTiming) == cudaSuccess;
     for (int h = 0; h < 2 && ok; ++h) {
         ok = cudaEventCreateWithFlags(&p->wave_gm[h], cudaEventDisableTiming) == cudaSuccess;
         for (int i = 0; i < kWaveStreams && ok; ++i)
@@ -2041,7 +2052,7 @@ static int job_maxima_a(SplitJob& j, cudaStream_t st)
     int cpb = 256;
     while (cpb > 32 && rows_blocks * ((j.d.ke + cpb - 1) / cpb) < 8 * 152) cpb /= 2;
     dim3 grid((unsigned)((j.m + 255) / 256), (unsigned)j.alg.kt, (unsigned)((j.d.ke + cpb - 1) / cpb));
-    amax_kernel<<<grid, 256, 0, st>>>(j.A, j.lda, j.m, j.k, j.alg.kt, amax, cpb);
+    amax_kernel<<<grid, 256, 0, st>>>(j.A, j.lda, j.m, j.k, j.alg.kt, amax, cpb, 0, j.m);
     fmm_count_launch(1);
     return FMM_OK;
 }
@@ -2120,7 +2131,10 @@ static void job_pack_a(SplitJob& j, int r0, int np, cudaStream_t st)
     fmm_count_launch(2);
 }
 
-static void job_pack_b_cols(SplitJob& j, int r0, int np, int64_t j0, int64_t j1, cudaStream_t st)
+/* small: the 128-thread pack tiles, which fit on an SM beside a resident
+ * GEMM CTA */
+static void job_pack_b_cols(SplitJob& j, int r0, int np, int64_t j0, int64_t j1, cudaStream_t st,
+                            bool small = false)
 {
     const Dims& d = j.d;
     if (j1 <= j0) return;
@@ -2132,6 +2146,45 @@ static void job_pack_b_cols(SplitJob& j, int r0, int np, int64_t j0, int64_t j1,
     sel.a = false;
     sel.jb0 = j0;
     sel.jb1 = j1;
+    sel.small = small;
+    launch_packs(j.fmt, j.s, j.alg.tab, r0, np, j.A, j.lda, j.B, j.ldb, j.m, j.n, j.k, d.m_pad, d.n_pad, d.k_pad,
+                 (int*)(j.w + j.L.erow), (int*)(j.w + j.L.fcol), j.w + j.L.sa, j.w + j.L.sb, st, st, sel);
+    fmm_count_launch(2);
+}
+
+/* per-sub-block row maxima of A (amax, zeroed beforehand) for the
+ * product-grid rows [a, b): the A rows ro_p + [a, b) of every row part p */
+static void job_maxima_a_rows(SplitJob& j, cudaStream_t st, int64_t a, int64_t b)
+{
+    unsigned long long* amax = (unsigned long long*)(j.w + j.L.amax);
+    for (int p = 0; p < j.alg.mt; ++p) {
+        int64_t ro, rl;
+        fmm_part_geom(j.m, j.alg.mt, p, &ro, &rl);
+        const int64_t r0 = ro + std::min(a, rl), r1 = ro + std::min(b, rl);
+        if (r1 <= r0) continue;
+        const int64_t rows_blocks = (r1 - r0 + 255) / 256 * j.alg.kt;
+        int cpb = 256;
+        while (cpb > 32 && rows_blocks * ((j.d.ke + cpb - 1) / cpb) < 8 * 152) cpb /= 2;
+        dim3 grid((unsigned)((r1 - r0 + 255) / 256), (unsigned)j.alg.kt, (unsigned)((j.d.ke + cpb - 1) / cpb));
+        amax_kernel<<<grid, 256, 0, st>>>(j.A, j.lda, j.m, j.k, j.alg.kt, amax, cpb, r0, r1);
+        fmm_count_launch(1);
+    }
+}
+
+/* row exponents and A slices of the products r0 .. r0+np-1 for the S_r rows
+ * [a, b) (multiples of 64, or b = m_pad) */
+static void job_pack_a_rows(SplitJob& j, int r0, int np, int64_t a, int64_t b, cudaStream_t st, bool small = false)
+{
+    const Dims& d = j.d;
+    if (b <= a) return;
+    exps_kernel<<<dim3((unsigned)((b - a + 255) / 256), (unsigned)np), 256, 0, st>>>(
+        j.alg.tab, r0, j.m, j.n, j.k, d.m_pad, d.n_pad, (unsigned long long*)(j.w + j.L.amax),
+        (unsigned long long*)(j.w + j.L.bmax), (int*)(j.w + j.L.erow), (int*)(j.w + j.L.fcol), a, b);
+    PackSel sel;
+    sel.b = false;
+    sel.ia0 = a;
+    sel.ia1 = b;
+    sel.small = small;
     launch_packs(j.fmt, j.s, j.alg.tab, r0, np, j.A, j.lda, j.B, j.ldb, j.m, j.n, j.k, d.m_pad, d.n_pad, d.k_pad,
                  (int*)(j.w + j.L.erow), (int*)(j.w + j.L.fcol), j.w + j.L.sa, j.w + j.L.sb, st, st, sel);
     fmm_count_launch(2);
@@ -2218,22 +2271,24 @@ static int job_gemm(const SplitJob& j, int np, cudaStream_t st)
     return FMM_OK;
 }
 
-/* job_gemm restricted to the tile columns [jt0, jt1) of every product: the
- * B slice map starts jt0 * 256 rows further and Z jt0 * 256 columns
- * further, with the same row strides, so each (product, tile) item computes
- * exactly what the full launch computes for it. */
-static int job_gemm_cols(const SplitJob& j, int np, int64_t jt0, int64_t jt1, cudaStream_t st)
+/* job_gemm restricted to the tile rows [it0, it1) and tile columns
+ * [jt0, jt1) of every product: the A slice map starts it0 tile rows
+ * further, the B slice map jt0 * 256 rows further and Z at (it0 tile rows,
+ * jt0 * 256 columns), with the same row strides, so each (product, tile)
+ * item computes exactly what the full launch computes for it. */
+static int job_gemm_block(const SplitJob& j, int np, int64_t it0, int64_t it1, int64_t jt0, int64_t jt1,
+                          cudaStream_t st)
 {
     const bool pair = job_pair(j);
-    const int64_t tn = jt1 - jt0;
-    if (tn <= 0) return FMM_OK;
-    const int64_t tiles_m = j.d.m_pad / (pair ? kPairTileM : kTileM);
-    const int64_t tiles = tiles_m * tn;
+    const int64_t tm = it1 - it0, tn = jt1 - jt0;
+    if (tm <= 0 || tn <= 0) return FMM_OK;
+    const int64_t tiles = tm * tn;
     const int64_t units = pair ? 76 : 152;
     int K = (int)std::min<int64_t>(np, std::max<int64_t>(1, (24 * units + tiles - 1) / tiles));
     const int nl = (np + K - 1) / K;
     K = (np + nl - 1) / nl;
     const size_t esz = j.fmt ? 1 : 2;
+    const int64_t r0 = it0 * (pair ? kPairTileM : kTileM), c0 = jt0 * kTileN;
     GemmLaunch gl;
     for (int r = 0; r < np; r += K) {
         const int cnt = std::min(K, np - r);
@@ -2242,12 +2297,14 @@ static int job_gemm_cols(const SplitJob& j, int np, int64_t jt0, int64_t jt1, cu
         gl.sched = (unsigned int*)(j.w + j.L.sched);
         GemmProblem& gp = gl.prob[0];
         if (int rc = job_fill(j, gp, cnt, 0, pair, r); rc != FMM_OK) return rc;
-        const int64_t c0 = jt0 * kTileN;
+        const uint8_t* sa = j.w + j.L.sa + ((size_t)r * j.s * j.d.m_pad + (size_t)r0) * j.d.k_pad * esz;
         const uint8_t* sb = j.w + j.L.sb + ((size_t)r * j.s * j.d.n_pad + (size_t)c0) * j.d.k_pad * esz;
-        if (make_slice_map(&gp.tmB, sb, j.d.k_pad, (int64_t)cnt * j.s * j.d.n_pad - c0, pair ? kTileN / 2 : kTileN,
+        if (make_slice_map(&gp.tmA, sa, j.d.k_pad, (int64_t)cnt * j.s * j.d.m_pad - r0, kTileM, j.fmt) != FMM_OK ||
+            make_slice_map(&gp.tmB, sb, j.d.k_pad, (int64_t)cnt * j.s * j.d.n_pad - c0, pair ? kTileN / 2 : kTileN,
                            j.fmt) != FMM_OK)
             return FMM_ERR_CUDA;
-        gp.Z += c0 * j.d.m_pad;
+        gp.Z += r0 + c0 * j.d.m_pad;
+        gp.tiles_m = (int)tm;
         gp.tiles_n = (int)tn;
         if (int rc = launch_gemm(gl, (int64_t)cnt * tiles, cnt, st, pair); rc != FMM_OK) return rc;
     }
@@ -2274,10 +2331,10 @@ static bool job_scatter_all(const SplitJob& j, int r0, int np, int* T_out, size_
     return P <= 64 && T >= 32 && smem <= 47 * 1024;
 }
 
-/* the C updates of products [r0, r0 + np) for the product-grid columns
- * [j0, j1) (all rows), element-major form only */
-static void job_scatter_cols(const SplitJob& j, int r0, int np, int64_t j0, int64_t j1, cudaStream_t st,
-                             bool small = false)
+/* the C updates of products [r0, r0 + np) for the product-grid rows
+ * [i0, i1) of the columns [j0, j1), element-major form only */
+static void job_scatter_block(const SplitJob& j, int r0, int np, int64_t i0, int64_t i1, int64_t j0, int64_t j1,
+                              cudaStream_t st, bool small = false)
 {
     int T;
     size_t smem;
@@ -2288,13 +2345,22 @@ static void job_scatter_cols(const SplitJob& j, int r0, int np, int64_t j0, int6
         T = 128;
         smem = (size_t)P * T * 8 + (size_t)E * 12 + (size_t)(np + 1) * 4;
     }
-    const uint64_t first = (uint64_t)j0 * (uint64_t)j.d.me, end = (uint64_t)j1 * (uint64_t)j.d.me;
+    const uint64_t rows = (uint64_t)(i1 - i0);
+    const uint64_t first = (uint64_t)j0 * rows, end = (uint64_t)j1 * rows;
     if (end <= first) return;
     scatter_all_kernel<<<scatter_blocks(end - first, T), (unsigned)T, smem, st>>>(
         j.alg.tab, r0, np, j.m, j.n, (int)j.d.m_pad, (int)j.d.n_pad, job_ebase(j), j.alpha,
         (const int64_t*)(j.w + j.L.z), (const int*)(j.w + j.L.erow), (const int*)(j.w + j.L.fcol), j.C, j.ldc, first,
-        end);
+        end, (uint32_t)i0, (uint32_t)rows);
     fmm_count_launch(1);
+}
+
+/* the C updates of products [r0, r0 + np) for the product-grid columns
+ * [j0, j1) (all rows), element-major form only */
+static void job_scatter_cols(const SplitJob& j, int r0, int np, int64_t j0, int64_t j1, cudaStream_t st,
+                             bool small = false)
+{
+    job_scatter_block(j, r0, np, 0, j.d.me, j0, j1, st, small);
 }
 
 /* small: blocks of at most 128 threads (and so at most 16 KB of sub-block
@@ -2314,7 +2380,7 @@ static void job_scatter(const SplitJob& j, int r0, int np, cudaStream_t st, bool
         scatter_all_kernel<<<scatter_blocks((uint64_t)elems, T), (unsigned)T, smem, st>>>(
             j.alg.tab, r0, np, j.m, j.n, (int)j.d.m_pad, (int)j.d.n_pad, job_ebase(j), j.alpha,
             (const int64_t*)(j.w + j.L.z), (const int*)(j.w + j.L.erow), (const int*)(j.w + j.L.fcol), j.C, j.ldc,
-            (uint64_t)0, (uint64_t)elems);
+            (uint64_t)0, (uint64_t)elems, 0u, 0u);
         fmm_count_launch(1);
         return;
     }
@@ -2535,6 +2601,172 @@ int fmm_split_host(const AlgView& alg, int64_t m, int64_t n, int64_t k, double a
         const int G = j.L.group, nt = alg.nt;
         const bool one_group = G >= alg.R;
         cudaStream_t sb = sp->s[0];
+        /* Blocked schedule, for one product group with the element-major C
+         * update and a product grid of at least two GEMM tiles along a side:
+         * the grid splits into up to 2 x 2 blocks of tiles (row halves of A,
+         * column halves of B). A's first row half and B's first column half
+         * go up first, so the GEMM of block (0, 0) starts after half of each
+         * operand; A's second half follows, then B's, and the blocks run in
+         * the order (0,0), (1,0), (0,1), (1,1). A block's C elements are final
+         * when its GEMM ends: they are updated (beside the next block's GEMM)
+         * and read back in four column chunks, so after the last GEMM only
+         * the last block's C is left. The work a block's GEMM meets beside
+         * it (the other halves' slices, the earlier blocks' C updates) runs
+         * in the 128-thread forms that fit on an SM beside a GEMM CTA. Every
+         * (product, tile) item and every C element is computed as in the
+         * unblocked call: the same bits. */
+        {
+            const bool pair = job_pair(j);
+            const int64_t me = j.d.me, ne = j.d.ne, m_pad = j.d.m_pad, n_pad = j.d.n_pad;
+            const int64_t U = pair ? kPairTileM : kTileM;
+            const int64_t tiles_m = m_pad / U, tiles_n = n_pad / kTileN;
+            const int RH = tiles_m >= 2 ? 2 : 1, CH = tiles_n >= 2 ? 2 : 1;
+            int Tchk;
+            size_t smchk;
+            if (one_group && RH * CH >= 2 && job_scatter_all(j, 0, alg.R, &Tchk, &smchk)) {
+                const int mt = alg.mt;
+                const int64_t tcm[3] = {0, RH == 2 ? (tiles_m + 1) / 2 : tiles_m, tiles_m};
+                const int64_t tcn[3] = {0, CH == 2 ? (tiles_n + 1) / 2 : tiles_n, tiles_n};
+                const int64_t rcut[3] = {0, tcm[1] * U, m_pad};          /* S_r row halves */
+                const int64_t ccut[3] = {0, tcn[1] * kTileN, n_pad};     /* T_r column halves */
+                cudaStream_t ss = sp->s[3], sa = sp->s[4];
+                auto up_a = [&](int h) -> int {
+                    /* the A rows ro_p + [rcut[h], rcut[h+1]) of every row part p, then that half's A side on s[4] */
+                    if (RH == 1) {
+                        if (!ok(fmm_copy2d_async(dA, row, A, sizeof(double) * lda, row, k, cudaMemcpyHostToDevice, cs)))
+                            return FMM_ERR_CUDA;
+                    } else {
+                        for (int p = 0; p < mt; ++p) {
+                            int64_t ro, rl;
+                            fmm_part_geom(m, mt, p, &ro, &rl);
+                            const int64_t a = ro + std::min(rcut[h], rl), b = ro + std::min(rcut[h + 1], rl);
+                            if (b > a && !ok(fmm_copy2d_async(dA + a, row, A + a, sizeof(double) * lda,
+                                                               sizeof(double) * (b - a), k, cudaMemcpyHostToDevice, cs)))
+                                return FMM_ERR_CUDA;
+                        }
+                    }
+                    if (!ok(cudaEventRecord(sp->blk[h], cs)) || !ok(cudaStreamWaitEvent(sa, sp->blk[h], 0)))
+                        return FMM_ERR_CUDA;
+                    if (h == 0 && !ok(cudaMemsetAsync(j.w + j.L.amax, 0,
+                                                      sizeof(unsigned long long) * (size_t)alg.kt * (size_t)m, sa)))
+                        return FMM_ERR_CUDA;
+                    job_maxima_a_rows(j, sa, rcut[h], rcut[h + 1]);
+                    job_pack_a_rows(j, 0, alg.R, rcut[h], rcut[h + 1], sa, h == 1);
+                    return ok(cudaEventRecord(sp->blk[2 + h], sa)) ? FMM_OK : FMM_ERR_CUDA;
+                };
+                int xb = 0;
+                auto up_b = [&](int h) -> int {
+                    /* the T_r columns [ccut[h], ccut[h+1]) in four chunks, each chunk's B side on s[0] */
+                    const int64_t w = round_up((ccut[h + 1] - ccut[h] + 3) / 4, 32);
+                    for (int64_t j0 = ccut[h]; j0 < ccut[h + 1]; j0 += w, ++xb) {
+                        const int64_t j1 = std::min(j0 + w, ccut[h + 1]);
+                        for (int c = 0; c < nt; ++c) {
+                            int64_t co, cl;
+                            fmm_part_geom(n, nt, c, &co, &cl);
+                            const int64_t a = co + std::min(j0, cl), b = co + std::min(j1, cl);
+                            if (b > a && !ok(fmm_copy2d_async(dB + a * k, sizeof(double) * k, B + a * ldb,
+                                                               sizeof(double) * ldb, sizeof(double) * k, b - a,
+                                                               cudaMemcpyHostToDevice, cs)))
+                                return FMM_ERR_CUDA;
+                        }
+                        if (!ok(cudaEventRecord(sp->chunk[xb], cs)) || !ok(cudaStreamWaitEvent(sb, sp->chunk[xb], 0)))
+                            return FMM_ERR_CUDA;
+                        for (int c = 0; c < nt; ++c) {
+                            int64_t co, cl;
+                            fmm_part_geom(n, nt, c, &co, &cl);
+                            job_maxima_b(j, sb, co + std::min(j0, cl), co + std::min(j1, cl));
+                        }
+                        job_pack_b_cols(j, 0, alg.R, j0, j1, sb, h == 1);
+                    }
+                    return ok(cudaEventRecord(sp->blk[4 + h], sb)) ? FMM_OK : FMM_ERR_CUDA;
+                };
+                mark(0, cs);
+                if ((rc = up_a(0)) != FMM_OK) return rc;
+                if (RH == 1) mark(1, cs);
+                if ((rc = up_b(0)) != FMM_OK) return rc;
+                if (RH == 2) {
+                    if ((rc = up_a(1)) != FMM_OK) return rc;
+                    mark(1, cs);
+                }
+                if (CH == 2 && (rc = up_b(1)) != FMM_OK) return rc;
+                mark(2, cs);
+                /* C up behind A and B, then C := beta*C, on s[3] */
+                if (beta != 0.0 &&
+                    (!ok(fmm_copy2d_async(dC, row, C, sizeof(double) * ldc, row, n, cudaMemcpyHostToDevice, cs)) ||
+                     !ok(cudaEventRecord(sp->gate[2], cs)) || !ok(cudaStreamWaitEvent(ss, sp->gate[2], 0))))
+                    return FMM_ERR_CUDA;
+                if ((rc = fmm_scale_c(m, n, beta, dC, m, ss)) != FMM_OK) return rc;
+                /* the GEMM blocks on the call's stream */
+                const int order[4][2] = {{0, 0}, {1, 0}, {0, 1}, {1, 1}};
+                int nq = 0;
+                int qr[4], qc[4];
+                for (const auto& o : order)
+                    if (o[0] < RH && o[1] < CH) {
+                        qr[nq] = o[0];
+                        qc[nq] = o[1];
+                        ++nq;
+                    }
+                for (int q = 0; q < nq; ++q) {
+                    if (!ok(cudaStreamWaitEvent(st, sp->blk[2 + qr[q]], 0)) ||
+                        !ok(cudaStreamWaitEvent(st, sp->blk[4 + qc[q]], 0)))
+                        return FMM_ERR_CUDA;
+                    if (q == 0) mark(3, st);
+                    if ((rc = job_gemm_block(j, alg.R, tcm[qr[q]], tcm[qr[q] + 1], tcn[qc[q]], tcn[qc[q] + 1], st)) !=
+                        FMM_OK)
+                        return rc;
+                    if (!ok(cudaEventRecord(sp->blk[6 + q], st))) return FMM_ERR_CUDA;
+                }
+                mark(4, st);
+                /* each block's C updates on s[3] in four column chunks, each
+                 * chunk's C elements read back on s[1] */
+                int xc = 0;
+                for (int q = 0; q < nq; ++q) {
+                    if (!ok(cudaStreamWaitEvent(ss, sp->blk[6 + q], 0))) return FMM_ERR_CUDA;
+                    const int64_t i0 = rcut[qr[q]], i1 = std::min(rcut[qr[q] + 1], me);
+                    const int64_t a0 = ccut[qc[q]], b0 = std::min(ccut[qc[q] + 1], ne);
+                    if (i1 <= i0 || b0 <= a0) continue;
+                    const int64_t w = std::max<int64_t>((b0 - a0 + 3) / 4, 1);
+                    for (int64_t j0 = a0; j0 < b0; j0 += w, ++xc) {
+                        const int64_t j1 = std::min(j0 + w, b0);
+                        job_scatter_block(j, 0, alg.R, i0, i1, j0, j1, ss, q + 1 < nq);
+                        if (!ok(cudaEventRecord(sp->chunk[8 + xc], ss)) ||
+                            !ok(cudaStreamWaitEvent(cs, sp->chunk[8 + xc], 0)))
+                            return FMM_ERR_CUDA;
+                        for (int p = 0; p < mt; ++p) {
+                            int64_t ro, rl;
+                            fmm_part_geom(m, mt, p, &ro, &rl);
+                            const int64_t ra = ro + std::min(i0, rl), rb = ro + std::min(i1, rl);
+                            if (rb <= ra) continue;
+                            for (int c = 0; c < nt; ++c) {
+                                int64_t co, cl;
+                                fmm_part_geom(n, nt, c, &co, &cl);
+                                const int64_t ca = co + std::min(j0, cl), cb = co + std::min(j1, cl);
+                                if (cb > ca &&
+                                    !ok(fmm_copy2d_async(C + ra + ca * ldc, sizeof(double) * ldc, dC + ra + ca * m, row,
+                                                          sizeof(double) * (rb - ra), cb - ca, cudaMemcpyDeviceToHost,
+                                                          cs)))
+                                    return FMM_ERR_CUDA;
+                            }
+                        }
+                    }
+                }
+                mark(5, cs);
+                if (!ok(cudaStreamSynchronize(cs)) || !ok(cudaStreamSynchronize(st)) ||
+                    !ok(cudaStreamSynchronize(ss)) || !ok(cudaStreamSynchronize(sa)) || !ok(cudaStreamSynchronize(sb)))
+                    return FMM_ERR_CUDA;
+                if (tline) {
+                    std::lock_guard<std::mutex> lk(g_timeline_mu);
+                    for (int y = 1; y <= kTimelinePoints; ++y) {
+                        float t = 0.f;
+                        cudaEventElapsedTime(&t, sp->tl[0], sp->tl[y]);
+                        g_timeline_ms[y - 1] = t;
+                    }
+                    g_timeline_ms[kTimelinePoints] =
+                        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - host_t0).count();
+                }
+                return cudaGetLastError() == cudaSuccess ? fmm_device_error_status() : FMM_ERR_CUDA;
+            }
+        }
         /* A, then the A side's maxima (and, with one product group, its
          * exponents and slices) */
         mark(0, cs);
@@ -2544,34 +2776,15 @@ int fmm_split_host(const AlgView& alg, int64_t m, int64_t n, int64_t k, double a
         mark(1, cs);
         if ((rc = job_maxima_a(j, st)) != FMM_OK) return rc;
         if (one_group) job_pack_a(j, 0, alg.R, st);
-        /* B in chunks of T_r columns [j0, j1): chunk x holds the B columns
-         * co_c + [j0, j1) of every column part c, and the B side of those
-         * columns (maxima; with one group, exponents and slices) runs on s[0]
-         * as soon as the chunk has arrived. With one product group and the
-         * element-major C update, the GEMM runs in two halves of tile
-         * columns: the first half starts once the B slices of its columns
-         * are formed, and its C columns are updated and read back while the
-         * second half is computed. */
+        /* B in kChunks chunks of T_r columns [j0, j1): chunk x holds the B
+         * columns co_c + [j0, j1) of every column part c, and the B side of
+         * those columns (maxima; with one group, exponents and slices) runs
+         * on s[0] as soon as the chunk has arrived */
         const int64_t ne = j.d.ne, n_pad = j.d.n_pad;
-        const int64_t tiles_n = n_pad / kTileN, th = (tiles_n + 1) / 2, js = th * kTileN;
-        int Tchk;
-        size_t smchk;
-        const bool halves = one_group && tiles_n >= 2 && job_scatter_all(j, 0, alg.R, &Tchk, &smchk);
-        std::vector<std::pair<int64_t, int64_t>> bch;
-        if (halves) {
-            /* four chunks per half, multiples of 32 columns */
-            for (int h = 0; h < 2; ++h) {
-                const int64_t a = h ? js : 0, b = h ? n_pad : js;
-                const int64_t w = round_up((b - a + 3) / 4, 32);
-                for (int64_t c0 = a; c0 < b; c0 += w) bch.emplace_back(c0, std::min(c0 + w, b));
-            }
-        } else {
-            const int64_t W = (ne + kChunks * 32 - 1) / (kChunks * 32) * 32;
-            for (int64_t j0 = 0; j0 < n_pad; j0 += W) bch.emplace_back(j0, std::min(j0 + W, n_pad));
-        }
+        const int64_t W = (ne + kChunks * 32 - 1) / (kChunks * 32) * 32;
         int x = 0;
-        for (const auto& ch : bch) {
-            const int64_t j0 = ch.first, j1 = ch.second;
+        for (int64_t j0 = 0; j0 < n_pad; j0 += W, ++x) {
+            const int64_t j1 = std::min(j0 + W, n_pad);
             for (int c = 0; c < nt; ++c) {
                 int64_t co, cl;
                 fmm_part_geom(n, nt, c, &co, &cl);
@@ -2588,64 +2801,6 @@ int fmm_split_host(const AlgView& alg, int64_t m, int64_t n, int64_t k, double a
                 job_maxima_b(j, sb, co + std::min(j0, cl), co + std::min(j1, cl));
             }
             if (one_group) job_pack_b_cols(j, 0, alg.R, j0, j1, sb);
-            if (halves && (j1 == js || j1 == n_pad) && !ok(cudaEventRecord(sp->half[j1 == js ? 0 : 1], sb)))
-                return FMM_ERR_CUDA;
-            ++x;
-        }
-        if (halves) {
-            cudaStream_t ss = sp->s[3];
-            mark(2, cs);
-            /* C up behind B, then C := beta*C, on s[3] */
-            if (beta != 0.0 &&
-                (!ok(fmm_copy2d_async(dC, row, C, sizeof(double) * ldc, row, n, cudaMemcpyHostToDevice, cs)) ||
-                 !ok(cudaEventRecord(sp->gate[2], cs)) || !ok(cudaStreamWaitEvent(ss, sp->gate[2], 0))))
-                return FMM_ERR_CUDA;
-            if ((rc = fmm_scale_c(m, n, beta, dC, m, ss)) != FMM_OK) return rc;
-            for (int h = 0; h < 2; ++h) {
-                if (!ok(cudaStreamWaitEvent(st, sp->half[h], 0))) return FMM_ERR_CUDA;
-                if (h == 0) mark(3, st);
-                if ((rc = job_gemm_cols(j, alg.R, h ? th : 0, h ? tiles_n : th, st)) != FMM_OK) return rc;
-                if (!ok(cudaEventRecord(sp->half[2 + h], st))) return FMM_ERR_CUDA;
-            }
-            mark(4, st);
-            /* per half, the C updates of its product-grid columns in four
-             * column chunks on s[3] (beside the second half's GEMM: 128-thread
-             * blocks), each chunk's C columns read back on s[1] */
-            x = 0;
-            for (int h = 0; h < 2; ++h) {
-                if (!ok(cudaStreamWaitEvent(ss, sp->half[2 + h], 0))) return FMM_ERR_CUDA;
-                const int64_t a0 = h ? js : 0, b0 = h ? ne : std::min(js, ne);
-                const int64_t w = std::max<int64_t>((b0 - a0 + 3) / 4, 1);
-                for (int64_t j0 = a0; j0 < b0; j0 += w, ++x) {
-                    const int64_t j1 = std::min(j0 + w, b0);
-                    job_scatter_cols(j, 0, alg.R, j0, j1, ss, h == 0);
-                    if (!ok(cudaEventRecord(sp->chunk[kChunks + x], ss)) ||
-                        !ok(cudaStreamWaitEvent(cs, sp->chunk[kChunks + x], 0)))
-                        return FMM_ERR_CUDA;
-                    for (int c = 0; c < nt; ++c) {
-                        int64_t co, cl;
-                        fmm_part_geom(n, nt, c, &co, &cl);
-                        const int64_t a = co + std::min(j0, cl), b = co + std::min(j1, cl);
-                        if (b > a && !ok(fmm_copy2d_async(C + a * ldc, sizeof(double) * ldc, dC + a * m, row, row,
-                                                           b - a, cudaMemcpyDeviceToHost, cs)))
-                            return FMM_ERR_CUDA;
-                    }
-                }
-            }
-            mark(5, cs);
-            if (!ok(cudaStreamSynchronize(cs)) || !ok(cudaStreamSynchronize(st)) || !ok(cudaStreamSynchronize(ss)))
-                return FMM_ERR_CUDA;
-            if (tline) {
-                std::lock_guard<std::mutex> lk(g_timeline_mu);
-                for (int y = 1; y <= kTimelinePoints; ++y) {
-                    float t = 0.f;
-                    cudaEventElapsedTime(&t, sp->tl[0], sp->tl[y]);
-                    g_timeline_ms[y - 1] = t;
-                }
-                g_timeline_ms[kTimelinePoints] =
-                    std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - host_t0).count();
-            }
-            return cudaGetLastError() == cudaSuccess ? fmm_device_error_status() : FMM_ERR_CUDA;
         }
         mark(2, cs);
         for (int r0 = 0; r0 < alg.R; r0 += G) {

@@ -63,7 +63,7 @@ SMS = 152
 CLOCK_HZ = 2.07e9
 FP64_EFF = 0.98
 FP64_SMALL_EFF = 0.8      # 32 x 32 tiles (two CTAs per SM)
-FP64_SUP_EFF = 0.5        # one small/skinny cluster CTA per SM: 128 x 128 x 16384 in 1.05 ms
+FP64_SUP_EFF = 0.5        # small/skinny cluster CTAs, up to two per SM: 128 x 128 x 16384 in 1.05 ms
 SPLIT_EFF = 0.61
 PACK_S_PER_ELEM_SLICE = 1.16e-12
 SCATTER_S_PER_ENTRY_ELEM = 2.44e-12

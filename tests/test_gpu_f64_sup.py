@@ -19,8 +19,10 @@ def test_sup_split_rule(fmm):
     """The chunk count is a function of the shape only (no GPU needed)."""
     assert fmm.f64_sup_splits(128, 128, 16384) == 8
     assert fmm.f64_sup_splits(33, 700, 3000) == 5        # 2 x 22 tiles: 256 CTAs at most
+    assert fmm.f64_sup_splits(100, 90, 5000) == 8        # 4 x 3 tiles, 96 CTAs
     assert fmm.f64_sup_splits(64, 64, 600) == 2          # k / 256 limits the chunks
     assert fmm.f64_sup_splits(257, 129, 2048) == 5       # 9 x 5 tiles: 256 / 45
+    assert fmm.f64_sup_splits(288, 512, 8192) == 0       # 9 x 16 tiles: more than 128
     assert fmm.f64_sup_splits(128, 128, 300) == 0        # too short a k
     assert fmm.f64_sup_splits(512, 512, 4096) == 0       # 256 tiles: the regular kernel fills the GPU
     assert fmm.f64_sup_splits(0, 10, 4096) == 0

@@ -166,13 +166,15 @@ def test_host_alloc_buffers(fmm, torch_cuda):
 
 
 @pytest.mark.parametrize("levels,shape,alpha,beta", [(1, (517, 1033, 700), 1.5, 0.5), (2, (1037, 1033, 411), 1.0, 0.0),
-                                                     (0, (300, 2311, 257), -1.0, 2.0)])
-def test_host_call_gemm_halves(fmm, torch_cuda, levels, shape, alpha, beta):
-    """Product grids of at least two 256-column tiles run the GEMM in two
-    halves of tile columns, the first half's C columns updated and read back
-    during the second (uneven halves: 517 / 3 and 259 / 2 columns of the
-    product grid; leading dimensions larger than the row counts): the device
-    call's bits."""
+                                                     (0, (300, 2311, 257), -1.0, 2.0), (1, (200, 1033, 300), 1.0, 1.0),
+                                                     (1, (1033, 200, 300), 0.5, 1.0)])
+def test_host_call_gemm_blocks(fmm, torch_cuda, levels, shape, alpha, beta):
+    """Product grids of at least two GEMM tiles along a side run the GEMM in
+    up to 2 x 2 blocks (A row halves, B column halves), each block's C
+    elements updated and read back during the next block (uneven halves such
+    as 259 / 3 rows and 517 / 3 columns of the product grid; row halves only;
+    column halves only; leading dimensions larger than the row counts): the
+    device call's bits."""
     m, n, k = shape
     A, B, C = rand(m, k, 551), rand(k, n, 552), rand(m, n, 553)
     f = fmm.strassen_fmm() if levels else None
