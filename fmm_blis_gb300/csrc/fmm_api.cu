@@ -529,6 +529,22 @@ extern "C" void fmm_gpu_release_host_buffers(void)
     }
 }
 
+void fmm_touch_host(const void* p, size_t bytes)
+{
+    static const size_t page = []() {
+        const long v = sysconf(_SC_PAGESIZE);
+        return v > 0 ? (size_t)v : (size_t)4096;
+    }();
+    if (p == nullptr || bytes == 0) return;
+    const volatile uint8_t* b = (const volatile uint8_t*)p;
+    /* from the page holding the first byte to the page holding the last */
+    const size_t lead = (uintptr_t)p % page;
+    uint8_t sink = 0;
+    for (size_t off = 0; off < bytes + lead; off += page) sink ^= b[off > lead ? off - lead : 0];
+    sink ^= b[bytes - 1];
+    (void)sink;
+}
+
 /* ---------------------------------------------------------------------------
  * Pinned host buffers on transparent huge pages.
  *
