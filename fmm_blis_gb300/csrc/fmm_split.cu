@@ -1550,6 +1550,21 @@ __device__ __forceinline__ void scatter_all_body(const int* __restrict__ tab, in
     const uint32_t rows = i_rows ? i_rows : me;
     const uint64_t idx = idx_first + vb * (uint64_t)T + (uint64_t)tid;
     const uint64_t end = idx_end < (uint64_t)rows * (uint64_t)ne ? idx_end : (uint64_t)rows * (uint64_t)ne;
+    if (P == 1 && E == 1 && nprod == 1) {
+        /* one sub-block fed by one product (the classical split GEMM): the
+         * same conversion and FMA per element without the per-sub-block
+         * bookkeeping, the element's C value kept in a register */
+        const double l = lam[0];
+        for (uint64_t idx2 = idx; idx2 < end; idx2 += vg * (uint64_t)T) {
+            const int i = (int)(i_lo + (uint32_t)idx2 % rows), j = (int)((uint32_t)idx2 / rows);
+            if (i >= geo[1][0] || j >= geo[3][0]) continue;
+            const int64_t z = Z[(int64_t)j * m_pad + i];
+            const int ex = e_row[i] + f_col[j] + ebase;
+            double* cp = C + geo[0][0] + i + (int64_t)(geo[2][0] + j) * ldc;
+            *cp = fma(l, i64_to_double_scaled(z, ex), *cp);
+        }
+        return;
+    }
     /* grid-stride: a block's set-up above serves many elements */
     for (uint64_t idx2 = idx; idx2 < end; idx2 += vg * (uint64_t)T)
         scatter_all_element(idx2, rows, i_lo, P, T, tid, nprod, m_pad, n_pad, ebase, geo, cs, lam, pidx, off, Z,
