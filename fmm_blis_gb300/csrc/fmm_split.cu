@@ -58,8 +58,10 @@
  * them as two groups, the second group's packs and the first group's C
  * updates on pool streams beside the other group's GEMM, and a group's GEMM
  * as launches of about 24 rounds of items. The host-buffer call overlaps the
- * copies with the work (B in column chunks chased by its packs, C read back
- * in column chunks behind the last C updates). Batched calls run waves of up
+ * copies with the work (A in row halves and B in column chunks chased by
+ * their packs, the GEMM in up to 2 x 2 blocks of tiles that start on half of
+ * each operand, each block's C read back in column chunks behind its C
+ * updates). Batched calls run waves of up
  * to 80 problems, one GEMM launch per tile kind per wave, waves alternating
  * between two workspace halves so a wave's packs overlap the previous wave.
  * Every path gives the same bits for a problem.
@@ -2539,13 +2541,15 @@ static int split_launch_budget(const AlgView& alg, int64_t m, int64_t n, int64_t
  *
  * Operands in host memory: the call owns the device copies and overlaps the
  * host<->device traffic with the device work. Copies run on s[1] in the
- * order A, B, C; the A side (row maxima, row exponents, A slices) starts as
- * soon as A has arrived, the B side on s[0] as soon as B has, and C is only
- * needed by the scatter, so its upload runs under the GEMM. The host enqueues
- * in the same order (copy A, A side, copy B, B side, GEMM, copy C), which keeps
- * the overlap when a copy from pageable memory blocks the host until it is
- * staged. The operand and workspace buffers are kept per device (grow-only)
- * until fmm_gpu_release_host_buffers.
+ * order A, B, C (with the blocked schedule below: A's first row half, B's
+ * first column half, A's second half, B's second half, C); the A side (row
+ * maxima, row exponents, A slices) starts as soon as its rows have arrived,
+ * the B side on s[0] as soon as its columns have, and C is only needed by the
+ * C updates, so its upload runs under the GEMM. The host enqueues in the same
+ * order, which keeps the overlap when a copy from pageable memory blocks the
+ * host until it is staged. Every host copy touches its host pages first
+ * (fmm_touch_host). The operand and workspace buffers are kept per device
+ * (grow-only) until fmm_gpu_release_host_buffers.
  * ------------------------------------------------------------------------- */
 struct HostBuffers {
     uint8_t* p = nullptr;
