@@ -1557,13 +1557,32 @@ __device__ __forceinline__ void scatter_all_body(const int* __restrict__ tab, in
          * same conversion and FMA per element without the per-sub-block
          * bookkeeping, the element's C value kept in a register */
         const double l = lam[0];
-        for (uint64_t idx2 = idx; idx2 < end; idx2 += vg * (uint64_t)T) {
-            const int i = (int)(i_lo + (uint32_t)idx2 % rows), j = (int)((uint32_t)idx2 / rows);
-            if (i >= geo[1][0] || j >= geo[3][0]) continue;
-            const int64_t z = Z[(int64_t)j * m_pad + i];
-            const int ex = e_row[i] + f_col[j] + ebase;
-            double* cp = C + geo[0][0] + i + (int64_t)(geo[2][0] + j) * ldc;
-            *cp = fma(l, i64_to_double_scaled(z, ex), *cp);
+        const uint64_t step = vg * (uint64_t)T;
+        constexpr int U = 2;   /* elements per thread per round: their loads go out together */
+        const int ro = geo[0][0], rl = geo[1][0], co = geo[2][0], cl = geo[3][0];
+        for (uint64_t idx2 = idx; idx2 < end; idx2 += U * step) {
+            int64_t z[U];
+            int ex[U];
+            double c[U];
+            int ii[U], jj[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const uint64_t e = idx2 + u * step;
+                ii[u] = (int)(i_lo + (uint32_t)e % rows);
+                jj[u] = e < end ? (int)((uint32_t)e / rows) : cl;   /* past the end: not live */
+                z[u] = 0;
+                ex[u] = 0;
+                c[u] = 0.0;
+                if (ii[u] < rl && jj[u] < cl) {
+                    z[u] = Z[(int64_t)jj[u] * m_pad + ii[u]];
+                    ex[u] = e_row[ii[u]] + f_col[jj[u]] + ebase;
+                    c[u] = C[ro + ii[u] + (int64_t)(co + jj[u]) * ldc];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+                if (ii[u] < rl && jj[u] < cl)
+                    C[ro + ii[u] + (int64_t)(co + jj[u]) * ldc] = fma(l, i64_to_double_scaled(z[u], ex[u]), c[u]);
         }
         return;
     }
