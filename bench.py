@@ -622,6 +622,7 @@ def serve_window(torch, dev, rate, duration, split_fraction, target, seed, clock
            "sustained_tflops": flops_done / duration / 1e12, "by_form": by_form,
            "graph_path_requests": sum(1 for r in done if r.path == "graph"), "batches": srv.launched_batches,
            "peak_hbm_gib": srv.peak_used / 2**30, "hbm_budget_gib": srv.budget / 2**30,
+           "placement_retries": srv.alloc_failures,
            "fp64_ctas": srv.fp64_ctas, "wall_s": t_end - t0}
     if clk:
         out["clocks"] = clk.summary()
@@ -765,6 +766,11 @@ def main():
     if args.impl == "reference":
         run_reference(args)
         return
+    if args.workload == "serve":
+        # a served mix keeps many streams busy (the server's, the library's side-work pool, graph slots): give
+        # them their own hardware queues, so work behind a long FP64 batch on a shared queue does not wait for it
+        # (read when the CUDA context is created, so before the first CUDA call)
+        os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
     import torch
 
     import fmm_blis_gb300 as fmm

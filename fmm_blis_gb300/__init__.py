@@ -411,22 +411,31 @@ def batch_workspace_size(batch) -> int:
     return int(lib().fmm_gpu_batch_workspace_size(count, arr))
 
 
+def batch_shapes_workspace_size(shapes) -> int:
+    """Workspace a batch needs, from its problems' shapes and plans alone:
+    shapes is an iterable of (m, n, k, fmm or None, levels, slices, fmt). The
+    sizing call reads no operand data, so placeholder addresses stand in for
+    the operands."""
+    items = list(shapes)
+    arr = (BatchProblem * max(len(items), 1))()
+    for i, (m, n, k, fmm, levels, slices, fmt) in enumerate(items):
+        arr[i].fmm = ctypes.cast(ctypes.pointer(fmm), ctypes.c_void_p) if fmm is not None else None
+        arr[i].levels = levels if fmm is not None else 0
+        arr[i].slices = slices
+        arr[i].m, arr[i].n, arr[i].k = m, n, k
+        arr[i].alpha, arr[i].beta = 1.0, 1.0
+        arr[i].A, arr[i].lda = 256, max(m, 1)
+        arr[i].B, arr[i].ldb = 256, max(k, 1)
+        arr[i].C, arr[i].ldc = 256, max(m, 1)
+        arr[i].format = _fmt(fmt)
+    return int(lib().fmm_gpu_batch_workspace_size(len(items), arr))
+
+
 def batch_problem_workspace_size(m: int, n: int, k: int, fmm: FmmT | None, levels: int, slices: int,
                                  fmt="bf16") -> int:
     """Workspace one problem of this shape needs inside a batch (all of its
-    products at once), from the shape alone: the sizing call reads no operand
-    data, so placeholder addresses stand in for the operands."""
-    arr = (BatchProblem * 1)()
-    arr[0].fmm = ctypes.cast(ctypes.pointer(fmm), ctypes.c_void_p) if fmm is not None else None
-    arr[0].levels = levels if fmm is not None else 0
-    arr[0].slices = slices
-    arr[0].m, arr[0].n, arr[0].k = m, n, k
-    arr[0].alpha, arr[0].beta = 1.0, 1.0
-    arr[0].A, arr[0].lda = 256, max(m, 1)
-    arr[0].B, arr[0].ldb = 256, max(k, 1)
-    arr[0].C, arr[0].ldc = 256, max(m, 1)
-    arr[0].format = _fmt(fmt)
-    return int(lib().fmm_gpu_batch_workspace_size(1, arr))
+    products at once), from the shape alone."""
+    return batch_shapes_workspace_size([(m, n, k, fmm, levels, slices, fmt)])
 
 
 def batch_dgemm(problems, workspace=None, stream=None) -> None:

@@ -26,8 +26,18 @@ Loop (Server.tick):
      (fmm_gpu_set_f64_batch_ctas), which leaves the other SMs to the split
      form's kernels while a long FP64 batch runs.
 
-Faults are handled on the host: a workspace allocation that fails puts the
-batch's requests back at the front of their queue (operands are regenerated
+Memory: the batched path's operands and workspaces are pieces of one device
+arena allocated when the server starts (the budget plus slack), so the loop
+never calls the CUDA allocator; a caching allocator under memory pressure
+frees cached blocks, and cudaFree waits for every kernel on the device, long
+FP64 batches included, which stalled the whole loop. FP64 requests take
+their pieces from the top of the arena and split requests from the bottom,
+so the long-lived FP64 pieces do not fragment the room split batches cycle
+through.
+
+Faults are handled on the host: a workspace allocation that fails (or finds
+no contiguous piece of the arena) puts the batch's requests back at the
+front of their queue (operands are regenerated
 from the request's seed when it is launched again) and the loop goes on;
 cancel(rid) withdraws a waiting request, or drops an admitted one's result
 when its batch completes.
@@ -75,6 +85,7 @@ class Request:
     cancelled: bool = False
     _A: object = field(default=None, repr=False)
     _B: object = field(default=None, repr=False)
+    _offs: object = field(default=None, repr=False)   # arena offsets of A, B, C on the batched path
 
     @property
     def latency(self) -> float | None:
@@ -89,6 +100,67 @@ def _colmajor_rand(torch, rows, cols, gen, dev):
     """uniform [-1, 1) column-major (rows x cols) tensor from a seeded
     generator (2u - 1 in place: no full-size temporaries)"""
     return torch.rand((cols, rows), generator=gen, device=dev, dtype=torch.float64).mul_(2).sub_(1).t()
+
+
+def _colmajor_rand_into(torch, view, gen):
+    """_colmajor_rand's values written into `view`, a column-major (rows x
+    cols) view of preallocated device memory: the same generator draws, so
+    the same bits"""
+    torch.rand(tuple(view.t().shape), generator=gen, dtype=torch.float64, out=view.t())
+    view.mul_(2).sub_(1)
+    return view
+
+
+class _Arena:
+    """One device allocation, handed out in 256-byte aligned pieces (first fit
+    over an ordered free list, neighbours merged on release). The server takes
+    every request's operands and every batch's workspace from it, so serving
+    never calls the CUDA allocator: a caching allocator under memory pressure
+    frees cached blocks, and cudaFree waits for every kernel on the device,
+    a long FP64 batch included."""
+
+    def __init__(self, torch, dev, nbytes: int):
+        self.torch = torch
+        # a multiple of 256 bytes, so pieces taken from the top are as aligned as those from the bottom
+        self.buf = torch.empty(max(nbytes, 256) // 256 * 256, dtype=torch.uint8, device=dev)
+        self.free = [(0, self.buf.numel())]   # (offset, size), ordered by offset
+
+    def alloc(self, nbytes: int, from_top: bool = False):
+        """first fit from the bottom, or (from_top) from the top, of the arena"""
+        need = (max(nbytes, 1) + 255) // 256 * 256
+        order = range(len(self.free) - 1, -1, -1) if from_top else range(len(self.free))
+        for x in order:
+            off, size = self.free[x]
+            if size < need:
+                continue
+            if size == need:
+                del self.free[x]
+                return off, need
+            if from_top:
+                self.free[x] = (off, size - need)
+                return off + size - need, need
+            self.free[x] = (off + need, size - need)
+            return off, need
+        return None
+
+    def release(self, off: int, size: int):
+        import bisect
+        x = bisect.bisect_left(self.free, (off, 0))
+        self.free.insert(x, (off, size))
+        # merge with the following and the preceding piece
+        if x + 1 < len(self.free) and off + size == self.free[x + 1][0]:
+            self.free[x] = (off, size + self.free[x + 1][1])
+            del self.free[x + 1]
+        if x > 0 and self.free[x - 1][0] + self.free[x - 1][1] == off:
+            self.free[x - 1] = (self.free[x - 1][0], self.free[x - 1][1] + self.free[x][1])
+            del self.free[x]
+
+    def bytes_view(self, off: int, nbytes: int):
+        return self.buf[off:off + nbytes]
+
+    def matrix(self, off: int, rows: int, cols: int):
+        """a column-major rows x cols float64 view at offset off"""
+        return self.buf[off:off + 8 * rows * cols].view(self.torch.float64).view(cols, rows).t()
 
 
 def _bucket(x: int, lo: int = 128) -> int:
@@ -137,12 +209,16 @@ class Server:
             hbm_budget = int(free * 0.8)
         self.budget = hbm_budget
         self.fp64_budget = int(hbm_budget * fp64_hbm_share)
+        # operands and workspaces of the batched path live in one allocation of the budget (plus room
+        # for the 256-byte rounding of each piece and a batch's own tables)
+        self.arena = _Arena(torch, self.dev, hbm_budget + (64 << 20))
         self.used = 0
         self.used_fp64 = 0
         self.peak_used = 0
         self.tuner = tuner or _tune.Tuner()
         self.streams = [torch.cuda.Stream(device=self.dev) for _ in range(streams)]
         self.fp64_stream = torch.cuda.Stream(device=self.dev)
+        self.copy_stream = torch.cuda.Stream(device=self.dev)   # results kept out of the arena
         sms = torch.cuda.get_device_properties(self.dev).multi_processor_count
         # the FP64 batch kernel holds one SM per CTA against the split GEMM (their shared memory does not fit
         # together): an eighth of the SMs by default
@@ -154,7 +230,7 @@ class Server:
         self.graph_slots = graph_slots
         self.queues: dict[str, collections.deque[Request]] = {"split": collections.deque(),
                                                               "fp64": collections.deque()}
-        self.inflight: list[tuple[object, list[Request], object]] = []   # (event, requests, workspace)
+        self.inflight: list[tuple[object, list[Request], list]] = []   # (event, requests, arena pieces)
         self.completed: list[Request] = []
         self.cancelled: list[Request] = []
         self.alloc_hook = alloc_hook          # called before each workspace allocation; may raise (fault injection)
@@ -249,18 +325,24 @@ class Server:
             self.used_fp64 -= r.footprint
         r._A = r._B = None
 
-    def _workspace(self, nbytes: int):
-        if self.alloc_hook is not None:
-            self.alloc_hook(nbytes)
-        return self.torch.empty(max(nbytes, 256), dtype=self.torch.uint8, device=self.dev)
+    def _piece(self, nbytes: int, pieces: list, from_top: bool = False):
+        got = self.arena.alloc(nbytes, from_top)
+        if got is None:
+            for off, size in pieces:
+                self.arena.release(off, size)
+            pieces.clear()
+            raise MemoryError(f"no contiguous {nbytes} bytes free in the serving arena")
+        pieces.append(got)
+        return got[0]
 
     def tick(self) -> int:
         """One scheduling round; returns the number of requests launched."""
         # 1. completions
         still = []
         now = time.perf_counter()
-        for ev, reqs, ws in self.inflight:
+        for ev, reqs, pieces in self.inflight:
             if ev.query():
+                kept = False
                 for r in reqs:
                     self._release(r)
                     if r.cancelled:
@@ -270,9 +352,17 @@ class Server:
                     r.done = now
                     if not self.keep_results:
                         r.C = None
+                    elif r.path == "batch":
+                        with self.torch.cuda.stream(self.copy_stream):
+                            r.C = r.C.clone()   # out of the arena, whose piece is reused next
+                        kept = True
                     self.completed.append(r)
+                if kept:
+                    self.copy_stream.synchronize()
+                for off, size in pieces:
+                    self.arena.release(off, size)
             else:
-                still.append((ev, reqs, ws))
+                still.append((ev, reqs, pieces))
         self.inflight = still
         # 2. admission per form, 3. launch
         launched = 0
@@ -282,7 +372,7 @@ class Server:
                 continue
             st = self.fp64_stream if form == "fp64" else self.streams[next(self._next_stream)]
             try:
-                ev, ws = self._launch(batch, st, form)
+                ev, pieces = self._launch(batch, st, form)
             except (MemoryError, RuntimeError) as e:
                 if not isinstance(e, MemoryError) and "out of memory" not in str(e).lower():
                     raise
@@ -294,35 +384,56 @@ class Server:
                     self.queues[form].appendleft(r)
                 self.alloc_failures += 1
                 continue
-            self.inflight.append((ev, batch, ws))
+            self.inflight.append((ev, batch, pieces))
             self.launched_batches += 1
             launched += len(batch)
         return launched
 
     def _launch(self, batch, st, form):
-        """operands, workspace (the one allocation that may fail: nothing has
-        been launched but operand generation when it does), graph requests,
-        then one batched call for the rest"""
+        """operands and workspace from the arena (the allocations that may
+        fail, before anything is launched: the pieces taken are returned),
+        graph requests, then one batched call for the rest"""
         torch = self.torch
+        pieces: list = []
+        direct, graphs = [], []
+        for r in batch:
+            bucket = self._graph_bucket(r)
+            if bucket is not None:
+                graphs.append((r, bucket))
+                continue
+            # FP64 requests run long: their pieces come from the top of the arena, so the holes split batches
+            # leave at the bottom merge back into large pieces
+            top = form == "fp64"
+            r._offs = (self._piece(8 * r.m * r.k, pieces, top), self._piece(8 * r.k * r.n, pieces, top),
+                       self._piece(8 * r.m * r.n, pieces, top))
+            direct.append(r)
+        ws_off, arr, wsb = None, None, 0
+        if direct:
+            # the batch's workspace size from its shapes and plans alone (host-only sizing)
+            wsb = max(self.fmm.batch_shapes_workspace_size(
+                [(r.m, r.n, r.k, self._alg(r.plan.alg), r.plan.levels, r.plan.slices, r.plan.fmt) for r in direct]), 256)
+            if self.alloc_hook is not None:
+                try:
+                    self.alloc_hook(wsb)
+                except BaseException:
+                    for off, size in pieces:
+                        self.arena.release(off, size)
+                    raise
+            ws_off = self._piece(wsb, pieces, form == "fp64")
         with torch.cuda.stream(st):
-            direct, graphs = [], []
-            for r in batch:
-                bucket = self._graph_bucket(r)
-                if bucket is not None:
-                    graphs.append((r, bucket))
-                    continue
+            for r in direct:
                 g = torch.Generator(device=self.dev).manual_seed(r.seed)
-                r._A = _colmajor_rand(torch, r.m, r.k, g, self.dev)
-                r._B = _colmajor_rand(torch, r.k, r.n, g, self.dev)
-                r.C = _colmajor_rand(torch, r.m, r.n, g, self.dev)
+                oa, ob, oc = r._offs
+                r._A = _colmajor_rand_into(torch, self.arena.matrix(oa, r.m, r.k), g)
+                r._B = _colmajor_rand_into(torch, self.arena.matrix(ob, r.k, r.n), g)
+                r.C = _colmajor_rand_into(torch, self.arena.matrix(oc, r.m, r.n), g)
                 r.path = "batch"
-                direct.append(r)
-            ws, arr = None, None
+            ws = None
             if direct:
                 probs = [{"A": r._A, "B": r._B, "C": r.C, "fmm": self._alg(r.plan.alg), "levels": r.plan.levels,
                           "slices": r.plan.slices, "fmt": r.plan.fmt} for r in direct]
                 arr = self.fmm.make_batch(probs)
-                ws = self._workspace(self.fmm.batch_workspace_size(arr))
+                ws = self.arena.bytes_view(ws_off, wsb)
             for r, bucket in graphs:
                 self._run_graph(r, bucket, torch.Generator(device=self.dev).manual_seed(r.seed), st)
             if direct:
@@ -336,7 +447,7 @@ class Server:
                     self.fmm.batch_dgemm(arr, workspace=ws, stream=st)
             ev = torch.cuda.Event()
             ev.record(st)
-        return ev, ws
+        return ev, pieces
 
     def _run_graph(self, r: Request, bucket, gen, st):
         """operands into a zero-padded slot of the bucket, one graph launch,
@@ -395,6 +506,7 @@ class Server:
 
     def close(self):
         self.torch.cuda.synchronize()
+        self.arena = None
         for f in self._algs.values():
             self.fmm.free_fmm(f)
         self._algs.clear()

@@ -1,0 +1,87 @@
+"""Host-side bookkeeping of the server (no GPU): the device arena that holds
+the batched path's operands and workspaces, so serving never calls the CUDA
+allocator (whose cudaFree, under memory pressure, waits for every kernel on
+the device)."""
+import random
+
+from fmm_blis_gb300 import serve
+
+
+class _Buf:
+    def __init__(self, n):
+        self.n = n
+
+    def numel(self):
+        return self.n
+
+
+class _FakeTorch:
+    uint8 = "uint8"
+    float64 = "float64"
+
+    def empty(self, n, dtype, device):
+        return _Buf(n)
+
+
+def test_arena_first_fit_and_merge():
+    a = serve._Arena(_FakeTorch(), None, 1 << 20)
+    x = a.alloc(1000)
+    y = a.alloc(3000)
+    z = a.alloc(1)
+    assert x == (0, 1024) and y == (1024, 3072) and z == (4096, 256)   # 256-byte pieces, first fit
+    a.release(*y)
+    assert a.alloc(2000) == (1024, 2048)          # the freed hole is reused
+    a.release(1024, 2048)
+    a.release(*x)
+    a.release(*z)
+    assert a.free == [(0, 1 << 20)]               # neighbours merged back into one piece
+    assert a.alloc((1 << 20) + 1) is None         # larger than the arena
+
+
+def test_arena_random_alloc_release_keeps_pieces_disjoint():
+    rng = random.Random(5)
+    size = 1 << 22
+    a = serve._Arena(_FakeTorch(), None, size)
+    held = []
+    for _ in range(2000):
+        if held and rng.random() < 0.45:
+            a.release(*held.pop(rng.randrange(len(held))))
+        else:
+            got = a.alloc(rng.randint(1, 200_000), from_top=rng.random() < 0.3)
+            if got is not None:
+                held.append(got)
+        spans = sorted(held + a.free)
+        assert sum(s for _o, s in spans) == size                         # nothing lost
+        assert all(o1 + s1 <= o2 for (o1, s1), (o2, _s2) in zip(spans, spans[1:]))   # nothing overlaps
+    for p in held:
+        a.release(*p)
+    assert a.free == [(0, size)]
+
+
+def test_arena_top_pieces_keep_the_bottom_contiguous():
+    """Pieces taken from the top (long-running requests) leave the bottom of
+    the arena one contiguous piece for the short-lived ones."""
+    a = serve._Arena(_FakeTorch(), None, 1 << 20)
+    low = [a.alloc(10_000) for _ in range(5)]
+    top = a.alloc(100_000, from_top=True)
+    assert top[0] + top[1] == 1 << 20
+    for p in low:
+        a.release(*p)
+    assert a.free[0] == (0, (1 << 20) - top[1])
+
+
+def test_arena_pieces_are_256_byte_aligned():
+    """Every piece, from either end, starts on a 256-byte boundary (the
+    operands are viewed as float64 and handed to kernels), whatever the
+    requested arena size."""
+    rng = random.Random(7)
+    a = serve._Arena(_FakeTorch(), None, 10_000_003)
+    held = []
+    for _ in range(500):
+        if held and rng.random() < 0.4:
+            a.release(*held.pop(rng.randrange(len(held))))
+        else:
+            got = a.alloc(rng.randint(1, 100_000), from_top=rng.random() < 0.5)
+            if got is not None:
+                assert got[0] % 256 == 0 and got[1] % 256 == 0
+                held.append(got)
