@@ -74,6 +74,13 @@ def test_batch_sizing_needs_no_gpu():
     sizes = [fmm.batch_problem_workspace_size(1000, 900, 800, f, 1, s) for s in (3, 5, 7)]
     assert 0 < sizes[0] < sizes[1] < sizes[2]
     assert fmm.batch_problem_workspace_size(100, 90, 80, None, 0, 5) > 0
+    # a whole batch from its shapes and plans (what the server sizes its arena pieces with): at least
+    # each problem's own workspace, and the FP64 problems' table beside the split problems'
+    shapes = [(1000, 900, 800, f, 1, 5, "bf16"), (300, 200, 700, None, 0, 6, "bf16"), (512, 512, 512, f, 1, 0, "bf16")]
+    whole = fmm.batch_shapes_workspace_size(shapes)
+    assert whole >= max(fmm.batch_problem_workspace_size(*p) for p in shapes)
+    assert whole == fmm.batch_shapes_workspace_size(list(shapes))
+    assert fmm.batch_shapes_workspace_size([]) >= 0
 
 
 def test_slice_format_choice():
