@@ -62,3 +62,26 @@ def test_single_rank_helpers_need_no_process_group():
     import bench
     bench.rank_barrier(1)
     assert bench.rank_max(3.25, 1, "cpu") == 3.25
+
+
+def test_reference_arm_reports_timed_samples():
+    """The reference arm times bounded samples of the workload on the host
+    cores: its steps' measured time fits in the run's wall time, and its value
+    is the sample's share of 2mnk over that time."""
+    import json
+    import time
+    env = dict(os.environ)
+    for key in ("RANK", "WORLD_SIZE", "LOCAL_RANK"):
+        env.pop(key, None)
+    t0 = time.perf_counter()
+    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--n", "256", "--steps", "3",
+                        "--warmup", "1"], env=env, capture_output=True, text=True, timeout=300)
+    wall = time.perf_counter() - t0
+    assert r.returncode == 0, r.stderr
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["steps"] == 3 and line["warmup"] == 1
+    assert (line["steps"] + line["warmup"]) * line["ms_per_step"] / 1e3 <= wall
+    P, R = line["config"]["sample_products"], line["config"]["products"]
+    assert 1 <= P <= R
+    assert abs(line["value"] - 2.0 * 256 ** 3 * P / R / (line["ms_per_step"] / 1e3) / 1e12) <= 1e-9 * line["value"]
+    assert line["e2e"]["value"] == line["value"] and line["cpu_baseline"]["kind"] == "port"
