@@ -266,7 +266,17 @@ class Server:
         p = r.plan
         if p.form != "split" or p.levels != 0 or max(r.m, r.n, r.k) > self.graph_max_dim:
             return None
-        return (_bucket(r.m), _bucket(r.n), _bucket(r.k), p.slices, p.fmt)
+        bucket = (_bucket(r.m), _bucket(r.n), _bucket(r.k), p.slices, p.fmt)
+        if bucket not in self._slots and self._fp64_in_flight():
+            # capturing a new bucket's graph synchronizes the whole device (torch.cuda.graph does, before
+            # capture), which would hold the loop until the FP64 batch in flight ends, tens of seconds for a
+            # large one: the request takes the batched path instead, which gives the same bits
+            return None
+        return bucket
+
+    def _fp64_in_flight(self) -> bool:
+        """an FP64 batch is still running (batches hold requests of one form)"""
+        return any(reqs and reqs[0].plan.form == "fp64" for _ev, reqs, _pieces in self.inflight)
 
     # -------------------------------------------------------------- API
     def submit(self, r: Request) -> Request:

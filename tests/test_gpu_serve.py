@@ -64,22 +64,26 @@ def test_served_mix_equals_alone_and_direct(fmm, torch_cuda):
     srv.close()
     assert len(done) == len(reqs)
     assert srv.launched_batches >= 2
-    paths = {r.path for r in reqs}
-    assert paths == {"batch", "graph"}, paths
+    # in the mix, small split requests whose size bucket has no graph yet take the batched path while an FP64
+    # batch runs; alone they take the graph path: both give the direct call's bits
+    assert {r.path for r in reqs} <= {"batch", "graph"}
     assert any(r.plan.levels > 0 for r in reqs)
     mixed = {r.seed: host(r.C) for r in reqs}
     algs = {}
+    alone_paths = set()
     try:
         for r in mix(5, 30):
             alone = serve.Server(streams=1, tuner=tuner)
             alone.run([serve.Request(r.m, r.n, r.k, r.form, r.target_rel_err, r.seed, 0.0)])
             (a,) = alone.completed
             alone.close()
+            alone_paths.add(a.path)
             assert np.array_equal(host(a.C), mixed[r.seed]), (r.m, r.n, r.k, r.form, a.path)
             assert np.array_equal(direct(fmm, torch, a, algs), mixed[r.seed]), (r.m, r.n, r.k, r.form, a.path)
     finally:
         for f in algs.values():
             fmm.free_fmm(f)
+    assert alone_paths == {"batch", "graph"}, alone_paths
     assert fmm.take_device_error() == 0
 
 

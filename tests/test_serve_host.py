@@ -85,3 +85,34 @@ def test_arena_pieces_are_256_byte_aligned():
             if got is not None:
                 assert got[0] % 256 == 0 and got[1] % 256 == 0
                 held.append(got)
+
+
+def test_new_graph_buckets_wait_while_an_fp64_batch_runs():
+    """A request whose size bucket has no captured graph yet takes the batched
+    path while an FP64 batch is in flight (capturing would synchronize the
+    whole device and hold the loop until that batch ends); a bucket already
+    captured keeps its graph path, and with no FP64 batch in flight a new
+    bucket is captured as before."""
+    from fmm_blis_gb300 import tune
+    srv = object.__new__(serve.Server)
+    srv.graph_max_dim = 1024
+    srv._slots = {}
+    srv.inflight = []
+    t = tune.Tuner()
+
+    def req(m, n, k, form="split"):
+        r = serve.Request(m, n, k, form=form)
+        r.plan = t.plan(m, n, k, form, 1e-10)
+        return r
+
+    small = req(200, 300, 250)
+    assert small.plan.levels == 0
+    key = srv._graph_bucket(small)
+    assert key == (256, 512, 256, small.plan.slices, small.plan.fmt)   # no FP64 in flight: graph path
+    srv.inflight = [(None, [req(4096, 4096, 4096, "fp64")], [])]
+    assert srv._graph_bucket(small) is None                              # new bucket, FP64 running: batched
+    srv._slots[key] = ["captured"]
+    assert srv._graph_bucket(small) == key                               # captured bucket: graph path
+    srv.inflight = [(None, [req(900, 900, 900)], [])]
+    assert srv._graph_bucket(req(100, 100, 100)) is not None             # only split work in flight
+    assert srv._graph_bucket(req(2000, 300, 300)) is None                # beyond the graph sizes
