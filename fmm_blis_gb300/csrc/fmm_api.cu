@@ -156,7 +156,7 @@ std::vector<std::vector<int>> g_brent_ok;   /* algorithms already verified, seri
 }  // namespace
 
 /* The Brent check, once per distinct algorithm of the process (a flat
- * two-level algorithm has up to 16.7 M equations; calls reuse the verdict). */
+ * two-level algorithm has up to 16.7 M equations; calls reuse the result). */
 static int brent_checked(const fmm_t* f)
 {
     const size_t a = (size_t)f->m_tilde * f->k_tilde * f->R, b = (size_t)f->k_tilde * f->n_tilde * f->R,
