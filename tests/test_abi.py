@@ -68,3 +68,24 @@ def test_split_host_gen_rejects_bad_arguments(fmm):
     bad = (1.0, p, 0, 1, p, 4, 1, 1.0, p, 4, 1, 4, 4, 4, f, 1, 6, 0)                   # row stride 0
     assert L.fmm_gpu_split_strassen_ab_gen(*bad) == 1
     assert L.fmm_gpu_split_strassen_ab_gen(1.0, p, 4, 1, p, 4, 1, 1.0, p, 4, 1, -1, 4, 4, f, 1, 6, 0) == 1
+
+
+def test_host_alloc_arguments_and_missing_gpu(fmm):
+    """fmm_gpu_host_alloc checks its arguments before touching the GPU; where
+    no GPU is present it fails with a status (no memory is handed out), and
+    fmm.host_empty raises instead of returning unpinned memory."""
+    import ctypes
+
+    import pytest
+    L = fmm.lib()
+    p = ctypes.c_void_p(1234)
+    assert L.fmm_gpu_host_alloc(0, ctypes.byref(p)) == 1 and not p.value       # zero bytes
+    assert L.fmm_gpu_host_alloc(4096, None) == 1                              # no result pointer
+    assert L.fmm_gpu_host_free(None) == 0                                     # freeing NULL is a no-op
+    assert L.fmm_gpu_host_free(ctypes.c_void_p(4096)) == 1                    # not from fmm_gpu_host_alloc
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present: the allocation itself is covered by the GPU tests")
+    assert L.fmm_gpu_host_alloc(1 << 20, ctypes.byref(p)) == 5 and not p.value
+    with pytest.raises(RuntimeError):
+        fmm.host_empty(16, 16)
