@@ -116,3 +116,19 @@ def test_new_graph_buckets_wait_while_an_fp64_batch_runs():
     srv.inflight = [(None, [req(900, 900, 900)], [])]
     assert srv._graph_bucket(req(100, 100, 100)) is not None             # only split work in flight
     assert srv._graph_bucket(req(2000, 300, 300)) is None                # beyond the graph sizes
+
+
+def test_operands_into_preallocated_memory_equal_fresh_ones():
+    """The arena path writes a request's operands into preallocated memory
+    with the same generator draws as a fresh allocation (CPU generator here;
+    the GPU tests check the served bits against the direct calls)."""
+    import torch
+    rows, cols = 37, 23
+    g1 = torch.Generator().manual_seed(11)
+    fresh = serve._colmajor_rand(torch, rows, cols, g1, torch.device("cpu"))
+    buf = torch.empty(8 * rows * cols + 256, dtype=torch.uint8)
+    view = buf[256:256 + 8 * rows * cols].view(torch.float64).view(cols, rows).t()
+    g2 = torch.Generator().manual_seed(11)
+    into = serve._colmajor_rand_into(torch, view, g2)
+    assert into.shape == (rows, cols) and into.stride() == (1, rows)
+    assert torch.equal(into, fresh)
